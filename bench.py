@@ -1,0 +1,366 @@
+"""Benchmark: marching-cubes extraction of the 512^3 fused TSDF volume.
+
+Workload (the 512^3 fusion configuration): a 512^3 short2 volume over a 3 m
+cube (trunc 0.03 m) built by integrating 60 ray-cast 640x480 depth frames of a
+seeded scene (20 spheres + boxes, sigma 2 mm noise) with this library's
+integrate kernel; then one step = one full extraction (classify, scan,
+generate with fused normals) of that volume into preallocated device buffers.
+The volume (512 MiB) is larger than L2 (129 MB), so no flush is needed
+between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Prints one JSON line (rank 0).  With torchrun and N > 1 every rank extracts
+its own replica (the path has no exchange step), value = all ranks' voxels
+/ max-over-ranks time.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+N_VOX = 512
+EXTENT = 3.0
+TRUNC = 0.03
+N_FRAMES = 60
+W, H = 640, 480
+FX = FY = 525.0
+CX, CY = 319.5, 239.5
+METRIC = "512^3 MC extraction throughput (Gvoxels/s)"
+UNIT = "Gvoxels/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=N_VOX, help="volume edge (default 512)")
+    ap.add_argument("--frames", type=int, default=N_FRAMES)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+# ---------------------------------------------------------------------------
+# clocks sampler (nvidia-smi during the timed region)
+# ---------------------------------------------------------------------------
+class Clocks:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True,
+                                     timeout=5).stdout.strip()
+                if out:
+                    self.rows.append([x.strip() for x in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for i, nm in enumerate(names):
+                if len(r) > 5 + i and r[5 + i].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+# ---------------------------------------------------------------------------
+# workload construction
+# ---------------------------------------------------------------------------
+def build_volume(mcg, synthetic, torch, n, frames, seed=0):
+    scene = synthetic.FusionScene(seed=seed, extent=EXTENT)
+    v = mcg.voxel_new((n, n, n), TRUNC, TRUNC, EXTENT / n)
+    k = mcg.intrinsic(FX, FY, CX, CY)
+    t_int = 0.0
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for i in range(frames):
+        R, t = scene.pose(i, frames)
+        mm = scene.depth_frame(R, t, w=W, h=H, fx=FX, fy=FY, cx=CX, cy=CY, seed=seed * 1000 + i, device="cuda")
+        d = synthetic.mm_to_u16_bits(mm)
+        ev0.record()
+        m, _, _ = mcg.depth_to_maps(d, k, vertex=False, normal=False)
+        mcg.volumetric_integration(v, k, mcg.extrinsic(R, t), m)
+        ev1.record()
+        torch.cuda.synchronize()
+        t_int += ev0.elapsed_time(ev1) * 1e-3
+    return v, {"frames": frames, "integrate_voxels_per_s": n ** 3 * frames / t_int if t_int else None,
+               "integrate_ms_per_frame": 1e3 * t_int / max(frames, 1)}
+
+
+def cpu_baseline(orc, vol_np, cell, target_s=10.0):
+    """Oracle (FP32 mirror) on a z-slab sample of the same volume, all host
+    threads; voxels/s scaled to Gvoxels/s."""
+    nthreads = orc.max_threads()
+    nz = vol_np.shape[0]
+    slab = 16
+    t0 = time.perf_counter()
+    sub = np.ascontiguousarray(vol_np[:slab + 1])
+    orc.mc_extract(sub, cell, normals=True, vi2vox=False, ver_voxel=False, tri_cube=False, nthreads=nthreads)
+    dt = time.perf_counter() - t0
+    # grow the sample towards target_s of CPU work
+    z0 = nz // 2 - slab
+    est = dt / slab
+    slab2 = int(min(nz - 1, max(slab, target_s / max(est, 1e-6))))
+    z0 = max(0, min(z0, nz - 1 - slab2))
+    sub = np.ascontiguousarray(vol_np[z0:z0 + slab2 + 1])
+    t0 = time.perf_counter()
+    out = orc.mc_extract(sub, cell, normals=True, vi2vox=False, ver_voxel=False, tri_cube=False, nthreads=nthreads)
+    dt = time.perf_counter() - t0
+    vox = sub.shape[1] * sub.shape[2] * slab2
+    return {"value": vox / dt / 1e9, "unit": UNIT, "cores": nthreads, "kind": "port",
+            "sample": "oracle FP32-mirror extraction (classify+scan+generate+normals) of z-slab [%d, %d) "
+                      "of the 512^3 fused volume, %d triangles, %.1f s" % (z0, z0 + slab2, len(out["soup"]) // 3, dt)}
+
+
+def run_reference(args):
+    """--impl reference: the reference has no CPU marching cubes (MyMarchingCube.h
+    is a declaration only); its algorithm restated in C (oracle/) runs on all
+    host cores over bounded samples of the same workload."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    import torch
+    import oracle as orc
+    import marching_cube_gb300 as mcg
+    from marching_cube_gb300 import synthetic
+    orc.build()
+    cfg = {"workload": "mc_extract_512_fusion", "volume": [args.n] * 3, "voxel": "short2",
+           "outputs": "soup+normals", "frames_integrated": args.frames}
+    if torch.cuda.is_available():
+        v, _ = build_volume(mcg, synthetic, torch, args.n, args.frames)
+        vol_np = v.data.cpu().numpy()
+        cell = v.grid_s
+    else:
+        vol_np = synthetic.sphere_volume(args.n, radius=args.n * 0.3, trunc=5.0)
+        cell = EXTENT / args.n
+    nthreads = orc.max_threads()
+    vals = []
+    slab = 32
+    for i in range(args.warmup + args.steps):
+        z0 = (i * slab) % max(1, vol_np.shape[0] - slab - 1)
+        sub = np.ascontiguousarray(vol_np[z0:z0 + slab + 1])
+        t0 = time.perf_counter()
+        orc.mc_extract(sub, cell, normals=True, vi2vox=False, ver_voxel=False, tri_cube=False, nthreads=nthreads)
+        dt = time.perf_counter() - t0
+        if i >= args.warmup:
+            vals.append(sub.shape[1] * sub.shape[2] * slab / dt / 1e9)
+    value = float(np.median(vals))
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": cfg,
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
+                             "sample": "each step: oracle extraction of a 32-slice z-slab of the volume"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    rank, world, local = dist_env()
+    import torch
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    import marching_cube_gb300 as mcg
+    from marching_cube_gb300 import synthetic
+    dev = torch.cuda.current_device()
+
+    v, integ = build_volume(mcg, synthetic, torch, args.n, args.frames, seed=0)
+    n = args.n
+    vox = n ** 3
+    cell = v.grid_s
+    ctx = mcg.Context(dev)
+    stream = torch.cuda.current_stream()
+
+    # size the outputs from one counting pass
+    mesh = mcg.extract(v.data, cell, normals=True, ctx=ctx)
+    nvert = mesh.num_vertices
+    counts = dict(mesh.counts)
+    del mesh
+    cap = nvert
+    soup = torch.empty((cap, 28), dtype=torch.uint8, device="cuda")
+    nrm = torch.empty((cap, 3), dtype=torch.float32, device="cuda")
+    outs = {"soup": soup, "normals": nrm}
+
+    import ctypes
+    from marching_cube_gb300 import _capi
+    cv = _capi.Volume(v.data.data_ptr(), n, n, n, 0, float(cell))
+    mo = _capi.MeshOut(soup.data_ptr(), nrm.data_ptr(), None, None, None, cap)
+    s = ctypes.c_void_p(stream.cuda_stream)
+    lib = mcg._lib
+
+    def step(ev=None):
+        if ev is not None:
+            ev[0].record(stream)
+        ctx.check(lib.mcg_mc_classify(ctx.handle, ctypes.byref(cv), s), "classify")
+        if ev is not None:
+            ev[1].record(stream)
+        ctx.check(lib.mcg_mc_generate(ctx.handle, ctypes.byref(cv), ctypes.byref(mo), s), "generate")
+        if ev is not None:
+            ev[2].record(stream)
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with Clocks(dev) as clk:
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        for i in range(args.steps):
+            step(evs[i])
+        t1.record(stream)
+        torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    total_ms = t0.elapsed_time(t1)
+    cls_ms = float(np.mean([e[0].elapsed_time(e[1]) for e in evs]))
+    gen_ms = float(np.mean([e[1].elapsed_time(e[2]) for e in evs]))
+    c = mcg.counts(ctx)
+    assert c["status"] == 0 and c["vertices"] == nvert
+    if world > 1:
+        tt = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(tt.item())
+    ms_per_step = total_ms / args.steps
+    value = vox * world / (ms_per_step * 1e-3) / 1e9
+
+    # ---- roofline --------------------------------------------------------
+    peaks = {}
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except Exception:
+        pass
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    ntri = counts["triangles"]
+    # classify: every voxel read once (4 B) + 8 B per brick of counts
+    bricks = ((n - 2) // 32 + 1) * ((n - 2) // 8 + 1) ** 2
+    cls_bytes = 4 * vox + 8 * bricks
+    # generate: active bricks' 32x8x8 voxels (4 B) + soup (28 B) + normals (12 B) per vertex
+    out_bytes = nvert * (28 + 12)
+    gen_bytes = out_bytes + 4 * 2048 * c["active_bricks"]
+    dominant = "classify" if cls_ms >= gen_ms else "generate"
+    if dominant == "classify":
+        achieved = cls_bytes / (cls_ms * 1e-3) / 1e9
+    else:
+        achieved = gen_bytes / (gen_ms * 1e-3) / 1e9
+    alg_bytes = 4 * vox + out_bytes
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                "traffic": None, "kernel": "mc_classify_kernel" if dominant == "classify" else "mc_generate_kernel",
+                "peak_source": peak_src,
+                "whole_step": {"alg_bytes": alg_bytes, "achieved_gbs": alg_bytes / (ms_per_step * 1e-3) / 1e9,
+                               "frac": alg_bytes / (ms_per_step * 1e-3) / 1e9 / hbm},
+                "classify_ms": cls_ms, "generate_ms": gen_ms}
+
+    # ---- e2e: host volume in, host mesh out, through the C ABI ------------
+    e2e = None
+    try:
+        h_vol = torch.empty(v.data.shape, dtype=v.data.dtype, pin_memory=True)
+        h_vol.copy_(v.data)
+        h_soup = torch.empty((cap, 28), dtype=torch.uint8, pin_memory=True)
+        h_nrm = torch.empty((cap, 3), dtype=torch.float32, pin_memory=True)
+        d_vol = torch.empty_like(v.data)
+        cv2 = _capi.Volume(d_vol.data_ptr(), n, n, n, 0, float(cell))
+        reps = max(3, min(args.steps, 10))
+        for i in range(reps + 2):
+            if i == 2:
+                torch.cuda.synchronize()
+                ta = time.perf_counter()
+            d_vol.copy_(h_vol, non_blocking=True)
+            ctx.check(lib.mcg_mc_classify(ctx.handle, ctypes.byref(cv2), s), "classify")
+            ctx.check(lib.mcg_mc_generate(ctx.handle, ctypes.byref(cv2), ctypes.byref(mo), s), "generate")
+            h_soup.copy_(soup, non_blocking=True)
+            h_nrm.copy_(nrm, non_blocking=True)
+            torch.cuda.synchronize()
+        tb = time.perf_counter()
+        e2e_s = (tb - ta) / reps
+        e2e = {"value": vox / e2e_s / 1e9, "unit": UNIT, "h2d_bytes_per_step": int(h_vol.numel() * 2),
+               "d2h_bytes_per_step": int(cap * 40), "ms_per_step": e2e_s * 1e3}
+        del h_vol, h_soup, h_nrm, d_vol
+    except Exception as ex:  # pragma: no cover
+        e2e = {"value": None, "unit": UNIT, "error": str(ex)}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        try:
+            import oracle as orc
+            orc.build()
+            cpu = cpu_baseline(orc, v.data.cpu().numpy(), cell)
+        except Exception as ex:  # pragma: no cover
+            cpu = {"value": None, "error": str(ex)}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int16", "data": "synthetic",
+        "config": {"workload": "mc_extract_512_fusion", "volume": [n, n, n], "voxel": "short2",
+                   "frames_integrated": args.frames, "outputs": "soup(vertex_voxel)+normals",
+                   "triangles": ntri, "occupied_cubes": counts["occupied"], "l2": "inputs larger than L2",
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+        "clocks": clk.summary(), "gpu_launches": 3 * args.steps,
+        "triangles_per_s": ntri * world / (ms_per_step * 1e-3),
+        "integrate": integ,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,168 @@
+/*
+ * mcg.h -- C ABI of the GB300 TSDF -> mesh library (libmcg.so).
+ *
+ * Plain C: pointers, sizes and status codes only.  Every entry point takes
+ * an explicit CUDA stream (mcg_stream_t == cudaStream_t, NULL = legacy
+ * default stream) and keeps all state in an mcg_context, so calls on
+ * different contexts are independent.  Device pointers are CUDA device (or
+ * managed) allocations; "host" pointers are ordinary host memory.
+ *
+ * Each declaration names the reference interface it replaces (paths are
+ * relative to the reference project root; mc.cu = cu_marching_cubes_v1.cu,
+ * kf.cu / kf.h = cu_kinect_fusion_v1.cu / .h).  The reference aborts the
+ * process on CUDA errors (cu_device.h checkCudaErrors); this ABI returns a
+ * status instead.
+ */
+#ifndef MCG_H
+#define MCG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MCG_VERSION 100
+
+typedef struct CUstream_st *mcg_stream_t; /* identical to cudaStream_t */
+typedef struct mcg_context mcg_context;   /* opaque per-instance state */
+
+typedef enum mcg_status {
+    MCG_OK = 0,
+    MCG_ERR_INVALID_ARG = 1, /* bad pointer, size or combination of arguments */
+    MCG_ERR_CAPACITY = 2,    /* output larger than the buffers given; counts hold the need */
+    MCG_ERR_CUDA = 3,        /* a CUDA call failed; mcg_last_cuda_error() has the code */
+    MCG_ERR_TIMEOUT = 4,     /* a bounded device-side wait expired */
+    MCG_ERR_IO = 5,          /* file could not be opened / read / written */
+    MCG_ERR_FORMAT = 6,      /* malformed RLE stream or file header */
+    MCG_ERR_STATE = 7        /* call order violated (e.g. generate without classify) */
+} mcg_status;
+
+/* voxel storage types */
+enum {
+    MCG_VOXEL_SHORT2 = 0, /* structure.h:14-18 cu_voxel_t {short tsdf; ushort w}, == short2 */
+    MCG_VOXEL_FLOAT2 = 1  /* {float tsdf; float w}: FP32 volume of the differentiable path */
+};
+
+/* structure.h:29-35 vertex_voxel, 28 bytes, byte-compatible */
+typedef struct mcg_vertex_voxel {
+    float x, y, z;        /* ver_pos */
+    int32_t vx, vy, vz;   /* vox_pos = floor(ver_pos / cell - 0.5) */
+    int16_t tsdf, w;      /* voxel vox_pos as stored */
+} mcg_vertex_voxel;
+
+/* cu_geometry_functions.h:96-101 float_camera_intrinsic (fc, cc, dc[5]) */
+typedef struct mcg_intrinsic { float fx, fy, cx, cy; float dc[5]; } mcg_intrinsic;
+/* cu_geometry_functions.h:104-108 float_camera_extrinsic, camera -> global:
+ * r = rotation, column-major (three float3 columns), t = translation */
+typedef struct mcg_extrinsic { float r[9]; float t[3]; } mcg_extrinsic;
+
+/* structure.h:20-27 cu_voxel, minus the truncation fields.  data is a dense
+ * [z][y][x] device array (x fastest, no pitch). */
+typedef struct mcg_volume {
+    const void *data;
+    int32_t nx, ny, nz;
+    int32_t voxel_type; /* MCG_VOXEL_* */
+    float cell;         /* grid_s, voxel edge length */
+} mcg_volume;
+
+/* Outputs of one extraction; every pointer is a device array or NULL.
+ * Soup arrays hold up to capacity_vertices entries (3 per triangle). */
+typedef struct mcg_mesh_out {
+    mcg_vertex_voxel *soup; /* MarchingCubes::run triangles_buffer            */
+    float *soup_normals;    /* float3 per soup vertex (d_voxel_extract_surface_normals) */
+    int32_t *vi2vox;        /* int3 per soup vertex (vertexindex_to_voxel)    */
+    int16_t *ver_voxel;     /* nx*ny*nz shorts: zeroed, then tsdf at each vertex voxel */
+    int64_t *tri_cube;      /* linear id z*nx*ny + y*nx + x of each triangle's cube */
+    int64_t capacity_vertices;
+} mcg_mesh_out;
+
+typedef struct mcg_mesh_counts {
+    int64_t occupied;  /* cubes that emit triangles (getOccupiedVoxels' count) */
+    int64_t triangles;
+    int64_t vertices;  /* soup vertices, 3 * triangles */
+    int64_t active_bricks; /* 32x8x8-cube bricks that emit triangles */
+    int32_t status;    /* MCG_OK, or MCG_ERR_CAPACITY if the last generate was truncated */
+    int32_t reserved;
+} mcg_mesh_counts;
+
+/* ---- context ----------------------------------------------------------- */
+const char *mcg_status_string(int status);
+int mcg_version(void);
+/* replaces the globals of mc.cu:29-51 (volume_size, textures, counters) */
+mcg_status mcg_create(mcg_context **out, int device);
+mcg_status mcg_destroy(mcg_context *ctx);
+int mcg_last_cuda_error(const mcg_context *ctx);
+
+/* ---- voxel init: kf.cu:364-398 (d_voxel_initialize in cu_voxel_new) ----- */
+/* every voxel -> {tsdf = -32766, w = 0} (FLOAT2: {-1, 0}) */
+mcg_status mcg_voxel_init(mcg_context *ctx, void *vol, int32_t voxel_type, int64_t n_voxels,
+                          mcg_stream_t stream);
+
+/* ---- marching cubes: mc.cu:416-467 MarchingCubes::run ------------------- */
+/* Count phase (getOccupiedVoxels mc.cu:185-206 + computeOffsetsAndTotalVertexes
+ * mc.cu:208-225).  Asynchronous; the counts become readable through
+ * mcg_mc_counts once the stream reaches this point. */
+mcg_status mcg_mc_classify(mcg_context *ctx, const mcg_volume *vol, mcg_stream_t stream);
+/* Waits for the last classify/generate on ctx and reports counts. */
+mcg_status mcg_mc_counts(mcg_context *ctx, mcg_mesh_counts *out);
+/* Generation phase (generateTriangles mc.cu:372-396 + normals kf.cu:3236-3242)
+ * over the volume passed to the preceding mcg_mc_classify on this ctx.
+ * Writes at most capacity_vertices soup vertices; the rest is dropped and
+ * mcg_mc_counts reports MCG_ERR_CAPACITY with the full size. */
+mcg_status mcg_mc_generate(mcg_context *ctx, const mcg_volume *vol, const mcg_mesh_out *out,
+                           mcg_stream_t stream);
+/* classify + generate in one call, no host synchronisation */
+mcg_status mcg_mc_extract(mcg_context *ctx, const mcg_volume *vol, const mcg_mesh_out *out,
+                          mcg_stream_t stream);
+/* kf.cu:3227-3242 d_voxel_extract_surface_normal(s) for n arbitrary vertex
+ * records (the normal of ver_pos); normals is float3[n] */
+mcg_status mcg_mc_normals(mcg_context *ctx, const mcg_volume *vol, const mcg_vertex_voxel *verts,
+                          int64_t n, float *normals, mcg_stream_t stream);
+
+/* ---- depth maps: kf.cu:99-151 (d_kinect_depth_to_meter, d_img_meter_to_vertex,
+ * d_img_vertex_to_normal), fused --------------------------------------------- */
+/* depth_mm: uint16 millimetres [h][w] (device).  meter/vertex/normal may be
+ * NULL individually.  Invalid metre = 0, invalid vertex/normal = (0,0,0). */
+mcg_status mcg_depth_to_maps(mcg_context *ctx, const mcg_intrinsic *k, int32_t w, int32_t h,
+                             const uint16_t *depth_mm, float depth_min, float depth_max,
+                             float *meter, float *vertex, float *normal, mcg_stream_t stream);
+/* kf.cu:116-127 on a metre image */
+mcg_status mcg_meter_to_vertex(mcg_context *ctx, const mcg_intrinsic *k, int32_t w, int32_t h,
+                               const float *meter, float *vertex, mcg_stream_t stream);
+/* kf.cu:130-151 */
+mcg_status mcg_vertex_to_normal(mcg_context *ctx, int32_t w, int32_t h, const float *vertex,
+                                float *normal, mcg_stream_t stream);
+
+/* ---- integrate: kf.cu:534-549 _cu_voxel_volumetric_integration ---------- */
+/* Projective TSDF update of vol (device, in place) with one depth frame in
+ * metres (device float [h][w]).  normals: NULL or float3 [h][w] camera-frame
+ * normal map (normal-weighted update).  Colour is not part of the volume. */
+mcg_status mcg_integrate(mcg_context *ctx, void *vol, int32_t voxel_type, int32_t nx, int32_t ny,
+                         int32_t nz, float min_t, float max_t, float grid_s,
+                         const mcg_intrinsic *k, const mcg_extrinsic *e, int32_t w, int32_t h,
+                         const float *depth_m, const float *normals, int32_t is_dynamic,
+                         mcg_stream_t stream);
+
+/* ---- RLE volume codec: kf.cu:1303-1600 ----------------------------------- */
+/* upper bound of the encoded file image size */
+int64_t mcg_rle_bound(int32_t nx, int32_t ny, int32_t nz);
+/* Encode a device short2 volume into a host file image (header + per-slice
+ * dumps, the reference's file layout).  lossless = 0 writes the reference
+ * format (runs compare tsdf only; weights inside a run are not kept);
+ * lossless = 1 writes the same layout with tag "VOLUME_TSDF_W32" and runs
+ * that compare whole voxels.  Synchronous. */
+mcg_status mcg_rle_encode(mcg_context *ctx, const void *vol, int32_t nx, int32_t ny, int32_t nz,
+                          float min_t, float max_t, float grid_s, int32_t lossless,
+                          uint8_t *image, int64_t capacity, int64_t *size, mcg_stream_t stream);
+/* Parse the header of a host file image: dims[3] and params {min_t,max_t,grid_s}. */
+mcg_status mcg_rle_header(const uint8_t *image, int64_t size, int32_t dims[3], float params[3]);
+/* Decode a host file image into a device short2 volume of capacity voxels.  Synchronous. */
+mcg_status mcg_rle_decode(mcg_context *ctx, const uint8_t *image, int64_t size, void *vol,
+                          int64_t capacity_voxels, mcg_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MCG_H */

@@ -1,0 +1,442 @@
+"""GB300-native TSDF -> mesh path (marching cubes, integrate, depth maps, RLE).
+
+Python host layer over the C ABI of libmcg.so (include/mcg.h).  PyTorch is
+used only to own device memory and to supply the current CUDA stream; every
+computation runs in the library's CUDA kernels.  The names mirror the
+reference's C++ interface:
+
+    MarchingCubes.run                 cu_marching_cubes_v1.h:28-65
+    voxel_new / voxel_delete          cu_kinect_fusion_v1.h:215-216
+    volumetric_integration            cu_kinect_fusion_v1.h:187-188
+    depth_to_maps (+ meter_to_vertex, vertex_to_normal)
+                                      cu_kinect_fusion_v1.cu:99-151
+    extract_surface_normals           cu_kinect_fusion_v1.cu:3227-3242
+    run_length_encode / _decode       cu_kinect_fusion_v1.h:218-219
+
+Volumes are torch tensors of shape (nz, ny, nx, 2): int16 for the reference's
+short2 voxels {tsdf, w} (w reinterpreted as uint16), float32 for the FP32
+volume of the differentiable path.
+"""
+import ctypes
+import dataclasses
+import os
+from typing import Optional
+
+import torch
+
+from . import _capi
+
+_lib = _capi.load()
+
+MCG_OK = 0
+MCG_ERR_INVALID_ARG = 1
+MCG_ERR_CAPACITY = 2
+MCG_ERR_CUDA = 3
+MCG_ERR_TIMEOUT = 4
+MCG_ERR_IO = 5
+MCG_ERR_FORMAT = 6
+MCG_ERR_STATE = 7
+
+VOXEL_SHORT2 = 0
+VOXEL_FLOAT2 = 1
+
+MAX_TSDF = 32766                       # cu_kinect_fusion_v1.h:44
+DEFAULT_TRIANGLES_BUFFER_SIZE = 9 * 1000 * 1000 * 3   # cu_marching_cubes_v1.h:35
+KINECT_DEPTH_MIN = 0.0                 # cu_kinect_fusion_v1.h:32
+KINECT_DEPTH_MAX = 2.0                 # cu_kinect_fusion_v1.h:33
+VERTEX_VOXEL_BYTES = 28
+
+
+class MCGError(RuntimeError):
+    def __init__(self, status, what, cuda_error=0):
+        msg = "%s: %s" % (what, _lib.mcg_status_string(status).decode())
+        if status == MCG_ERR_CUDA:
+            msg += " (cudaError %d)" % cuda_error
+        super().__init__(msg)
+        self.status = status
+        self.cuda_error = cuda_error
+
+
+def library_path():
+    return _capi.LIB_PATH
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else ctypes.c_void_p(0)
+
+
+def _stream(stream=None):
+    if stream is None:
+        stream = torch.cuda.current_stream()
+    return ctypes.c_void_p(stream.cuda_stream)
+
+
+class Context:
+    """Owns one mcg_context (scratch buffers, counters) on one device."""
+
+    def __init__(self, device=None):
+        if device is None:
+            device = torch.cuda.current_device()
+        self.device = int(device)
+        h = ctypes.c_void_p()
+        st = _lib.mcg_create(ctypes.byref(h), self.device)
+        if st != MCG_OK:
+            raise MCGError(st, "mcg_create")
+        self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    def check(self, st, what):
+        if st != MCG_OK:
+            raise MCGError(st, what, _lib.mcg_last_cuda_error(self._h))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.mcg_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_default_ctx = {}
+
+
+def default_context(device=None):
+    if device is None:
+        device = torch.cuda.current_device()
+    ctx = _default_ctx.get(device)
+    if ctx is None:
+        ctx = _default_ctx[device] = Context(device)
+    return ctx
+
+
+def _voxel_type(vol):
+    if vol.dtype == torch.int16:
+        return VOXEL_SHORT2
+    if vol.dtype == torch.float32:
+        return VOXEL_FLOAT2
+    raise TypeError("volume must be int16 (short2) or float32 (float2), got %s" % vol.dtype)
+
+
+def _check_volume(vol):
+    if not vol.is_cuda or vol.dim() != 4 or vol.shape[3] != 2 or not vol.is_contiguous():
+        raise ValueError("volume must be a contiguous CUDA tensor of shape (nz, ny, nx, 2)")
+    return _voxel_type(vol)
+
+
+def _cvol(vol, cell):
+    vt = _check_volume(vol)
+    nz, ny, nx, _ = vol.shape
+    return _capi.Volume(vol.data_ptr(), nx, ny, nz, vt, float(cell))
+
+
+# ---------------------------------------------------------------------------
+# voxel volume (structure.h:20-27 cu_voxel)
+# ---------------------------------------------------------------------------
+@dataclasses.dataclass
+class Voxel:
+    """cu_voxel: size (x, y, z), truncation bounds, grid size and the data."""
+    data: torch.Tensor
+    min_t: float
+    max_t: float
+    grid_s: float
+
+    @property
+    def size(self):
+        nz, ny, nx, _ = self.data.shape
+        return (nx, ny, nz)
+
+    @property
+    def size_xy(self):
+        return self.size[0] * self.size[1]
+
+
+def voxel_init(data, ctx=None, stream=None):
+    """Every voxel -> {tsdf=-32766, w=0} (FP32: {-1, 0}); kf.cu:364-379."""
+    vt = _check_volume(data)
+    ctx = ctx or default_context(data.device.index)
+    n = data.numel() // 2
+    ctx.check(_lib.mcg_voxel_init(ctx.handle, _ptr(data), vt, n, _stream(stream)), "mcg_voxel_init")
+
+
+def voxel_new(size, min_t, max_t, grid_s, dtype=torch.int16, device=None, ctx=None, stream=None):
+    """cu_voxel_new (kf.cu:381-398): allocate and initialise a volume."""
+    nx, ny, nz = (int(s) for s in size)
+    if device is None:
+        device = torch.device("cuda", torch.cuda.current_device())
+    data = torch.empty((nz, ny, nx, 2), dtype=dtype, device=device)
+    voxel_init(data, ctx, stream)
+    return Voxel(data, float(min_t), float(max_t), float(grid_s))
+
+
+def voxel_delete(v: Voxel):
+    """cu_voxel_delete (kf.cu:3245-3258): release the data, zero the fields."""
+    v.data = torch.empty((0, 0, 0, 2), dtype=v.data.dtype, device=v.data.device)
+    v.min_t = v.max_t = v.grid_s = 0.0
+
+
+# ---------------------------------------------------------------------------
+# marching cubes
+# ---------------------------------------------------------------------------
+class Mesh:
+    """Triangle soup as produced by MarchingCubes::run, plus optional side
+    outputs.  soup is the raw 28-byte vertex_voxel records (N, 28) uint8."""
+
+    def __init__(self, soup=None, normals=None, vi2vox=None, ver_voxel=None, tri_cube=None,
+                 counts=None):
+        self.soup = soup
+        self.normals = normals
+        self.vi2vox = vi2vox
+        self.ver_voxel = ver_voxel
+        self.tri_cube = tri_cube
+        self.counts = counts or {}
+
+    @property
+    def num_vertices(self):
+        return int(self.counts.get("vertices", 0))
+
+    @property
+    def num_triangles(self):
+        return int(self.counts.get("triangles", 0))
+
+    def _words(self):
+        return self.soup.view(torch.int32).view(-1, 7)
+
+    @property
+    def positions(self):
+        return self.soup.view(torch.float32).view(-1, 7)[:, 0:3]
+
+    @property
+    def vox_pos(self):
+        return self._words()[:, 3:6]
+
+    @property
+    def tsdf(self):
+        return self.soup.view(torch.int16).view(-1, 14)[:, 12]
+
+    @property
+    def w(self):
+        return self.soup.view(torch.int16).view(-1, 14)[:, 13]
+
+
+def _alloc_outputs(n, nvox, device, soup, normals, vi2vox, ver_voxel, tri_cube):
+    out = {}
+    out["soup"] = torch.empty((n, VERTEX_VOXEL_BYTES), dtype=torch.uint8, device=device) if soup else None
+    out["normals"] = torch.empty((n, 3), dtype=torch.float32, device=device) if normals else None
+    out["vi2vox"] = torch.empty((n, 3), dtype=torch.int32, device=device) if vi2vox else None
+    out["ver_voxel"] = torch.empty((nvox,), dtype=torch.int16, device=device) if ver_voxel else None
+    out["tri_cube"] = torch.empty((n // 3,), dtype=torch.int64, device=device) if tri_cube else None
+    return out
+
+
+def _mesh_out(o, cap):
+    return _capi.MeshOut(
+        o["soup"].data_ptr() if o["soup"] is not None else None,
+        o["normals"].data_ptr() if o["normals"] is not None else None,
+        o["vi2vox"].data_ptr() if o["vi2vox"] is not None else None,
+        o["ver_voxel"].data_ptr() if o["ver_voxel"] is not None else None,
+        o["tri_cube"].data_ptr() if o["tri_cube"] is not None else None,
+        int(cap))
+
+
+def counts(ctx):
+    c = _capi.MeshCounts()
+    st = _lib.mcg_mc_counts(ctx.handle, ctypes.byref(c))
+    if st not in (MCG_OK, MCG_ERR_CAPACITY):
+        ctx.check(st, "mcg_mc_counts")
+    return {"occupied": c.occupied, "triangles": c.triangles, "vertices": c.vertices,
+            "active_bricks": c.active_bricks, "status": c.status}
+
+
+def extract(volume, cell, *, soup=True, normals=True, vi2vox=False, ver_voxel=False, tri_cube=False,
+            ctx=None, stream=None) -> Mesh:
+    """Marching cubes over a (nz, ny, nx, 2) volume; outputs sized exactly.
+
+    Runs the count phase, reads the totals (one host synchronisation, as the
+    reference's getOccupiedVoxels / computeOffsetsAndTotalVertexes do), then
+    generates into exactly-sized buffers."""
+    ctx = ctx or default_context(volume.device.index)
+    cv = _cvol(volume, cell)
+    s = _stream(stream)
+    ctx.check(_lib.mcg_mc_classify(ctx.handle, ctypes.byref(cv), s), "mcg_mc_classify")
+    c = counts(ctx)
+    n = c["vertices"]
+    nz, ny, nx, _ = volume.shape
+    o = _alloc_outputs(n, nx * ny * nz, volume.device, soup, normals, vi2vox, ver_voxel, tri_cube)
+    mo = _mesh_out(o, n)
+    ctx.check(_lib.mcg_mc_generate(ctx.handle, ctypes.byref(cv), ctypes.byref(mo), s), "mcg_mc_generate")
+    return Mesh(o["soup"], o["normals"], o["vi2vox"], o["ver_voxel"], o["tri_cube"], c)
+
+
+def extract_into(volume, cell, outputs: dict, capacity, ctx=None, stream=None):
+    """Asynchronous extraction into preallocated buffers (no host sync).
+
+    outputs: dict with any of soup/normals/vi2vox/ver_voxel/tri_cube tensors.
+    Call counts(ctx) afterwards for the totals and the capacity status."""
+    ctx = ctx or default_context(volume.device.index)
+    cv = _cvol(volume, cell)
+    o = {k: outputs.get(k) for k in ("soup", "normals", "vi2vox", "ver_voxel", "tri_cube")}
+    mo = _mesh_out(o, capacity)
+    ctx.check(_lib.mcg_mc_extract(ctx.handle, ctypes.byref(cv), ctypes.byref(mo), _stream(stream)),
+              "mcg_mc_extract")
+    return ctx
+
+
+class MarchingCubes:
+    """cu_marching_cubes_v1.h:28-65.  run() returns the triangle soup; if the
+    caller's buffer is empty it is sized from the count phase."""
+
+    POINTS_PER_TRIANGLE = 3
+    DEFAULT_TRIANGLES_BUFFER_SIZE = DEFAULT_TRIANGLES_BUFFER_SIZE
+
+    def __init__(self, ctx=None):
+        self.ctx = ctx
+
+    def run(self, tsdf: Voxel, normals=True, vi2vox=True, ver_voxel=True, stream=None) -> Mesh:
+        return extract(tsdf.data, tsdf.grid_s, soup=True, normals=normals, vi2vox=vi2vox,
+                       ver_voxel=ver_voxel, tri_cube=False, ctx=self.ctx, stream=stream)
+
+
+def extract_surface_normals(volume, cell, soup, ctx=None, stream=None):
+    """d_voxel_extract_surface_normals (kf.cu:3236-3242) over vertex records."""
+    ctx = ctx or default_context(volume.device.index)
+    cv = _cvol(volume, cell)
+    n = soup.shape[0]
+    out = torch.empty((n, 3), dtype=torch.float32, device=volume.device)
+    ctx.check(_lib.mcg_mc_normals(ctx.handle, ctypes.byref(cv), _ptr(soup), n, _ptr(out), _stream(stream)),
+              "mcg_mc_normals")
+    return out
+
+
+# ---------------------------------------------------------------------------
+# cameras, depth maps, integrate
+# ---------------------------------------------------------------------------
+def intrinsic(fx, fy, cx, cy):
+    k = _capi.Intrinsic()
+    k.fx, k.fy, k.cx, k.cy = float(fx), float(fy), float(cx), float(cy)
+    return k
+
+
+def extrinsic(R, t):
+    """camera -> global pose; R is a 3x3 rotation (row-major nested list or
+    array), stored column-major as the reference's float33."""
+    import numpy as np
+    R = np.asarray(R, dtype=np.float32).reshape(3, 3)
+    e = _capi.Extrinsic()
+    cols = R.T.reshape(-1)  # column 0 first
+    for i in range(9):
+        e.r[i] = float(cols[i])
+    for i in range(3):
+        e.t[i] = float(np.asarray(t, dtype=np.float32).reshape(3)[i])
+    return e
+
+
+def depth_to_maps(depth_mm, k, depth_min=KINECT_DEPTH_MIN, depth_max=KINECT_DEPTH_MAX, meter=True,
+                  vertex=True, normal=True, ctx=None, stream=None):
+    """uint16-mm depth (h, w) -> metre (h, w), vertex (h, w, 3), normal (h, w, 3)."""
+    if depth_mm.dtype not in (torch.int16, torch.uint16) or not depth_mm.is_cuda or depth_mm.dim() != 2:
+        raise ValueError("depth_mm must be a (h, w) 16-bit CUDA tensor")
+    depth_mm = depth_mm.contiguous()
+    ctx = ctx or default_context(depth_mm.device.index)
+    h, w = depth_mm.shape
+    dev = depth_mm.device
+    m = torch.empty((h, w), dtype=torch.float32, device=dev) if meter else None
+    v = torch.empty((h, w, 3), dtype=torch.float32, device=dev) if vertex else None
+    n = torch.empty((h, w, 3), dtype=torch.float32, device=dev) if normal else None
+    ctx.check(_lib.mcg_depth_to_maps(ctx.handle, ctypes.byref(k), w, h, _ptr(depth_mm), float(depth_min),
+                                     float(depth_max), _ptr(m), _ptr(v), _ptr(n), _stream(stream)),
+              "mcg_depth_to_maps")
+    return m, v, n
+
+
+def meter_to_vertex(meter, k, ctx=None, stream=None):
+    meter = meter.contiguous()
+    ctx = ctx or default_context(meter.device.index)
+    h, w = meter.shape
+    v = torch.empty((h, w, 3), dtype=torch.float32, device=meter.device)
+    ctx.check(_lib.mcg_meter_to_vertex(ctx.handle, ctypes.byref(k), w, h, _ptr(meter), _ptr(v), _stream(stream)),
+              "mcg_meter_to_vertex")
+    return v
+
+
+def vertex_to_normal(vertex, ctx=None, stream=None):
+    vertex = vertex.contiguous()
+    ctx = ctx or default_context(vertex.device.index)
+    h, w, _ = vertex.shape
+    n = torch.empty_like(vertex)
+    ctx.check(_lib.mcg_vertex_to_normal(ctx.handle, w, h, _ptr(vertex), _ptr(n), _stream(stream)),
+              "mcg_vertex_to_normal")
+    return n
+
+
+def volumetric_integration(v: Voxel, k, e, depth_m, normals=None, is_dynamic=False, ctx=None, stream=None):
+    """_cu_voxel_volumetric_integration (kf.cu:534-549): fuse one depth frame
+    (metres, (h, w) float32 CUDA tensor) into v in place."""
+    vt = _check_volume(v.data)
+    depth_m = depth_m.contiguous()
+    if normals is not None:
+        normals = normals.contiguous()
+    ctx = ctx or default_context(v.data.device.index)
+    h, w = depth_m.shape
+    nx, ny, nz = v.size
+    ctx.check(_lib.mcg_integrate(ctx.handle, _ptr(v.data), vt, nx, ny, nz, v.min_t, v.max_t, v.grid_s,
+                                 ctypes.byref(k), ctypes.byref(e), w, h, _ptr(depth_m), _ptr(normals),
+                                 1 if is_dynamic else 0, _stream(stream)),
+              "mcg_integrate")
+
+
+# ---------------------------------------------------------------------------
+# RLE volume I/O (kf.cu:1303-1600)
+# ---------------------------------------------------------------------------
+def rle_encode(v: Voxel, lossless=False, ctx=None, stream=None) -> bytes:
+    """Encode a short2 volume into the reference's RLE file image."""
+    if v.data.dtype != torch.int16:
+        raise TypeError("RLE volumes are short2 (int16) volumes")
+    ctx = ctx or default_context(v.data.device.index)
+    nx, ny, nz = v.size
+    cap = _lib.mcg_rle_bound(nx, ny, nz)
+    buf = (ctypes.c_uint8 * cap)()
+    size = ctypes.c_int64(0)
+    ctx.check(_lib.mcg_rle_encode(ctx.handle, _ptr(v.data), nx, ny, nz, v.min_t, v.max_t, v.grid_s,
+                                  1 if lossless else 0, buf, cap, ctypes.byref(size), _stream(stream)),
+              "mcg_rle_encode")
+    return ctypes.string_at(buf, size.value)
+
+
+def rle_header(image: bytes):
+    dims = (ctypes.c_int32 * 3)()
+    params = (ctypes.c_float * 3)()
+    st = _lib.mcg_rle_header(image, len(image), dims, params)
+    if st != MCG_OK:
+        raise MCGError(st, "mcg_rle_header")
+    return (dims[0], dims[1], dims[2]), (params[0], params[1], params[2])
+
+
+def rle_decode(image: bytes, device=None, ctx=None, stream=None) -> Voxel:
+    (nx, ny, nz), (min_t, max_t, grid_s) = rle_header(image)
+    if device is None:
+        device = torch.device("cuda", torch.cuda.current_device())
+    data = torch.empty((nz, ny, nx, 2), dtype=torch.int16, device=device)
+    ctx = ctx or default_context(data.device.index)
+    ctx.check(_lib.mcg_rle_decode(ctx.handle, image, len(image), _ptr(data), nx * ny * nz, _stream(stream)),
+              "mcg_rle_decode")
+    return Voxel(data, min_t, max_t, grid_s)
+
+
+def run_length_encode(v: Voxel, file_name, lossless=False):
+    """cu_voxel_run_length_encode (kf.cu:1451-1478), whole-volume form."""
+    img = rle_encode(v, lossless)
+    with open(file_name, "wb") as f:
+        f.write(img)
+
+
+def run_length_decode(file_name, device=None) -> Voxel:
+    """cu_voxel_run_length_decode (kf.cu:1533-1563), whole-volume form."""
+    with open(file_name, "rb") as f:
+        return rle_decode(f.read(), device)

@@ -1,0 +1,78 @@
+// Context lifetime, status strings and error plumbing of the C ABI.
+#include <cuda_runtime.h>
+
+#include <new>
+
+#include "mcg_internal.h"
+
+mcg_status mcg_cuda_fail(mcg_context *ctx, cudaError_t e) {
+    if (ctx) ctx->last_cuda_error = (int)e;
+    cudaGetLastError();  // clear a sticky-free error so later calls can proceed
+    return MCG_ERR_CUDA;
+}
+
+extern "C" {
+
+const char *mcg_status_string(int status) {
+    switch (status) {
+        case MCG_OK: return "ok";
+        case MCG_ERR_INVALID_ARG: return "invalid argument";
+        case MCG_ERR_CAPACITY: return "output capacity exceeded";
+        case MCG_ERR_CUDA: return "CUDA error";
+        case MCG_ERR_TIMEOUT: return "device wait timed out";
+        case MCG_ERR_IO: return "I/O error";
+        case MCG_ERR_FORMAT: return "malformed stream or header";
+        case MCG_ERR_STATE: return "call order violated";
+        default: return "unknown status";
+    }
+}
+
+int mcg_version(void) { return MCG_VERSION; }
+
+mcg_status mcg_create(mcg_context **out, int device) {
+    if (!out) return MCG_ERR_INVALID_ARG;
+    *out = nullptr;
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess) { cudaGetLastError(); return MCG_ERR_CUDA; }
+    if (device < 0 || device >= count) return MCG_ERR_INVALID_ARG;
+    mcg_context *ctx = new (std::nothrow) mcg_context();
+    if (!ctx) return MCG_ERR_INVALID_ARG;
+    ctx->device = device;
+    e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&ctx->d_totals, sizeof(mcg::MeshTotals));
+    if (e == cudaSuccess) e = cudaMemset(ctx->d_totals, 0, sizeof(mcg::MeshTotals));
+    if (e == cudaSuccess) e = cudaMallocHost((void **)&ctx->h_totals, sizeof(mcg::MeshTotals));
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->counts_ready, cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        mcg_destroy(ctx);
+        return MCG_ERR_CUDA;
+    }
+    *ctx->h_totals = mcg::MeshTotals{};
+    *out = ctx;
+    return MCG_OK;
+}
+
+mcg_status mcg_destroy(mcg_context *ctx) {
+    if (!ctx) return MCG_OK;
+    cudaSetDevice(ctx->device);
+    if (ctx->counts_ready) cudaEventSynchronize(ctx->counts_ready);
+    cudaFree(ctx->brick_tris);
+    cudaFree(ctx->brick_occ);
+    cudaFree(ctx->brick_vofs);
+    cudaFree(ctx->active);
+    cudaFree(ctx->d_totals);
+    if (ctx->h_totals) cudaFreeHost(ctx->h_totals);
+    if (ctx->counts_ready) cudaEventDestroy(ctx->counts_ready);
+    cudaFree(ctx->depth_scaled);
+    cudaFree(ctx->ray_x);
+    if (ctx->h_ray_x) cudaFreeHost(ctx->h_ray_x);
+    delete ctx;
+    return MCG_OK;
+}
+
+int mcg_last_cuda_error(const mcg_context *ctx) { return ctx ? ctx->last_cuda_error : 0; }
+
+}  // extern "C"

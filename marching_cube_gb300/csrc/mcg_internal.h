@@ -1,0 +1,78 @@
+// Internal declarations shared by the libmcg translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "mcg.h"
+
+namespace mcg {
+
+constexpr int kMaxTsdf = 32766;  // cu_kinect_fusion_v1.h:44 CU_VOXEL_MAX_TSDF
+constexpr int kMaxW = 65535;     // cu_kinect_fusion_v1.h:42 CU_VOXEL_MAX_W
+constexpr float kUbW = 50.0f;    // cu_kinect_fusion_v1.h:46 CU_VOXEL_UB_W
+
+// Totals written by the scan kernel (device) and copied to pinned memory.
+struct MeshTotals {
+    unsigned long long occupied;
+    unsigned long long triangles;
+    unsigned long long vertices;
+    unsigned int active_bricks;
+    unsigned int pad;
+};
+
+// Grows a device allocation; returns false on cudaMalloc failure.
+template <class T>
+bool ensure(T **ptr, size_t *cap, size_t n) {
+    if (*cap >= n && *ptr) return true;
+    if (*ptr) cudaFree(*ptr);
+    *ptr = nullptr;
+    *cap = 0;
+    size_t want = n ? n : 1;
+    if (cudaMalloc((void **)ptr, want * sizeof(T)) != cudaSuccess) return false;
+    *cap = want;
+    return true;
+}
+
+}  // namespace mcg
+
+struct mcg_context {
+    int device = 0;
+    int num_sms = 0;
+    int last_cuda_error = 0;
+
+    // marching-cubes scratch (one entry per brick)
+    uint32_t *brick_tris = nullptr;
+    size_t brick_tris_cap = 0;
+    uint32_t *brick_occ = nullptr;
+    size_t brick_occ_cap = 0;
+    unsigned long long *brick_vofs = nullptr;
+    size_t brick_vofs_cap = 0;
+    uint32_t *active = nullptr;
+    size_t active_cap = 0;
+    mcg::MeshTotals *d_totals = nullptr;
+    mcg::MeshTotals *h_totals = nullptr;  // pinned
+    cudaEvent_t counts_ready = nullptr;
+    bool counts_pending = false;
+
+    // geometry of the last classify (generate must match it)
+    bool classified = false;
+    const void *cls_data = nullptr;
+    int cls_nx = 0, cls_ny = 0, cls_nz = 0, cls_vtype = 0;
+    int64_t last_capacity = -1;
+
+    // integrate scratch
+    float *depth_scaled = nullptr;
+    size_t depth_scaled_cap = 0;
+    // x coordinates of the voxel centres as the reference accumulates them
+    // (p.x += grid_s per voxel); cached per (nx, grid_s)
+    float *ray_x = nullptr;
+    size_t ray_x_cap = 0;
+    float *h_ray_x = nullptr;  // pinned staging copy
+    size_t h_ray_x_cap = 0;
+    int ray_x_n = 0;
+    float ray_x_g = 0.0f;
+};
+
+// records a CUDA failure on ctx and returns the matching status
+mcg_status mcg_cuda_fail(mcg_context *ctx, cudaError_t e);

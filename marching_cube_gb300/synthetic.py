@@ -1,0 +1,138 @@
+"""Seeded synthetic inputs for the TSDF -> mesh workloads.
+
+The reference measures on input files that are not part of it (512dim.vol,
+1024dim.vol, sdf.txt); these generators stand in for them with the shapes,
+sizes and value ranges of the workloads:
+
+  sphere_volume   128^3 short2 sphere (r 40 voxels, truncation 5 voxels,
+                  weights uniform in [1, 128]), cell 1 cm
+  fusion_scene    20 random spheres (r 0.1-0.4 m) and axis-aligned boxes in
+                  a 3 m cube, depth frames ray-cast from a camera orbiting at
+                  1.5 m (pinhole 525/525/319.5/239.5, 640x480), Gaussian
+                  noise sigma 2 mm, uint16 millimetres
+  random_volume   small random short2 volumes for exhaustive parity cases
+
+Randomness: numpy.random.default_rng(seed) for scene parameters and
+torch.Generator(seed) for per-pixel noise.
+"""
+import math
+
+import numpy as np
+import torch
+
+MAX_TSDF = 32766
+
+
+def sphere_volume(n=128, radius=40.0, trunc=5.0, seed=0, weight_max=128, scale=32767, center=None):
+    """(n, n, n, 2) int16: tsdf = trunc(clamp(sd/trunc, -1, 1) * scale)
+    with sd the signed distance (voxel units) of voxel centres (i+0.5) to a
+    sphere centred at n/2; w uniform integer in [1, weight_max]."""
+    c = n / 2.0 if center is None else center
+    i = np.arange(n, dtype=np.float64) + 0.5
+    z, y, x = np.meshgrid(i, i, i, indexing="ij")
+    sd = np.sqrt((x - c) ** 2 + (y - c) ** 2 + (z - c) ** 2) - radius
+    t = np.trunc(np.clip(sd / trunc, -1.0, 1.0) * scale).astype(np.int16)
+    rng = np.random.default_rng(seed)
+    w = rng.integers(1, weight_max + 1, size=t.shape, dtype=np.int64).astype(np.uint16).view(np.int16)
+    return np.stack([t, w], axis=-1)
+
+
+def random_volume(shape, seed=0, p_zero_weight=0.05, sentinel_frac=0.1):
+    """Random short2 volume (nz, ny, nx, 2) exercising every cube case,
+    zero weights and the +-32766 sentinels."""
+    rng = np.random.default_rng(seed)
+    nz, ny, nx = shape
+    t = rng.integers(-32767, 32768, size=(nz, ny, nx), dtype=np.int64)
+    s = rng.random((nz, ny, nx))
+    t[s < sentinel_frac / 2] = MAX_TSDF
+    t[(s >= sentinel_frac / 2) & (s < sentinel_frac)] = -MAX_TSDF
+    w = rng.integers(1, 65536, size=(nz, ny, nx), dtype=np.int64)
+    w[rng.random((nz, ny, nx)) < p_zero_weight] = 0
+    return np.stack([t.astype(np.int16), w.astype(np.uint16).view(np.int16)], axis=-1)
+
+
+# ---------------------------------------------------------------------------
+# fusion scene
+# ---------------------------------------------------------------------------
+class FusionScene:
+    """Spheres and boxes inside a cube of side `extent` metres (volume
+    coordinates [0, extent)^3, voxel (x, y, z) at (x, y, z) * grid_s as the
+    reference's integrate places it)."""
+
+    def __init__(self, seed=0, n_spheres=20, n_boxes=8, extent=3.0):
+        rng = np.random.default_rng(seed)
+        c = extent / 2.0
+        self.extent = extent
+        self.center = np.array([c, c, c])
+        # objects stay within 1.1 m of the centre; the camera orbits at 1.5 m
+        self.sph_c = c + rng.uniform(-0.7, 0.7, size=(n_spheres, 3))
+        self.sph_r = rng.uniform(0.1, 0.4, size=n_spheres)
+        self.box_c = c + rng.uniform(-0.7, 0.7, size=(n_boxes, 3))
+        self.box_h = rng.uniform(0.05, 0.25, size=(n_boxes, 3))
+
+    def pose(self, frame, n_frames, radius=1.5):
+        """camera -> global (R, t) of frame `frame` of an orbit looking at the centre."""
+        a = 2.0 * math.pi * frame / n_frames
+        elev = 0.25 * math.sin(2.0 * a)
+        eye = self.center + radius * np.array([math.cos(a) * math.cos(elev), math.sin(elev),
+                                               math.sin(a) * math.cos(elev)])
+        fwd = self.center - eye
+        fwd /= np.linalg.norm(fwd)
+        up = np.array([0.0, 1.0, 0.0])
+        right = np.cross(up, fwd)
+        right /= np.linalg.norm(right)
+        down = np.cross(fwd, right)
+        R = np.stack([right, down, fwd], axis=1)  # columns: camera x, y, z in world
+        return R, eye
+
+    def depth_frame(self, R, t, w=640, h=480, fx=525.0, fy=525.0, cx=319.5, cy=239.5,
+                    noise_sigma=0.002, seed=0, device="cpu"):
+        """Ray-cast z-depth + N(0, sigma), rounded to uint16 millimetres
+        (0 where the ray misses)."""
+        dev = torch.device(device)
+        dt = torch.float64
+        v, u = torch.meshgrid(torch.arange(h, device=dev, dtype=dt), torch.arange(w, device=dev, dtype=dt),
+                              indexing="ij")
+        dc = torch.stack([(u - cx) / fx, (v - cy) / fy, torch.ones_like(u)], dim=-1).reshape(-1, 3)
+        Rt = torch.as_tensor(R, dtype=dt, device=dev)
+        o = torch.as_tensor(t, dtype=dt, device=dev)
+        d = dc @ Rt.T  # world direction, camera-z component 1 -> ray parameter == z-depth
+        best = torch.full((d.shape[0],), float("inf"), dtype=dt, device=dev)
+        # spheres
+        sc = torch.as_tensor(self.sph_c, dtype=dt, device=dev)
+        sr = torch.as_tensor(self.sph_r, dtype=dt, device=dev)
+        oc = o[None, :] - sc  # (S, 3)
+        a = (d * d).sum(-1)[:, None]
+        b = 2.0 * (d @ oc.T)
+        cc = (oc * oc).sum(-1)[None, :] - sr[None, :] ** 2
+        disc = b * b - 4 * a * cc
+        sq = torch.sqrt(torch.clamp(disc, min=0.0))
+        s0 = (-b - sq) / (2 * a)
+        s0 = torch.where((disc >= 0) & (s0 > 1e-6), s0, torch.full_like(s0, float("inf")))
+        best = torch.minimum(best, s0.min(dim=1).values)
+        # boxes (slab test)
+        bc = torch.as_tensor(self.box_c, dtype=dt, device=dev)
+        bh = torch.as_tensor(self.box_h, dtype=dt, device=dev)
+        lo = bc - bh
+        hi = bc + bh
+        inv = 1.0 / torch.where(d.abs() < 1e-12, torch.full_like(d, 1e-12), d)
+        t1 = (lo[None, :, :] - o[None, None, :]) * inv[:, None, :]
+        t2 = (hi[None, :, :] - o[None, None, :]) * inv[:, None, :]
+        tmin = torch.minimum(t1, t2).max(dim=-1).values
+        tmax = torch.maximum(t1, t2).min(dim=-1).values
+        hit = (tmax >= tmin) & (tmin > 1e-6)
+        tb = torch.where(hit, tmin, torch.full_like(tmin, float("inf")))
+        best = torch.minimum(best, tb.min(dim=1).values)
+        g = torch.Generator(device=dev)
+        g.manual_seed(int(seed))
+        noise = torch.randn(best.shape, generator=g, device=dev, dtype=dt) * noise_sigma
+        z = torch.where(torch.isfinite(best), best + noise, torch.zeros_like(best))
+        mm = torch.clamp(torch.round(z * 1000.0), 0, 65535)
+        return mm.reshape(h, w).to(torch.int32)
+
+
+def mm_to_u16_bits(mm):
+    """int32 millimetre tensor -> int16 tensor holding the uint16 bit
+    pattern (the depth kernels read the 16 bits as unsigned)."""
+    m = mm.to(torch.int32) & 0xFFFF
+    return torch.where(m >= 32768, m - 65536, m).to(torch.int16)

@@ -1,0 +1,256 @@
+"""Python bindings of the CPU oracle (oracle.c).  TEST INFRASTRUCTURE ONLY.
+
+Used by tests/, by __graft_entry__.smoke() and by bench.py's CPU-baseline
+leg as the checker.  Parity status: unpinned by reference tests (the
+reference has none); see oracle.h.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+
+VOXEL_SHORT2 = 0
+VOXEL_FLOAT2 = 1
+
+
+def build():
+    r = subprocess.run(["make", "-s", "-C", HERE], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + r.stdout + r.stderr)
+    return LIB_PATH
+
+
+class Intrinsic(ctypes.Structure):
+    _fields_ = [("fx", ctypes.c_float), ("fy", ctypes.c_float), ("cx", ctypes.c_float),
+                ("cy", ctypes.c_float), ("dc", ctypes.c_float * 5)]
+
+
+class Extrinsic(ctypes.Structure):
+    _fields_ = [("r", ctypes.c_float * 9), ("t", ctypes.c_float * 3)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = ctypes.CDLL(LIB_PATH)
+        vp, i32, i64, f32, f64 = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_float, ctypes.c_double
+        sig = {
+            "orc_mc_classify": (None, [vp, i32, i32, i32, i32, vp, vp]),
+            "orc_mc_count": (None, [vp, i32, i32, i32, i32, vp, vp, i32]),
+            "orc_mc_extract": (i64, [vp, i32, i32, i32, i32, f32, vp, vp, vp, vp, vp, i64, i32]),
+            "orc_mc_extract_f64": (i64, [vp, i32, i32, i32, i32, f64, vp, vp, i64]),
+            "orc_surface_normal": (None, [vp, i32, i32, i32, i32, f32, vp, vp]),
+            "orc_voxel_init": (None, [vp, i64]),
+            "orc_depth_to_meter": (None, [vp, i64, f32, f32, vp]),
+            "orc_meter_to_vertex": (None, [vp, i32, i32, vp, vp]),
+            "orc_vertex_to_normal": (None, [i32, i32, vp, vp]),
+            "orc_depth_scale": (None, [vp, i32, i32, vp, vp]),
+            "orc_integrate": (None, [vp, i32, i32, i32, i32, f32, f32, f32, vp, vp, i32, i32, vp, vp, i32, i32]),
+            "orc_rle_encode_slice": (i64, [vp, i64, i32, vp]),
+            "orc_rle_decode_slice": (i64, [vp, i64, vp, i64]),
+            "orc_rle_encode_volume": (i64, [vp, i32, i32, i32, f32, f32, f32, i32, vp, i64]),
+            "orc_rle_decode_volume": (i32, [vp, i64, vp, i64, vp, vp]),
+            "orc_max_threads": (i32, []),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
+
+
+def _vol(vol):
+    vol = np.ascontiguousarray(vol)
+    if vol.ndim != 4 or vol.shape[3] != 2:
+        raise ValueError("volume must be (nz, ny, nx, 2)")
+    if vol.dtype == np.int16:
+        vt = VOXEL_SHORT2
+    elif vol.dtype == np.float32:
+        vt = VOXEL_FLOAT2
+    else:
+        raise TypeError(vol.dtype)
+    nz, ny, nx, _ = vol.shape
+    return vol, vt, nx, ny, nz
+
+
+def max_threads():
+    return lib().orc_max_threads()
+
+
+def mc_classify(vol):
+    vol, vt, nx, ny, nz = _vol(vol)
+    shape = (max(nz - 1, 0), max(ny - 1, 0), max(nx - 1, 0))
+    ci = np.zeros(shape, np.uint8)
+    nv = np.zeros(shape, np.uint8)
+    lib().orc_mc_classify(_p(vol), vt, nx, ny, nz, _p(ci), _p(nv))
+    return ci, nv
+
+
+def mc_count(vol, nthreads=0):
+    vol, vt, nx, ny, nz = _vol(vol)
+    o = np.zeros(1, np.int64)
+    t = np.zeros(1, np.int64)
+    lib().orc_mc_count(_p(vol), vt, nx, ny, nz, _p(o), _p(t), nthreads)
+    return int(o[0]), int(t[0])
+
+
+VERTEX_DTYPE = np.dtype([("pos", "<f4", (3,)), ("vox", "<i4", (3,)), ("tsdf", "<i2"), ("w", "<i2")])
+assert VERTEX_DTYPE.itemsize == 28
+
+
+def mc_extract(vol, cell, normals=True, vi2vox=True, ver_voxel=True, tri_cube=True, nthreads=0):
+    """FP32 mirror; canonical order (cube linear id, table slot)."""
+    vol, vt, nx, ny, nz = _vol(vol)
+    _, ntri = mc_count(vol, nthreads)
+    n = 3 * ntri
+    soup = np.zeros(n, VERTEX_DTYPE)
+    nrm = np.zeros((n, 3), np.float32) if normals else None
+    v2v = np.zeros((n, 3), np.int32) if vi2vox else None
+    vv = np.zeros(nx * ny * nz, np.int16) if ver_voxel else None
+    tc = np.zeros(ntri, np.int64) if tri_cube else None
+    total = lib().orc_mc_extract(_p(vol), vt, nx, ny, nz, float(cell), _p(soup), _p(nrm), _p(v2v), _p(vv),
+                                 _p(tc), n, nthreads)
+    assert total == n
+    return {"soup": soup, "normals": nrm, "vi2vox": v2v, "ver_voxel": vv, "tri_cube": tc}
+
+
+def mc_extract_f64(vol, cell):
+    vol, vt, nx, ny, nz = _vol(vol)
+    _, ntri = mc_count(vol)
+    n = 3 * ntri
+    pos = np.zeros((n, 3), np.float64)
+    nrm = np.zeros((n, 3), np.float64)
+    lib().orc_mc_extract_f64(_p(vol), vt, nx, ny, nz, float(cell), _p(pos), _p(nrm), n)
+    return pos, nrm
+
+
+def surface_normal(vol, cell, p):
+    vol, vt, nx, ny, nz = _vol(vol)
+    p = np.asarray(p, np.float32)
+    n = np.zeros(3, np.float32)
+    lib().orc_surface_normal(_p(vol), vt, nx, ny, nz, float(cell), _p(p), _p(n))
+    return n
+
+
+def voxel_init(n_voxels):
+    v = np.zeros((n_voxels, 2), np.int16)
+    lib().orc_voxel_init(_p(v), n_voxels)
+    return v
+
+
+def intrinsic(fx, fy, cx, cy):
+    k = Intrinsic()
+    k.fx, k.fy, k.cx, k.cy = fx, fy, cx, cy
+    return k
+
+
+def extrinsic(R, t):
+    R = np.asarray(R, np.float32).reshape(3, 3)
+    e = Extrinsic()
+    cols = R.T.reshape(-1)
+    for i in range(9):
+        e.r[i] = float(cols[i])
+    t = np.asarray(t, np.float32).reshape(3)
+    for i in range(3):
+        e.t[i] = float(t[i])
+    return e
+
+
+def depth_to_meter(depth_mm, dmin=0.0, dmax=2.0):
+    d = np.ascontiguousarray(depth_mm, np.uint16)
+    m = np.zeros(d.shape, np.float32)
+    lib().orc_depth_to_meter(_p(d), d.size, dmin, dmax, _p(m))
+    return m
+
+
+def meter_to_vertex(k, meter):
+    meter = np.ascontiguousarray(meter, np.float32)
+    h, w = meter.shape
+    v = np.zeros((h, w, 3), np.float32)
+    lib().orc_meter_to_vertex(ctypes.byref(k), w, h, _p(meter), _p(v))
+    return v
+
+
+def vertex_to_normal(vertex):
+    vertex = np.ascontiguousarray(vertex, np.float32)
+    h, w, _ = vertex.shape
+    n = np.zeros_like(vertex)
+    lib().orc_vertex_to_normal(w, h, _p(vertex), _p(n))
+    return n
+
+
+def depth_scale(k, depth):
+    depth = np.ascontiguousarray(depth, np.float32)
+    h, w = depth.shape
+    out = np.zeros_like(depth)
+    lib().orc_depth_scale(ctypes.byref(k), w, h, _p(depth), _p(out))
+    return out
+
+
+def integrate(vol, min_t, max_t, grid_s, k, e, depth_m, normals=None, is_dynamic=False, nthreads=0):
+    """In place on a contiguous numpy volume."""
+    if not vol.flags.c_contiguous:
+        raise ValueError("volume must be contiguous")
+    _, vt, nx, ny, nz = _vol(vol)
+    depth_m = np.ascontiguousarray(depth_m, np.float32)
+    h, w = depth_m.shape
+    if normals is not None:
+        normals = np.ascontiguousarray(normals, np.float32)
+    lib().orc_integrate(_p(vol), vt, nx, ny, nz, min_t, max_t, grid_s, ctypes.byref(k), ctypes.byref(e), w, h,
+                        _p(depth_m), _p(normals), 1 if is_dynamic else 0, nthreads)
+
+
+def rle_encode_slice(vox, lossless=False):
+    vox = np.ascontiguousarray(vox, np.int16).reshape(-1, 2)
+    buf = np.zeros(6 * len(vox) + 16, np.uint8)
+    n = lib().orc_rle_encode_slice(_p(vox), len(vox), 1 if lossless else 0, _p(buf))
+    return buf[:n].tobytes()
+
+
+def rle_decode_slice(data: bytes, n_voxels):
+    buf = np.frombuffer(data, np.uint8).copy()
+    out = np.zeros((n_voxels, 2), np.int16)
+    r = lib().orc_rle_decode_slice(_p(buf), len(buf), _p(out), n_voxels)
+    if r < 0:
+        raise ValueError("malformed RLE slice")
+    return out
+
+
+def rle_encode_volume(vol, min_t, max_t, grid_s, lossless=False):
+    vol, vt, nx, ny, nz = _vol(vol)
+    assert vt == VOXEL_SHORT2
+    cap = 40 + nz * (4 + 6 * nx * ny)
+    buf = np.zeros(cap, np.uint8)
+    n = lib().orc_rle_encode_volume(_p(vol), nx, ny, nz, min_t, max_t, grid_s, 1 if lossless else 0, _p(buf), cap)
+    if n < 0:
+        raise RuntimeError("encode failed")
+    return buf[:n].tobytes()
+
+
+def rle_decode_volume(img: bytes):
+    buf = np.frombuffer(img, np.uint8).copy()
+    dims = np.zeros(3, np.int32)
+    params = np.zeros(3, np.float32)
+    r = lib().orc_rle_decode_volume(_p(buf), len(buf), None, 0, _p(dims), _p(params))
+    if r != 0:
+        raise ValueError("bad header (%d)" % r)
+    nx, ny, nz = (int(d) for d in dims)
+    vol = np.zeros((nz, ny, nx, 2), np.int16)
+    r = lib().orc_rle_decode_volume(_p(buf), len(buf), _p(vol), vol.size // 2, _p(dims), _p(params))
+    if r != 0:
+        raise ValueError("malformed RLE volume (%d)" % r)
+    return vol, tuple(float(p) for p in params)
