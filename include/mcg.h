@@ -36,7 +36,8 @@ typedef enum mcg_status {
     MCG_ERR_TIMEOUT = 4,     /* a bounded device-side wait expired */
     MCG_ERR_IO = 5,          /* file could not be opened / read / written */
     MCG_ERR_FORMAT = 6,      /* malformed RLE stream or file header */
-    MCG_ERR_STATE = 7        /* call order violated (e.g. generate without classify) */
+    MCG_ERR_STATE = 7,       /* call order violated (e.g. generate without classify) */
+    MCG_ERR_TOO_LARGE = 8    /* volume larger than the fixed scratch of mcg_mc_extract_noalloc */
 } mcg_status;
 
 /* voxel storage types */
@@ -116,6 +117,27 @@ mcg_status mcg_mc_generate(mcg_context *ctx, const mcg_volume *vol, const mcg_me
 /* classify + generate in one call, no host synchronisation */
 mcg_status mcg_mc_extract(mcg_context *ctx, const mcg_volume *vol, const mcg_mesh_out *out,
                           mcg_stream_t stream);
+/* No counterpart in the reference.  The same extraction as mcg_mc_extract
+ * for callers that cannot allocate device memory -- a process whose device
+ * memory is owned by another allocator (a caching allocator or an arena
+ * reserved at start-up, where a stray cudaMalloc can fail or fragment the
+ * budget), or a real-time loop that forbids allocation once running
+ * (cudaMalloc/cudaFree may synchronise the device and take unbounded time).
+ * It takes no context and allocates nothing: its scratch is one static
+ * device array of MCG_NOALLOC_SCRATCH_BYTES (about 1.25 MiB) that every
+ * device the library is loaded on holds until the process exits.  Volumes
+ * with more than MCG_NOALLOC_MAX_BRICKS bricks of 32x8x8 cubes (e.g. larger
+ * than 513^3 voxels) are rejected with MCG_ERR_TOO_LARGE.  The first call on
+ * a device looks up the array's device address (cudaGetSymbolAddress) with
+ * that device current; make that first call before any stream capture.
+ * Every call shares the one array, so calls whose work overlaps on the GPU
+ * (other streams, other host threads) race and corrupt each other's
+ * results: serialise them.  The call waits for its stream to finish and
+ * fills *counts (status MCG_ERR_CAPACITY if the soup was truncated). */
+#define MCG_NOALLOC_MAX_BRICKS 65536
+#define MCG_NOALLOC_SCRATCH_BYTES (65536 * 20 + 256)
+mcg_status mcg_mc_extract_noalloc(const mcg_volume *vol, const mcg_mesh_out *out,
+                                  mcg_mesh_counts *counts, mcg_stream_t stream);
 /* kf.cu:3227-3242 d_voxel_extract_surface_normal(s) for n arbitrary vertex
  * records (the normal of ver_pos); normals is float3[n] */
 mcg_status mcg_mc_normals(mcg_context *ctx, const mcg_volume *vol, const mcg_vertex_voxel *verts,

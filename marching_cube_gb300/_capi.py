@@ -52,6 +52,8 @@ SIGNATURES = {
     "mcg_mc_counts": (c_int, [c_void_p, ctypes.POINTER(MeshCounts)]),
     "mcg_mc_generate": (c_int, [c_void_p, ctypes.POINTER(Volume), ctypes.POINTER(MeshOut), c_void_p]),
     "mcg_mc_extract": (c_int, [c_void_p, ctypes.POINTER(Volume), ctypes.POINTER(MeshOut), c_void_p]),
+    "mcg_mc_extract_noalloc": (c_int, [ctypes.POINTER(Volume), ctypes.POINTER(MeshOut),
+                                       ctypes.POINTER(MeshCounts), c_void_p]),
     "mcg_mc_normals": (c_int, [c_void_p, ctypes.POINTER(Volume), c_void_p, c_int64, c_void_p, c_void_p]),
     "mcg_depth_to_maps": (c_int, [c_void_p, ctypes.POINTER(Intrinsic), c_int32, c_int32, c_void_p,
                                   c_float, c_float, c_void_p, c_void_p, c_void_p, c_void_p]),

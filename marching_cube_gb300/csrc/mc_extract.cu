@@ -779,3 +779,126 @@ mcg_status mcg_mc_normals(mcg_context *ctx, const mcg_volume *vol, const mcg_ver
     e = cudaGetLastError();
     return e == cudaSuccess ? MCG_OK : mcg_cuda_fail(ctx, e);
 }
+
+// ---- extraction without any allocation ------------------------------------------
+// For callers that cannot allocate device memory: the scratch of the three
+// passes lives in one file-scope device array of fixed size, reserved when
+// the library is loaded onto a device and held until the process exits.
+namespace mcg {
+namespace {
+
+constexpr long long kNoAllocBricks = MCG_NOALLOC_MAX_BRICKS;
+constexpr size_t kNoAllocTrisOff = 0;
+constexpr size_t kNoAllocOccOff = kNoAllocTrisOff + sizeof(uint32_t) * kNoAllocBricks;
+constexpr size_t kNoAllocVofsOff = kNoAllocOccOff + sizeof(uint32_t) * kNoAllocBricks;
+constexpr size_t kNoAllocActiveOff = kNoAllocVofsOff + sizeof(unsigned long long) * kNoAllocBricks;
+constexpr size_t kNoAllocTotalsOff = kNoAllocActiveOff + sizeof(uint32_t) * kNoAllocBricks;
+constexpr size_t kNoAllocBytes = kNoAllocTotalsOff + 256;
+static_assert(kNoAllocVofsOff % 8 == 0 && kNoAllocTotalsOff % 8 == 0, "scratch alignment");
+static_assert(kNoAllocBytes == MCG_NOALLOC_SCRATCH_BYTES, "scratch size stated in mcg.h");
+
+// brick counts, soup offsets, active-brick list and totals of one call
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+// device address of g_noalloc_scratch per device, taken once with that device current
+unsigned char *g_noalloc_addr[64] = {nullptr};
+
+}  // namespace
+}  // namespace mcg
+
+extern "C" mcg_status mcg_mc_extract_noalloc(const mcg_volume *vol, const mcg_mesh_out *out,
+                                             mcg_mesh_counts *counts, mcg_stream_t stream) {
+    using namespace mcg;
+    if (!vol_ok(vol) || !out || !counts || out->capacity_vertices < 0) return MCG_ERR_INVALID_ARG;
+    const Geometry g = geometry(vol->nx, vol->ny, vol->nz);
+    if (g.nbricks > kNoAllocBricks) return MCG_ERR_TOO_LARGE;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess || dev < 0 || dev >= 64) return MCG_ERR_CUDA;
+    // set-up, once per device: the host-side symbol is only a stand-in, the
+    // kernels need the device address of the array
+    if (!g_noalloc_addr[dev]) {
+        void *p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p) { cudaGetLastError(); return MCG_ERR_CUDA; }
+        g_noalloc_addr[dev] = static_cast<unsigned char *>(p);
+    }
+    e = upload_tables(dev);
+    if (e != cudaSuccess) { cudaGetLastError(); return MCG_ERR_CUDA; }
+    unsigned char *base = g_noalloc_addr[dev];
+    uint32_t *tris = reinterpret_cast<uint32_t *>(base + kNoAllocTrisOff);
+    uint32_t *occ = reinterpret_cast<uint32_t *>(base + kNoAllocOccOff);
+    unsigned long long *vofs = reinterpret_cast<unsigned long long *>(base + kNoAllocVofsOff);
+    uint32_t *active = reinterpret_cast<uint32_t *>(base + kNoAllocActiveOff);
+    MeshTotals *totals = reinterpret_cast<MeshTotals *>(base + kNoAllocTotalsOff);
+    int sms = 0;
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) { cudaGetLastError(); return MCG_ERR_CUDA; }
+    cudaStream_t s = (cudaStream_t)stream;
+    // every scratch entry read later is written first by these launches, so
+    // nothing carried over from an earlier call is used
+    long long cgrid = (long long)sms * 8;
+    if (cgrid > g.nbricks) cgrid = g.nbricks;
+    if (vol->voxel_type == MCG_VOXEL_SHORT2)
+        mc_classify_kernel<MCG_VOXEL_SHORT2><<<(int)cgrid, THREADS, 0, s>>>(
+            (const short2 *)vol->data, vol->nx, vol->ny, vol->nz, g.nbx, g.nby, g.nbricks, tris, occ);
+    else
+        mc_classify_kernel<MCG_VOXEL_FLOAT2><<<(int)cgrid, THREADS, 0, s>>>(
+            (const float2 *)vol->data, vol->nx, vol->ny, vol->nz, g.nbx, g.nby, g.nbricks, tris, occ);
+    mc_scan_kernel<<<1, SCAN_THREADS, 0, s>>>(tris, occ, g.nbricks, vofs, active, totals);
+    if (out->ver_voxel) {
+        e = cudaMemsetAsync(out->ver_voxel, 0, sizeof(int16_t) * (size_t)vol->nx * vol->ny * vol->nz, s);
+        if (e != cudaSuccess) { cudaGetLastError(); return MCG_ERR_CUDA; }
+    }
+    GenParams p;
+    p.vol = vol->data;
+    p.nx = vol->nx;
+    p.ny = vol->ny;
+    p.nz = vol->nz;
+    p.cell = vol->cell;
+    p.nbx = g.nbx;
+    p.nby = g.nby;
+    p.active = active;
+    p.brick_vofs = vofs;
+    p.totals = totals;
+    p.soup = out->soup;
+    p.normals = out->soup_normals;
+    p.vi2vox = out->vi2vox;
+    p.ver_voxel = out->ver_voxel;
+    p.tri_cube = out->tri_cube;
+    p.cap = out->capacity_vertices;
+    int occb = 1;
+    if (vol->voxel_type == MCG_VOXEL_SHORT2) {
+        cudaFuncSetAttribute(mc_generate_kernel<MCG_VOXEL_SHORT2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)gen_smem<MCG_VOXEL_SHORT2>());
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occb, mc_generate_kernel<MCG_VOXEL_SHORT2>, THREADS,
+                                                          gen_smem<MCG_VOXEL_SHORT2>()) != cudaSuccess || occb < 1)
+            occb = 1;
+        long long grid = (long long)sms * occb;
+        if (grid > g.nbricks) grid = g.nbricks;
+        mc_generate_kernel<MCG_VOXEL_SHORT2><<<(int)grid, THREADS, gen_smem<MCG_VOXEL_SHORT2>(), s>>>(p);
+    } else {
+        cudaFuncSetAttribute(mc_generate_kernel<MCG_VOXEL_FLOAT2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)gen_smem<MCG_VOXEL_FLOAT2>());
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occb, mc_generate_kernel<MCG_VOXEL_FLOAT2>, THREADS,
+                                                          gen_smem<MCG_VOXEL_FLOAT2>()) != cudaSuccess || occb < 1)
+            occb = 1;
+        long long grid = (long long)sms * occb;
+        if (grid > g.nbricks) grid = g.nbricks;
+        mc_generate_kernel<MCG_VOXEL_FLOAT2><<<(int)grid, THREADS, gen_smem<MCG_VOXEL_FLOAT2>(), s>>>(p);
+    }
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return MCG_ERR_CUDA;
+    // counts: copy the totals out of the array into a host variable and wait
+    MeshTotals t;
+    e = cudaMemcpyAsync(&t, totals, sizeof(MeshTotals), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) { cudaGetLastError(); return MCG_ERR_CUDA; }
+    counts->occupied = (int64_t)t.occupied;
+    counts->triangles = (int64_t)t.triangles;
+    counts->vertices = (int64_t)t.vertices;
+    counts->active_bricks = (int64_t)t.active_bricks;
+    counts->status = counts->vertices > out->capacity_vertices ? MCG_ERR_CAPACITY : MCG_OK;
+    counts->reserved = 0;
+    return (mcg_status)counts->status;
+}
