@@ -6,14 +6,31 @@
 //   trianglesGeneratorKernel (:228-396) -> mc_generate_kernel (+ fused normals,
 //                                          cu_kinect_fusion_v1.cu:3146-3242)
 //
-// Work is organised in bricks of 32x8x8 cubes.  Pass 1 reads the whole volume
-// once (brick + 1-voxel halo staged in shared memory), counts triangles and
-// occupied cubes per brick.  A single-CTA scan turns brick counts into 64-bit
-// soup offsets and a list of active bricks in brick order.  Pass 2 revisits
-// only active bricks (brick + halo of -1/+2 voxels for the side outputs and
-// normals), re-derives cube indices, scans emitted vertices inside the brick
-// and writes one soup vertex per thread through a per-warp shared-memory
-// stage so every global store is a full coalesced line.
+// Work is organised in bricks of 32x8x8 cubes.
+//
+// Pass 1 (classify) streams the whole volume once: each persistent CTA keeps
+// a 4-stage pipeline of brick tiles (brick + 1-voxel halo, 36x9x9 voxels)
+// loaded by TMA (cp.async.bulk.tensor.3d, completion on an mbarrier that one
+// thread polls with a time bound).  Each of 81 threads turns one 33-voxel row
+// of the tile into two bit masks (tsdf < 0, weight == 0) from 16-byte
+// shared-memory loads; a cube row of 32 cubes is then classified with a
+// handful of 64-bit AND/OR operations on four row masks and __popc, so only
+// occupied cubes (a few per mille of a fusion volume) ever look up a table.
+// Output: triangle and occupied-cube counts per brick.
+//
+// A single-CTA scan turns brick counts into 64-bit soup offsets and a list of
+// active bricks in brick order.
+//
+// Pass 2 (generate) visits only active bricks, with a 2-stage TMA prefetch of
+// the brick + halo (-4/-1/-1 .. +4/+2/+2 voxels, 40x11x11, x rounded down to a
+// 16-byte boundary).  The same masks give a compact list of occupied cubes
+// with their vertex offsets; each thread then emits one soup vertex (owning
+// cube by binary search over the list), computes the fused normal from the
+// tile, and the 28-byte records go out through a per-warp shared-memory stage
+// as full coalesced lines.
+//
+// When TMA cannot describe the volume (x row not a multiple of 16 bytes or an
+// unaligned base) the same kernels fill the tiles with plain loads.
 //
 // Output order is deterministic: bricks in (bz, by, bx) order, cubes in
 // (z, y, x) order inside a brick, then the table slot -- the reference's
@@ -21,11 +38,15 @@
 //
 // Arithmetic follows the reference's expressions in IEEE binary32, source
 // order, no contraction (the library is built with --fmad=false).
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
 
 #include "mc_tables.h"
 #include "mcg_internal.h"
+#include "tma.cuh"
 
 namespace mcg {
 namespace {
@@ -34,22 +55,30 @@ constexpr int BX = 32, BY = 8, BZ = 8;
 constexpr int BRICK_CUBES = BX * BY * BZ;  // 2048
 constexpr int THREADS = 256;
 constexpr int WARPS = THREADS / 32;
-static_assert(BX == 32 && BY == WARPS, "thread (lane, warp) maps to cube (x, y)");
+constexpr int ROWS = (BY + 1) * (BZ + 1);  // voxel rows feeding one brick: 81
+constexpr int CUBE_ROWS = BY * BZ;         // 64
+constexpr int CHUNK = 256;                 // bricks per scan chunk
 
-// generate tile: voxels [x0-1, x0+BX+2) etc.
-constexpr int TX = BX + 3, TY = BY + 3, TZ = BZ + 3;
-constexpr int TILE = TX * TY * TZ;
-// classify tile: voxels [x0, x0+BX+1)
-constexpr int CX1 = BX + 1, CY1 = BY + 1, CZ1 = BZ + 1;
-constexpr int CTILE = CX1 * CY1 * CZ1;
+// classify tile: voxels [x0, x0+36) x [y0, y0+9) x [z0, z0+9)
+constexpr int CTX = 36, CTY = BY + 1, CTZ = BZ + 1;
+constexpr int CTILE = CTX * CTY * CTZ;
+// generate tile: voxels [x0, x0+36) x [y0, y0+10) x [z0, z0+10) -- every
+// corner and normal sample of the brick's cubes; the rare side-output reads
+// of voxel x0-1 / y0-1 / z0-1 go to global memory
+constexpr int TXO = 0, TYO = 0, TZO = 0;
+constexpr int TX = BX + 4, TY = BY + 2, TZ = BZ + 2;
+constexpr int GTILE = TX * TY * TZ;
+constexpr int GSTAGES = 2;
 
-// corner offsets (cu_marching_cubes_v1.cu:74-81) and edge corner pairs in
-// vertex_interp argument order (:304-315)
+__host__ __device__ constexpr int pad128(int bytes) { return (bytes + 127) / 128 * 128; }
+
 // corner c: x = {0,1,1,0,0,1,1,0}, y = {0,0,1,1,0,0,1,1}, z = {0,0,0,0,1,1,1,1}
+// (corner order of cu_marching_cubes_v1.cu:74-81)
 __device__ __forceinline__ int c_cx(int c) { return (c ^ (c >> 1)) & 1; }
 __device__ __forceinline__ int c_cy(int c) { return (c >> 1) & 1; }
 __device__ __forceinline__ int c_cz(int c) { return c >> 2; }
 // edge e: first corner {0..7,0,1,2,3}, second {1,2,3,0,5,6,7,4,4,5,6,7}
+// (vertex_interp argument order, :304-315)
 __device__ __forceinline__ int c_ea(int e) { return e < 8 ? e : e - 8; }
 __device__ __forceinline__ int c_eb(int e) { return e < 8 ? (e & 4) | ((e + 1) & 3) : e - 4; }
 __constant__ signed char c_tri[256][16];
@@ -62,6 +91,7 @@ struct Vox;
 template <>
 struct Vox<MCG_VOXEL_SHORT2> {
     using T = short2;  // {tsdf, w}: w is a ushort, only ==0 is tested
+    static constexpr int bytes = 4;
     static __device__ __forceinline__ T fill() { return make_short2(0, 0); }
     static __device__ __forceinline__ bool neg(T v) { return v.x < 0; }
     static __device__ __forceinline__ bool w0(T v) { return v.y == 0; }
@@ -75,6 +105,7 @@ struct Vox<MCG_VOXEL_SHORT2> {
 template <>
 struct Vox<MCG_VOXEL_FLOAT2> {
     using T = float2;
+    static constexpr int bytes = 8;
     static __device__ __forceinline__ T fill() { return make_float2(0.f, 0.f); }
     static __device__ __forceinline__ bool neg(T v) { return v.x < 0.f; }
     static __device__ __forceinline__ bool w0(T v) { return v.y == 0.f; }
@@ -88,155 +119,299 @@ __device__ __forceinline__ long long lin3(int nx, int ny, int x, int y, int z) {
     return ((long long)z * ny + y) * nx + x;
 }
 
-// ---- pass 1: classify ------------------------------------------------------
-template <int VT>
-__global__ void __launch_bounds__(THREADS)
-    mc_classify_kernel(const typename Vox<VT>::T *__restrict__ vol, int nx, int ny, int nz,
-                       int nbx, int nby, long long nbricks, uint32_t *__restrict__ brick_tris,
-                       uint32_t *__restrict__ brick_occ) {
-    using V = Vox<VT>;
-    __shared__ unsigned char s_ntri[256];
-    __shared__ unsigned char s_flag[CTILE];
-    __shared__ unsigned int s_red[2][WARPS];
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    // triangles per case; cases 0 and 255 emit nothing (:136)
-    s_ntri[tid] = (tid == 0 || tid == 255) ? 0 : c_nverts[tid] / 3;
+struct BrickPos {
+    int x0, y0, z0;
+};
 
-    for (long long b = blockIdx.x; b < nbricks; b += gridDim.x) {
-        const int bx = (int)(b % nbx);
-        const long long r = b / nbx;
-        const int by = (int)(r % nby), bz = (int)(r / nby);
-        const int x0 = bx * BX, y0 = by * BY, z0 = bz * BZ;
-        __syncthreads();  // s_flag reuse
-        // flags: bit0 = tsdf < 0, bit1 = weight == 0 (outside volume counts as w == 0)
-        for (int i = tid; i < CTILE; i += THREADS) {
-            const int lx = i % CX1, t = i / CX1, ly = t % CY1, lz = t / CY1;
-            const int gx = x0 + lx, gy = y0 + ly, gz = z0 + lz;
-            unsigned char fl = 2;
-            if (gx < nx && gy < ny && gz < nz) {
-                const typename V::T v = vol[lin3(nx, ny, gx, gy, gz)];
-                fl = (unsigned char)(V::neg(v) | (V::w0(v) << 1));
+__device__ __forceinline__ BrickPos brick_pos(long long b, int nbx, int nby) {
+    BrickPos p;
+    const long long r = b / nbx;
+    p.x0 = (int)(b % nbx) * BX;
+    p.y0 = (int)(r % nby) * BY;
+    p.z0 = (int)(r / nby) * BZ;
+    return p;
+}
+
+// Plain-load fill of a (DX, DY, DZ) tile whose origin is (ox, oy, oz);
+// outside the volume reads as the zero voxel, like the TMA fill.
+template <int VT, int DX, int DY, int DZ>
+__device__ __forceinline__ void fill_tile(typename Vox<VT>::T *tile, const typename Vox<VT>::T *__restrict__ vol,
+                                          int nx, int ny, int nz, int ox, int oy, int oz) {
+    for (int i = threadIdx.x; i < DX * DY * DZ; i += THREADS) {
+        const int lx = i % DX, t = i / DX, ly = t % DY, lz = t / DY;
+        const int gx = ox + lx, gy = oy + ly, gz = oz + lz;
+        typename Vox<VT>::T v = Vox<VT>::fill();
+        if (gx >= 0 && gy >= 0 && gz >= 0 && gx < nx && gy < ny && gz < nz) v = vol[lin3(nx, ny, gx, gy, gz)];
+        tile[i] = v;
+    }
+}
+
+// Row masks: bit k of neg / dead = voxel (x0 + k) of a 33-voxel row is
+// negative / has weight 0, k = 0..32.  One thread builds one row from 16-byte
+// shared-memory loads (`row` must be 16-byte aligned and readable for 36
+// voxels): about 4 integer operations per voxel instead of a warp vote per
+// row.
+template <int VT>
+struct RowMask;
+
+template <>
+struct RowMask<MCG_VOXEL_SHORT2> {
+    static __device__ __forceinline__ void build(const short2 *row, unsigned long long &neg,
+                                                 unsigned long long &dead) {
+        const uint4 *q = reinterpret_cast<const uint4 *>(row);
+        unsigned int n = 0, d = 0;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const uint4 v = q[k];
+            const unsigned int w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                n |= ((w[j] >> 15) & 1u) << (4 * k + j);     // tsdf (low half) < 0
+                d |= (unsigned int)(w[j] < 0x10000u) << (4 * k + j);  // w (high half) == 0
             }
-            s_flag[i] = fl;
+        }
+        const unsigned int w32 = q[8].x;
+        neg = (unsigned long long)n | ((unsigned long long)((w32 >> 15) & 1u) << 32);
+        dead = (unsigned long long)d | ((unsigned long long)(w32 < 0x10000u) << 32);
+    }
+};
+
+template <>
+struct RowMask<MCG_VOXEL_FLOAT2> {
+    static __device__ __forceinline__ void build(const float2 *row, unsigned long long &neg,
+                                                 unsigned long long &dead) {
+        const float4 *q = reinterpret_cast<const float4 *>(row);
+        unsigned int n = 0, d = 0;
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+            const float4 v = q[k];
+            n |= (unsigned int)(v.x < 0.f) << (2 * k);
+            n |= (unsigned int)(v.z < 0.f) << (2 * k + 1);
+            d |= (unsigned int)(v.y == 0.f) << (2 * k);
+            d |= (unsigned int)(v.w == 0.f) << (2 * k + 1);
+        }
+        const float4 v32 = q[16];
+        neg = (unsigned long long)n | ((unsigned long long)(v32.x < 0.f) << 32);
+        dead = (unsigned long long)d | ((unsigned long long)(v32.y == 0.f) << 32);
+    }
+};
+
+// Occupied-cube mask of cube row (cy, cz) of a brick: bit x set iff cube x
+// has a sign change and no weight-0 corner (cu_marching_cubes_v1.cu:74-91,
+// :136 -- every case other than 0 and 255 emits triangles).
+struct CubeRow {
+    unsigned long long a, b, c, d;  // neg masks of rows (y,z), (y+1,z), (y,z+1), (y+1,z+1)
+    unsigned int occ;
+};
+
+__device__ __forceinline__ CubeRow cube_row(const unsigned long long *neg, const unsigned long long *dead, int cy,
+                                            int cz, unsigned int valid) {
+    CubeRow r;
+    const int r00 = cz * (BY + 1) + cy, r01 = r00 + 1, r10 = r00 + (BY + 1), r11 = r10 + 1;
+    r.a = neg[r00];
+    r.b = neg[r01];
+    r.c = neg[r10];
+    r.d = neg[r11];
+    const unsigned long long all = r.a & (r.a >> 1) & r.b & (r.b >> 1) & r.c & (r.c >> 1) & r.d & (r.d >> 1);
+    const unsigned long long any = r.a | (r.a >> 1) | r.b | (r.b >> 1) | r.c | (r.c >> 1) | r.d | (r.d >> 1);
+    const unsigned long long da = dead[r00], db = dead[r01], dc = dead[r10], dd = dead[r11];
+    const unsigned long long dz = da | (da >> 1) | db | (db >> 1) | dc | (dc >> 1) | dd | (dd >> 1);
+    r.occ = (unsigned int)(any & ~all & ~dz) & valid;
+    return r;
+}
+
+// cube index of cube x of a row (bit i = corner i negative)
+__device__ __forceinline__ unsigned int cube_index(const CubeRow &r, int x) {
+    return (unsigned int)(((r.a >> x) & 1) | (((r.a >> (x + 1)) & 1) << 1) | (((r.b >> (x + 1)) & 1) << 2) |
+                          (((r.b >> x) & 1) << 3) | (((r.c >> x) & 1) << 4) | (((r.c >> (x + 1)) & 1) << 5) |
+                          (((r.d >> (x + 1)) & 1) << 6) | (((r.d >> x) & 1) << 7));
+}
+
+__device__ __forceinline__ unsigned int valid_mask(int x0, int nx) {
+    const int nvalid = nx - 1 - x0;  // cubes exist for x < nx - 1
+    return nvalid >= 32 ? 0xffffffffu : (nvalid <= 0 ? 0u : ((1u << nvalid) - 1u));
+}
+
+// ---- pass 1: classify ------------------------------------------------------
+constexpr int CTHREADS = 128;
+
+template <int VT, int CSTAGES>
+struct ClsSmem {
+    static constexpr int STAGE_BYTES = pad128(CTILE * Vox<VT>::bytes);
+    unsigned char tiles[CSTAGES][STAGE_BYTES];
+    unsigned long long neg[ROWS], dead[ROWS];
+    uint64_t bars[CSTAGES];
+    unsigned int red[2][2];
+    unsigned char ntri[256];
+    int abort;
+};
+
+template <int VT, bool TMA, int CSTAGES>
+__global__ void __launch_bounds__(CTHREADS)
+    mc_classify_kernel(const __grid_constant__ CUtensorMap map, const typename Vox<VT>::T *__restrict__ vol,
+                       int nx, int ny, int nz, int nbx, int nby, long long nbricks,
+                       uint32_t *__restrict__ brick_tris, uint32_t *__restrict__ chunk,
+                       unsigned int *__restrict__ flags) {
+    using V = Vox<VT>;
+    using T = typename V::T;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    ClsSmem<VT, CSTAGES> &S = *reinterpret_cast<ClsSmem<VT, CSTAGES> *>(smem_raw);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const long long stride = gridDim.x;
+    for (int c = tid; c < 256; c += CTHREADS) S.ntri[c] = (c == 0 || c == 255) ? 0 : c_nverts[c] / 3;
+    if (tid == 0) {
+        S.abort = 0;
+        if (TMA) {
+            for (int s = 0; s < CSTAGES; ++s) mbar_init(&S.bars[s], 1);
+            fence_barrier_init();
+            for (int s = 0; s < CSTAGES; ++s) {
+                const long long b = blockIdx.x + s * stride;
+                if (b >= nbricks) break;
+                const BrickPos bp = brick_pos(b, nbx, nby);
+                mbar_arrive_expect_tx(&S.bars[s], CTILE * V::bytes);
+                tma_load_3d(S.tiles[s], &map, &S.bars[s], bp.x0, bp.y0, bp.z0);
+            }
+        }
+    }
+    __syncthreads();
+    for (int i = 0;; ++i) {
+        const long long b = blockIdx.x + (long long)i * stride;
+        if (b >= nbricks) break;
+        const int s = TMA ? i % CSTAGES : 0;
+        const BrickPos bp = brick_pos(b, nbx, nby);
+        T *tile = reinterpret_cast<T *>(S.tiles[s]);
+        if (TMA) {
+            // one thread polls the barrier; the others wait at __syncthreads
+            if (tid == 0 && !mbar_wait(&S.bars[s], (uint32_t)((i / CSTAGES) & 1))) S.abort = 1;
+        } else {
+            for (int k = tid; k < CTILE; k += CTHREADS) {
+                const int lx = k % CTX, t = k / CTX, ly = t % CTY, lz = t / CTY;
+                const int gx = bp.x0 + lx, gy = bp.y0 + ly, gz = bp.z0 + lz;
+                T v = V::fill();
+                if (gx < nx && gy < ny && gz < nz) v = vol[lin3(nx, ny, gx, gy, gz)];
+                tile[k] = v;
+            }
         }
         __syncthreads();
-        unsigned int tri = 0, occ = 0;
-        const int cx = lane, cy = warp;
-        if (x0 + cx < nx - 1 && y0 + cy < ny - 1) {
-            const unsigned char *p = s_flag + cy * CX1 + cx;
-            // rolling pair of voxel planes along z
-            unsigned int a0 = p[0], a1 = p[1], a2 = p[CX1 + 1], a3 = p[CX1];
-            const int zend = min(BZ, nz - 1 - z0);
-            for (int cz = 0; cz < zend; ++cz) {
-                const unsigned char *q = p + (cz + 1) * (CX1 * CY1);
-                const unsigned int b0 = q[0], b1 = q[1], b2 = q[CX1 + 1], b3 = q[CX1];
-                const unsigned int any = a0 | a1 | a2 | a3 | b0 | b1 | b2 | b3;
-                if (!(any & 2)) {
-                    const unsigned int ci = (a0 & 1) | ((a1 & 1) << 1) | ((a2 & 1) << 2) |
-                                            ((a3 & 1) << 3) | ((b0 & 1) << 4) | ((b1 & 1) << 5) |
-                                            ((b2 & 1) << 6) | ((b3 & 1) << 7);
-                    const unsigned int nt = s_ntri[ci];
-                    tri += nt;
-                    occ += nt > 0;
+        if (S.abort) break;
+        if (tid < ROWS) RowMask<VT>::build(tile + tid * CTX, S.neg[tid], S.dead[tid]);
+        __syncthreads();
+        if (tid < CUBE_ROWS) {
+            const int cy = tid & (BY - 1), cz = tid / BY;
+            unsigned int tri = 0, occ = 0;
+            if (bp.y0 + cy < ny - 1 && bp.z0 + cz < nz - 1) {
+                const CubeRow cr = cube_row(S.neg, S.dead, cy, cz, valid_mask(bp.x0, nx));
+                occ = __popc(cr.occ);
+                unsigned int m = cr.occ;
+                while (m) {
+                    const int x = __ffs(m) - 1;
+                    m &= m - 1;
+                    tri += S.ntri[cube_index(cr, x)];
                 }
-                a0 = b0; a1 = b1; a2 = b2; a3 = b3;
+            }
+            tri = __reduce_add_sync(0xffffffffu, tri);
+            occ = __reduce_add_sync(0xffffffffu, occ);
+            if (lane == 0) {
+                S.red[warp][0] = tri;
+                S.red[warp][1] = occ;
             }
         }
-#pragma unroll
-        for (int o = 16; o; o >>= 1) {
-            tri += __shfl_xor_sync(0xffffffffu, tri, o);
-            occ += __shfl_xor_sync(0xffffffffu, occ, o);
-        }
-        if (lane == 0) { s_red[0][warp] = tri; s_red[1][warp] = occ; }
-        __syncthreads();
+        __syncthreads();  // tile s consumed, red[] complete
         if (tid == 0) {
-            unsigned int t = 0, o = 0;
-#pragma unroll
-            for (int w = 0; w < WARPS; ++w) { t += s_red[0][w]; o += s_red[1][w]; }
+            const unsigned int t = S.red[0][0] + S.red[1][0], o = S.red[0][1] + S.red[1][1];
             brick_tris[b] = t;
-            brick_occ[b] = o;
+            // per-chunk (CHUNK consecutive bricks) sums feed the scan
+            if (t) {
+                atomicAdd(&chunk[(b / CHUNK) * 3 + 0], t);
+                atomicAdd(&chunk[(b / CHUNK) * 3 + 1], 1u);
+                atomicAdd(&chunk[(b / CHUNK) * 3 + 2], o);
+            }
+            if (TMA) {
+                const long long nb = b + CSTAGES * stride;
+                if (nb < nbricks) {
+                    const BrickPos np = brick_pos(nb, nbx, nby);
+                    mbar_arrive_expect_tx(&S.bars[s], CTILE * V::bytes);
+                    tma_load_3d(S.tiles[s], &map, &S.bars[s], np.x0, np.y0, np.z0);
+                }
+            }
         }
+    }
+    if (S.abort && tid == 0) {
+        atomicOr(flags, 1u);
+        // give loads still in flight a bounded chance to land before exit
+        for (int s = 0; s < CSTAGES; ++s) mbar_wait(&S.bars[s], 0, 100000000ull);
     }
 }
 
 // ---- scan: brick counts -> soup offsets + active brick list ---------------------
-constexpr int SCAN_THREADS = 1024;
-constexpr int SCAN_PER = 8;
-
-__global__ void __launch_bounds__(SCAN_THREADS)
-    mc_scan_kernel(const uint32_t *__restrict__ brick_tris, const uint32_t *__restrict__ brick_occ,
-                   long long nb, unsigned long long *__restrict__ brick_vofs,
-                   uint32_t *__restrict__ active, MeshTotals *__restrict__ totals) {
-    __shared__ unsigned long long s_wv[32];
-    __shared__ unsigned int s_wa[32];
-    __shared__ unsigned long long s_occ[32];
+// One CTA per chunk of CHUNK consecutive bricks.  Classify has accumulated
+// each chunk's (triangles, active bricks, occupied cubes); a CTA adds up the
+// chunks before its own for its base offsets, scans its bricks, and writes
+// 64-bit soup offsets and its part of the active-brick list (brick order).
+// CTA 0 also writes the totals.
+__global__ void __launch_bounds__(CHUNK)
+    mc_scan_kernel(const uint32_t *__restrict__ brick_tris, const uint32_t *__restrict__ chunk, long long nb,
+                   unsigned long long *__restrict__ brick_vofs, uint32_t *__restrict__ active,
+                   MeshTotals *__restrict__ totals) {
+    __shared__ unsigned long long s_part[5][CHUNK / 32];
+    __shared__ unsigned long long s_base_v;
+    __shared__ unsigned int s_base_a;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    unsigned long long carry_v = 0, occ_sum = 0;
-    unsigned int carry_a = 0;
-    for (long long base = 0; base < nb; base += (long long)SCAN_THREADS * SCAN_PER) {
-        const long long i0 = base + (long long)tid * SCAN_PER;
-        uint32_t t[SCAN_PER];
-        unsigned long long lv = 0;
-        unsigned int la = 0;
-#pragma unroll
-        for (int k = 0; k < SCAN_PER; ++k) {
-            const long long i = i0 + k;
-            t[k] = i < nb ? brick_tris[i] : 0u;
-            occ_sum += i < nb ? brick_occ[i] : 0u;
-            lv += t[k];
-            la += t[k] != 0;
-        }
-        // warp inclusive scans
-        unsigned long long iv = lv;
-        unsigned int ia = la;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const unsigned long long nv = __shfl_up_sync(0xffffffffu, iv, o);
-            const unsigned int na = __shfl_up_sync(0xffffffffu, ia, o);
-            if (lane >= o) { iv += nv; ia += na; }
-        }
-        if (lane == 31) { s_wv[warp] = iv; s_wa[warp] = ia; }
-        __syncthreads();
-        if (warp == 0) {
-            unsigned long long wv = s_wv[lane];
-            unsigned int wa = s_wa[lane];
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const unsigned long long nv = __shfl_up_sync(0xffffffffu, wv, o);
-                const unsigned int na = __shfl_up_sync(0xffffffffu, wa, o);
-                if (lane >= o) { wv += nv; wa += na; }
-            }
-            s_wv[lane] = wv;  // inclusive over warps
-            s_wa[lane] = wa;
-        }
-        __syncthreads();
-        unsigned long long ev = carry_v + (warp ? s_wv[warp - 1] : 0ull) + (iv - lv);
-        unsigned int ea = carry_a + (warp ? s_wa[warp - 1] : 0u) + (ia - la);
-#pragma unroll
-        for (int k = 0; k < SCAN_PER; ++k) {
-            const long long i = i0 + k;
-            if (i < nb) {
-                brick_vofs[i] = 3ull * ev;
-                if (t[k]) active[ea++] = (uint32_t)i;
-            }
-            ev += t[k];
-        }
-        carry_v += s_wv[31];
-        carry_a += s_wa[31];
-        __syncthreads();
+    const long long j = blockIdx.x;
+    const long long nchunks = (nb + CHUNK - 1) / CHUNK;
+    // base offsets: sums over the chunks before this one; CTA 0 also sums all
+    // chunks for the totals
+    const long long upto = j == 0 ? nchunks : j;
+    unsigned long long acc[5] = {0, 0, 0, 0, 0};  // base tris, base active, all tris, all active, all occupied
+    for (long long i = tid; i < upto; i += CHUNK) {
+        const unsigned long long cv = chunk[i * 3 + 0], ca = chunk[i * 3 + 1];
+        if (i < j) { acc[0] += cv; acc[1] += ca; }
+        acc[2] += cv;
+        acc[3] += ca;
+        acc[4] += chunk[i * 3 + 2];
     }
 #pragma unroll
-    for (int o = 16; o; o >>= 1) occ_sum += __shfl_xor_sync(0xffffffffu, occ_sum, o);
-    if (lane == 0) s_occ[warp] = occ_sum;
+    for (int k = 0; k < 5; ++k) {
+#pragma unroll
+        for (int o = 16; o; o >>= 1) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], o);
+        if (lane == 0) s_part[k][warp] = acc[k];
+    }
     __syncthreads();
     if (tid == 0) {
-        unsigned long long o = 0;
-        for (int w = 0; w < SCAN_THREADS / 32; ++w) o += s_occ[w];
-        totals->occupied = o;
-        totals->triangles = carry_v;
-        totals->vertices = 3ull * carry_v;
-        totals->active_bricks = carry_a;
-        totals->pad = 0;
+        unsigned long long r[5] = {0, 0, 0, 0, 0};
+        for (int k = 0; k < 5; ++k)
+            for (int w = 0; w < CHUNK / 32; ++w) r[k] += s_part[k][w];
+        s_base_v = r[0];
+        s_base_a = (unsigned int)r[1];
+        if (j == 0) {
+            totals->occupied = r[4];
+            totals->triangles = r[2];
+            totals->vertices = 3ull * r[2];
+            totals->active_bricks = (unsigned int)r[3];
+        }
+    }
+    __syncthreads();
+    const unsigned long long base_v = s_base_v;
+    const unsigned int base_a = s_base_a;
+    // scan of this chunk's bricks
+    const long long b = j * CHUNK + tid;
+    const unsigned int t = b < nb ? brick_tris[b] : 0u;
+    const unsigned int f = t != 0;
+    unsigned int it = t, ia = f;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned int x = __shfl_up_sync(0xffffffffu, it, o);
+        const unsigned int y = __shfl_up_sync(0xffffffffu, ia, o);
+        if (lane >= o) { it += x; ia += y; }
+    }
+    __shared__ unsigned int s_wt[CHUNK / 32], s_wa[CHUNK / 32];
+    if (lane == 31) { s_wt[warp] = it; s_wa[warp] = ia; }
+    __syncthreads();
+    unsigned int wt = 0, wa = 0;
+    for (int w = 0; w < warp; ++w) { wt += s_wt[w]; wa += s_wa[w]; }
+    if (b < nb) {
+        brick_vofs[b] = 3ull * (base_v + wt + it - t);
+        if (t) active[base_a + wa + ia - f] = (uint32_t)b;
     }
 }
 
@@ -320,7 +495,7 @@ struct GenParams {
     int nbx, nby;
     const uint32_t *active;
     const unsigned long long *brick_vofs;
-    const MeshTotals *totals;
+    MeshTotals *totals;
     mcg_vertex_voxel *soup;
     float *normals;
     int32_t *vi2vox;
@@ -331,23 +506,31 @@ struct GenParams {
 
 template <int VT>
 struct GenSmem {
-    typename Vox<VT>::T tile[TILE];
+    static constexpr int STAGE_BYTES = pad128(GTILE * Vox<VT>::bytes);
+    unsigned char tiles[GSTAGES][STAGE_BYTES];
+    unsigned long long neg[ROWS], dead[ROWS];
+    uint64_t bars[GSTAGES];
+    unsigned int stage[WARPS][32 * 7];
+    unsigned short occ_cube[BRICK_CUBES];  // local cube index (z*8 + y)*32 + x, in that order
+    unsigned short occ_off[BRICK_CUBES];   // exclusive soup-vertex offset inside the brick
+    unsigned char occ_ci[BRICK_CUBES];
     signed char tri[256][16];
     unsigned char nv[256];
-    unsigned char ci[BRICK_CUBES];
-    unsigned short off[BRICK_CUBES];
-    unsigned int stage[WARPS][32 * 7];
-    unsigned int wsum[BZ][WARPS];
-    unsigned int total;
+    unsigned short vmap[BRICK_CUBES];      // soup vertex -> list entry, when the brick has <= 2048
+    long long sbrick[GSTAGES];             // brick id and soup offset of each stage's tile
+    unsigned long long svbase[GSTAGES];
+    unsigned int wsum[2][2];
+    unsigned int nocc, total;
+    int abort;
 };
 
 __device__ __forceinline__ int tidx(int lx, int ly, int lz) { return (lz * TY + ly) * TX + lx; }
 
-template <int VT>
-__global__ void __launch_bounds__(THREADS) mc_generate_kernel(GenParams p) {
+template <int VT, bool TMA>
+__global__ void __launch_bounds__(THREADS, 4) mc_generate_kernel(const __grid_constant__ CUtensorMap map, GenParams p) {
     using V = Vox<VT>;
     using T = typename V::T;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     GenSmem<VT> &S = *reinterpret_cast<GenSmem<VT> *>(smem_raw);
     const T *__restrict__ vol = static_cast<const T *>(p.vol);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -357,83 +540,108 @@ __global__ void __launch_bounds__(THREADS) mc_generate_kernel(GenParams p) {
 
     for (int i = tid; i < 256 * 16; i += THREADS) (&S.tri[0][0])[i] = (&c_tri[0][0])[i];
     S.nv[tid] = (tid == 0 || tid == 255) ? 0 : c_nverts[tid];
-
+    if (tid == 0) {
+        S.abort = 0;
+        if (TMA) {
+            for (int s = 0; s < GSTAGES; ++s) mbar_init(&S.bars[s], 1);
+            fence_barrier_init();
+        }
+    }
+    __syncthreads();
     const unsigned int nactive = p.totals->active_bricks;
-    for (unsigned int w = blockIdx.x; w < nactive; w += gridDim.x) {
-        const long long b = p.active[w];
-        const unsigned long long vbase = p.brick_vofs[b];
-        const int bx = (int)(b % p.nbx);
-        const long long r = b / p.nbx;
-        const int by = (int)(r % p.nby), bz = (int)(r / p.nby);
-        const int x0 = bx * BX, y0 = by * BY, z0 = bz * BZ;
-        __syncthreads();  // previous brick finished with the tile
-        for (int i = tid; i < TILE; i += THREADS) {
-            const int lx = i % TX, t = i / TX, ly = t % TY, lz = t / TY;
-            const int gx = x0 - 1 + lx, gy = y0 - 1 + ly, gz = z0 - 1 + lz;
-            T v = V::fill();
-            if (gx >= 0 && gy >= 0 && gz >= 0 && gx < nx && gy < ny && gz < nz)
-                v = vol[lin3(nx, ny, gx, gy, gz)];
-            S.tile[i] = v;
+    if (TMA && tid == 0) {
+        for (int s = 0; s < GSTAGES; ++s) {
+            const unsigned int w = blockIdx.x + s * gridDim.x;
+            if (w >= nactive) break;
+            const long long b = p.active[w];
+            S.sbrick[s] = b;
+            S.svbase[s] = p.brick_vofs[b];
+            const BrickPos bp = brick_pos(b, p.nbx, p.nby);
+            mbar_arrive_expect_tx(&S.bars[s], GTILE * V::bytes);
+            tma_load_3d(S.tiles[s], &map, &S.bars[s], bp.x0 - TXO, bp.y0 - TYO, bp.z0 - TZO);
         }
-        __syncthreads();
+    }
+    int it = 0;
+    for (unsigned int w = blockIdx.x; w < nactive; w += gridDim.x, ++it) {
+        const int s = TMA ? it % GSTAGES : 0;
+        const T *tile = reinterpret_cast<const T *>(S.tiles[s]);
+        long long b;
+        unsigned long long vbase;
+        if (TMA) {
+            if (tid == 0 && !mbar_wait(&S.bars[s], (uint32_t)((it / GSTAGES) & 1))) S.abort = 1;
+            __syncthreads();
+            if (S.abort) break;
+            b = S.sbrick[s];
+            vbase = S.svbase[s];
+        } else {
+            b = p.active[w];
+            vbase = p.brick_vofs[b];
+            const BrickPos fp = brick_pos(b, p.nbx, p.nby);
+            fill_tile<VT, TX, TY, TZ>(reinterpret_cast<T *>(S.tiles[s]), vol, nx, ny, nz, fp.x0 - TXO,
+                                      fp.y0 - TYO, fp.z0 - TZO);
+            __syncthreads();
+        }
+        const BrickPos bp = brick_pos(b, p.nbx, p.nby);
+        const int x0 = bp.x0, y0 = bp.y0, z0 = bp.z0;
 
-        // classify the brick's cubes; thread (lane, warp) owns column (x, y)
-        unsigned int nvs[BZ];
-        const int cx = lane, cy = warp;
-        const bool col_ok = (x0 + cx < nx - 1) && (y0 + cy < ny - 1);
-#pragma unroll
-        for (int cz = 0; cz < BZ; ++cz) {
-            unsigned int ci = 0;
-            if (col_ok && z0 + cz < nz - 1) {
-                bool dead = false;
-#pragma unroll
-                for (int c = 0; c < 8; ++c) {
-                    const T v = S.tile[tidx(cx + 1 + c_cx(c), cy + 1 + c_cy(c), cz + 1 + c_cz(c))];
-                    dead |= V::w0(v);
-                    ci |= (unsigned int)V::neg(v) << c;
-                }
-                if (dead) ci = 0;
-            }
-            const int idx = (cz * BY + cy) * BX + cx;
-            S.ci[idx] = (unsigned char)ci;
-            nvs[cz] = S.nv[ci];
+        // occupied cubes of the brick, from row masks (voxel rows y0..y0+8, z0..z0+8)
+        if (tid < ROWS) {
+            const int ry = tid % (BY + 1), rz = tid / (BY + 1);
+            RowMask<VT>::build(tile + tidx(TXO, ry + TYO, rz + TZO), S.neg[tid], S.dead[tid]);
         }
-        // exclusive scan in (z, y, x) order: warp scans per z-row, then rows x warps
-        unsigned int incl[BZ];
-#pragma unroll
-        for (int cz = 0; cz < BZ; ++cz) {
-            unsigned int x = nvs[cz];
+        __syncthreads();
+        CubeRow cr;
+        cr.occ = 0;
+        unsigned int cnt = 0, vsum = 0;
+        if (tid < CUBE_ROWS) {
+            const int cy = tid & (BY - 1), cz = tid / BY;
+            if (y0 + cy < ny - 1 && z0 + cz < nz - 1) cr = cube_row(S.neg, S.dead, cy, cz, valid_mask(x0, nx));
+            cnt = __popc(cr.occ);
+            unsigned int m = cr.occ;
+            while (m) {
+                const int x = __ffs(m) - 1;
+                m &= m - 1;
+                vsum += S.nv[cube_index(cr, x)];
+            }
+            // exclusive scans over the 64 cube rows (row = tid, (z, y) order)
+            unsigned int ic = cnt, iv = vsum;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
-                const unsigned int y = __shfl_up_sync(0xffffffffu, x, o);
-                if (lane >= o) x += y;
+                const unsigned int a = __shfl_up_sync(0xffffffffu, ic, o);
+                const unsigned int c = __shfl_up_sync(0xffffffffu, iv, o);
+                if (lane >= o) { ic += a; iv += c; }
             }
-            incl[cz] = x;
-            if (lane == 31) S.wsum[cz][warp] = x;
+            if (lane == 31) { S.wsum[warp][0] = ic; S.wsum[warp][1] = iv; }
+            cnt = ic - cnt;  // now exclusive
+            vsum = iv - vsum;
         }
         __syncthreads();
-        if (warp == 0) {
-            // 64 (row, warp) sums in row-major order, 2 per lane
-            const unsigned int a = (&S.wsum[0][0])[2 * lane], c = (&S.wsum[0][0])[2 * lane + 1];
-            unsigned int x = a + c;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const unsigned int y = __shfl_up_sync(0xffffffffu, x, o);
-                if (lane >= o) x += y;
+        if (tid < CUBE_ROWS) {
+            if (warp == 1) { cnt += S.wsum[0][0]; vsum += S.wsum[0][1]; }
+            const int cy = tid & (BY - 1), cz = tid / BY;
+            unsigned int m = cr.occ;
+            const bool small = S.wsum[0][1] + S.wsum[1][1] <= BRICK_CUBES;
+            while (m) {
+                const int x = __ffs(m) - 1;
+                m &= m - 1;
+                const unsigned int ci = cube_index(cr, x);
+                const unsigned int nvc = S.nv[ci];
+                S.occ_cube[cnt] = (unsigned short)((cz * BY + cy) * BX + x);
+                S.occ_ci[cnt] = (unsigned char)ci;
+                S.occ_off[cnt] = (unsigned short)vsum;
+                if (small)
+                    for (unsigned int q = 0; q < nvc; ++q) S.vmap[vsum + q] = (unsigned short)cnt;
+                ++cnt;
+                vsum += nvc;
             }
-            const unsigned int ex = x - a - c;
-            (&S.wsum[0][0])[2 * lane] = ex;
-            (&S.wsum[0][0])[2 * lane + 1] = ex + a;
-            if (lane == 31) S.total = x;
+            if (tid == 0) {
+                S.nocc = S.wsum[0][0] + S.wsum[1][0];
+                S.total = S.wsum[0][1] + S.wsum[1][1];
+            }
         }
         __syncthreads();
-#pragma unroll
-        for (int cz = 0; cz < BZ; ++cz) {
-            const int idx = (cz * BY + cy) * BX + cx;
-            S.off[idx] = (unsigned short)(S.wsum[cz][warp] + incl[cz] - nvs[cz]);
-        }
-        __syncthreads();
-        const unsigned int T_brick = S.total;
+        const unsigned int nocc = S.nocc, T_brick = S.total;
+        const bool use_map = T_brick <= BRICK_CUBES;
 
         // emission: one soup vertex per thread, warps take 32 consecutive vertices
         for (unsigned int v0 = warp * 32; v0 < T_brick; v0 += THREADS) {
@@ -446,25 +654,32 @@ __global__ void __launch_bounds__(THREADS) mc_generate_kernel(GenParams p) {
             long long cube_lin = 0;
             int kslot = 1;
             if (valid) {
-                // owning cube: last c with off[c] <= v
-                int lo = 0, hi = BRICK_CUBES - 1;
-                while (lo < hi) {
-                    const int mid = (lo + hi + 1) >> 1;
-                    if (S.off[mid] <= v) lo = mid; else hi = mid - 1;
+                // owning cube: the map, or the last list entry with off <= v
+                int lo = 0;
+                if (use_map) {
+                    lo = S.vmap[v];
+                } else {
+                    int hi = (int)nocc - 1;
+                    while (lo < hi) {
+                        const int mid = (lo + hi + 1) >> 1;
+                        if (S.occ_off[mid] <= v) lo = mid; else hi = mid - 1;
+                    }
                 }
-                const int c = lo;
+                const int c = S.occ_cube[lo];
                 const int lcx = c & (BX - 1), lcy = (c / BX) & (BY - 1), lcz = c / (BX * BY);
-                const unsigned int ci = S.ci[c];
-                const unsigned int s = v - S.off[c];
-                const unsigned int j = s / 3, k = s - 3 * j;
+                const unsigned int ci = S.occ_ci[lo];
+                const unsigned int sl = v - S.occ_off[lo];
+                const unsigned int j = sl / 3, k = sl - 3 * j;
                 kslot = (int)k;
                 // output slot k of triangle j takes edge tri[3j+2-k] (:322-333)
                 const int e = S.tri[ci][3 * j + 2 - k];
                 const int a = c_ea(e), bb = c_eb(e);
                 const int gx = x0 + lcx, gy = y0 + lcy, gz = z0 + lcz;
                 cube_lin = lin3(nx, ny, gx, gy, gz);
-                const float f0 = V::f(S.tile[tidx(lcx + 1 + c_cx(a), lcy + 1 + c_cy(a), lcz + 1 + c_cz(a))]);
-                const float f1 = V::f(S.tile[tidx(lcx + 1 + c_cx(bb), lcy + 1 + c_cy(bb), lcz + 1 + c_cz(bb))]);
+                const float f0 =
+                    V::f(tile[tidx(lcx + TXO + c_cx(a), lcy + TYO + c_cy(a), lcz + TZO + c_cz(a))]);
+                const float f1 =
+                    V::f(tile[tidx(lcx + TXO + c_cx(bb), lcy + TYO + c_cy(bb), lcz + TZO + c_cz(bb))]);
                 // getNodeCoo (:243-254) and vertex_interp (:256-264)
                 const float t = (0.0f - f0) / (f1 - f0 + 1e-15f);
                 const int ga[3] = {gx + c_cx(a), gy + c_cy(a), gz + c_cz(a)};
@@ -477,18 +692,19 @@ __global__ void __launch_bounds__(THREADS) mc_generate_kernel(GenParams p) {
                 }
                 // store_point (:336-367): voxel of the vertex, its tsdf / w
                 const int dims[3] = {nx, ny, nz};
-                const int org[3] = {x0 - 1, y0 - 1, z0 - 1};
-                // tile path only when the voxel is inside the volume and the tile
+                const int org[3] = {x0 - TXO, y0 - TYO, z0 - TZO};
                 const int tdim[3] = {TX, TY, TZ};
+                // P / cell serves both the voxel (:344-350) and the normal sample (kf.cu:3241)
+                const float pf[3] = {P[0] / cell, P[1] / cell, P[2] / cell};
                 bool inside = true;
 #pragma unroll
                 for (int d = 0; d < 3; ++d) {
-                    vox[d] = (int)floorf(P[d] / cell - 0.5f);
+                    vox[d] = (int)floorf(pf[d] - 0.5f);
                     inside &= vox[d] >= 0 && vox[d] < dims[d] && vox[d] - org[d] >= 0 && vox[d] - org[d] < tdim[d];
                 }
                 const long long li = lin3(nx, ny, vox[0], vox[1], vox[2]);
                 if (inside) {
-                    const T vv = S.tile[tidx(vox[0] - org[0], vox[1] - org[1], vox[2] - org[2])];
+                    const T vv = tile[tidx(vox[0] - org[0], vox[1] - org[1], vox[2] - org[2])];
                     vt = V::tsdf(vv);
                     vw = V::wt(vv);
                 } else if (li >= 0 && li < N) {
@@ -499,15 +715,15 @@ __global__ void __launch_bounds__(THREADS) mc_generate_kernel(GenParams p) {
                 if (p.ver_voxel && li >= 0 && li < N && vbase + v < (unsigned long long)p.cap)
                     p.ver_voxel[li] = vt;
                 if (p.normals) {
-                    const float fx = P[0] / cell, fy = P[1] / cell, fz = P[2] / cell;
+                    const float fx = pf[0], fy = pf[1], fz = pf[2];
                     const int ix = (int)fx, iy = (int)fy, iz = (int)fz;
                     const int lx = ix - org[0], ly = iy - org[1], lz = iz - org[2];
                     if (ix + 1 < nx && iy + 1 < ny && iz + 1 < nz && lx >= 0 && ly >= 0 && lz >= 0 &&
                         lx + 1 < TX && ly + 1 < TY && lz + 1 < TZ) {
-                        const T smp[8] = {S.tile[tidx(lx, ly, lz)],         S.tile[tidx(lx + 1, ly, lz)],
-                                          S.tile[tidx(lx + 1, ly + 1, lz)], S.tile[tidx(lx, ly + 1, lz)],
-                                          S.tile[tidx(lx, ly, lz + 1)],     S.tile[tidx(lx + 1, ly, lz + 1)],
-                                          S.tile[tidx(lx + 1, ly + 1, lz + 1)], S.tile[tidx(lx, ly + 1, lz + 1)]};
+                        const T smp[8] = {tile[tidx(lx, ly, lz)],         tile[tidx(lx + 1, ly, lz)],
+                                          tile[tidx(lx + 1, ly + 1, lz)], tile[tidx(lx, ly + 1, lz)],
+                                          tile[tidx(lx, ly, lz + 1)],     tile[tidx(lx + 1, ly, lz + 1)],
+                                          tile[tidx(lx + 1, ly + 1, lz + 1)], tile[tidx(lx, ly + 1, lz + 1)]};
                         bool sent = false;
                         float sd[8];
 #pragma unroll
@@ -573,6 +789,22 @@ __global__ void __launch_bounds__(THREADS) mc_generate_kernel(GenParams p) {
             if (p.tri_cube && valid && kslot == 0 && (long long)(g0 + lane) + 2 < p.cap)
                 p.tri_cube[(g0 + lane) / 3] = cube_lin;
         }
+        __syncthreads();  // tile s, the list and the stage are free again
+        if (TMA && tid == 0) {
+            const unsigned int wn = w + GSTAGES * gridDim.x;
+            if (wn < nactive) {
+                const long long nb2 = p.active[wn];
+                S.sbrick[s] = nb2;
+                S.svbase[s] = p.brick_vofs[nb2];
+                const BrickPos np = brick_pos(nb2, p.nbx, p.nby);
+                mbar_arrive_expect_tx(&S.bars[s], GTILE * V::bytes);
+                tma_load_3d(S.tiles[s], &map, &S.bars[s], np.x0 - TXO, np.y0 - TYO, np.z0 - TZO);
+            }
+        }
+    }
+    if (S.abort && tid == 0) {
+        atomicOr(&p.totals->flags, 1u);
+        for (int s = 0; s < GSTAGES; ++s) mbar_wait(&S.bars[s], 0, 100000000ull);
     }
 }
 
@@ -590,6 +822,7 @@ __global__ void mc_normals_kernel(const typename Vox<VT>::T *__restrict__ vol, i
     normals[3 * i + 2] = nn.z;
 }
 
+// ---- host side ----------------------------------------------------------------
 bool g_tables_ready[64] = {false};
 
 cudaError_t upload_tables(int device) {
@@ -620,28 +853,139 @@ bool vol_ok(const mcg_volume *v) {
     if (v->nx < 2 || v->ny < 2 || v->nz < 2) return false;
     if (v->voxel_type != MCG_VOXEL_SHORT2 && v->voxel_type != MCG_VOXEL_FLOAT2) return false;
     if (!(v->cell > 0.0f)) return false;
-    // brick coordinates are 32-bit
-    if ((long long)v->nx * v->ny * v->nz > (1ll << 40)) return false;
+    // brick ids are 32-bit in the active list
+    if (geometry(v->nx, v->ny, v->nz).nbricks >= (1ll << 32)) return false;
     return true;
 }
 
-template <int VT>
-size_t gen_smem() { return sizeof(GenSmem<VT>); }
+struct Scratch {
+    uint32_t *tris;
+    uint32_t *chunk;  // 3 per chunk of CHUNK bricks: triangles, active bricks, occupied cubes
+    unsigned long long *vofs;
+    uint32_t *active;
+    MeshTotals *totals;
+};
 
-template <int VT>
-int gen_grid(mcg_context *ctx, long long nbricks) {
-    static int occ[2] = {0, 0};
-    int &o = occ[VT];
-    if (!o) {
-        cudaFuncSetAttribute(mc_generate_kernel<VT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)gen_smem<VT>());
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, mc_generate_kernel<VT>, THREADS,
-                                                          gen_smem<VT>()) != cudaSuccess || o < 1)
-            o = 1;
+template <class K>
+int occupancy(K kernel, int threads, size_t smem) {
+    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int o = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kernel, threads, smem) != cudaSuccess || o < 1) {
+        cudaGetLastError();
+        o = 1;
     }
-    long long g = (long long)ctx->num_sms * o;
-    if (g > nbricks) g = nbricks;
-    return (int)(g < 1 ? 1 : g);
+    return o;
+}
+
+template <int VT, bool TMA, int CSTAGES>
+void launch_classify_s(const CUtensorMap &map, const mcg_volume *vol, const Geometry &g, const Scratch &sc, int sms,
+                       cudaStream_t s) {
+    const size_t smem = sizeof(ClsSmem<VT, CSTAGES>);
+    static int occ = 0;  // per instantiation; all devices of a run are the same part
+    if (!occ) occ = occupancy(mc_classify_kernel<VT, TMA, CSTAGES>, CTHREADS, smem);
+    long long grid = (long long)sms * occ;
+    if (grid > g.nbricks) grid = g.nbricks;
+    mc_classify_kernel<VT, TMA, CSTAGES><<<(int)grid, CTHREADS, smem, s>>>(
+        map, static_cast<const typename Vox<VT>::T *>(vol->data), vol->nx, vol->ny, vol->nz, g.nbx, g.nby,
+        g.nbricks, sc.tris, sc.chunk, &sc.totals->flags);
+}
+
+// pipeline depth of the classify pass (tile stages per CTA); MCG_CLS_STAGES
+// overrides it for tuning
+int classify_stages() {
+    static int st = 0;
+    if (!st) {
+        st = 2;
+        if (const char *e = getenv("MCG_CLS_STAGES")) {
+            const int v = atoi(e);
+            if (v == 2 || v == 3 || v == 4) st = v;
+        }
+    }
+    return st;
+}
+
+template <int VT, bool TMA>
+void launch_classify_t(const CUtensorMap &map, const mcg_volume *vol, const Geometry &g, const Scratch &sc, int sms,
+                       cudaStream_t s) {
+    // without TMA only one stage is ever used
+    const int st = TMA ? classify_stages() : 2;
+    if (st == 4) launch_classify_s<VT, TMA, 4>(map, vol, g, sc, sms, s);
+    else if (st == 3) launch_classify_s<VT, TMA, 3>(map, vol, g, sc, sms, s);
+    else launch_classify_s<VT, TMA, 2>(map, vol, g, sc, sms, s);
+}
+
+template <int VT, bool TMA>
+void launch_generate_t(const CUtensorMap &map, const GenParams &p, const Geometry &g, int sms, cudaStream_t s) {
+    const size_t smem = sizeof(GenSmem<VT>);
+    static int occ = 0;
+    if (!occ) occ = occupancy(mc_generate_kernel<VT, TMA>, THREADS, smem);
+    long long grid = (long long)sms * occ;
+    if (grid > g.nbricks) grid = g.nbricks;
+    mc_generate_kernel<VT, TMA><<<(int)grid, THREADS, smem, s>>>(map, p);
+}
+
+// classify + scan into sc; clears the timeout flag first
+long long num_chunks(long long nbricks) { return (nbricks + CHUNK - 1) / CHUNK; }
+
+cudaError_t launch_count_phase(const mcg_volume *vol, const Geometry &g, const Scratch &sc, int sms, cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(&sc.totals->flags, 0, sizeof(unsigned int), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(sc.chunk, 0, sizeof(uint32_t) * 3 * num_chunks(g.nbricks), s);
+    if (e != cudaSuccess) return e;
+    CUtensorMap map;
+    const int eb = vol->voxel_type == MCG_VOXEL_SHORT2 ? 4 : 8;
+    const bool tma = encode_volume_map(&map, vol->data, vol->nx, vol->ny, vol->nz, eb, CTX, CTY, CTZ);
+    if (!tma) memset(&map, 0, sizeof(map));
+    if (vol->voxel_type == MCG_VOXEL_SHORT2) {
+        if (tma) launch_classify_t<MCG_VOXEL_SHORT2, true>(map, vol, g, sc, sms, s);
+        else launch_classify_t<MCG_VOXEL_SHORT2, false>(map, vol, g, sc, sms, s);
+    } else {
+        if (tma) launch_classify_t<MCG_VOXEL_FLOAT2, true>(map, vol, g, sc, sms, s);
+        else launch_classify_t<MCG_VOXEL_FLOAT2, false>(map, vol, g, sc, sms, s);
+    }
+    mc_scan_kernel<<<(unsigned int)num_chunks(g.nbricks), CHUNK, 0, s>>>(sc.tris, sc.chunk, g.nbricks, sc.vofs,
+                                                                        sc.active, sc.totals);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_generate_phase(const mcg_volume *vol, const Geometry &g, const Scratch &sc,
+                                  const mcg_mesh_out *out, int sms, cudaStream_t s) {
+    if (out->ver_voxel) {
+        cudaError_t e = cudaMemsetAsync(out->ver_voxel, 0, sizeof(int16_t) * (size_t)vol->nx * vol->ny * vol->nz, s);
+        if (e != cudaSuccess) return e;
+    }
+    GenParams p;
+    p.vol = vol->data;
+    p.nx = vol->nx;
+    p.ny = vol->ny;
+    p.nz = vol->nz;
+    p.cell = vol->cell;
+    p.nbx = g.nbx;
+    p.nby = g.nby;
+    p.active = sc.active;
+    p.brick_vofs = sc.vofs;
+    p.totals = sc.totals;
+    p.soup = out->soup;
+    p.normals = out->soup_normals;
+    p.vi2vox = out->vi2vox;
+    p.ver_voxel = out->ver_voxel;
+    p.tri_cube = out->tri_cube;
+    p.cap = out->capacity_vertices;
+    CUtensorMap map;
+    const int eb = vol->voxel_type == MCG_VOXEL_SHORT2 ? 4 : 8;
+    const bool tma = encode_volume_map(&map, vol->data, vol->nx, vol->ny, vol->nz, eb, TX, TY, TZ);
+    if (!tma) memset(&map, 0, sizeof(map));
+    if (vol->voxel_type == MCG_VOXEL_SHORT2) {
+        if (tma) launch_generate_t<MCG_VOXEL_SHORT2, true>(map, p, g, sms, s);
+        else launch_generate_t<MCG_VOXEL_SHORT2, false>(map, p, g, sms, s);
+    } else {
+        if (tma) launch_generate_t<MCG_VOXEL_FLOAT2, true>(map, p, g, sms, s);
+        else launch_generate_t<MCG_VOXEL_FLOAT2, false>(map, p, g, sms, s);
+    }
+    return cudaGetLastError();
+}
+
+Scratch ctx_scratch(mcg_context *ctx) {
+    return Scratch{ctx->brick_tris, ctx->brick_occ, ctx->brick_vofs, ctx->active, ctx->d_totals};
 }
 
 }  // namespace
@@ -657,23 +1001,11 @@ mcg_status mcg_mc_classify(mcg_context *ctx, const mcg_volume *vol, mcg_stream_t
     if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
     const Geometry g = geometry(vol->nx, vol->ny, vol->nz);
     if (!ensure(&ctx->brick_tris, &ctx->brick_tris_cap, (size_t)g.nbricks) ||
-        !ensure(&ctx->brick_occ, &ctx->brick_occ_cap, (size_t)g.nbricks) ||
+        !ensure(&ctx->brick_occ, &ctx->brick_occ_cap, (size_t)(3 * num_chunks(g.nbricks))) ||
         !ensure(&ctx->brick_vofs, &ctx->brick_vofs_cap, (size_t)g.nbricks) ||
         !ensure(&ctx->active, &ctx->active_cap, (size_t)g.nbricks))
         return mcg_cuda_fail(ctx, cudaErrorMemoryAllocation);
-    long long grid = (long long)ctx->num_sms * 8;
-    if (grid > g.nbricks) grid = g.nbricks;
-    if (vol->voxel_type == MCG_VOXEL_SHORT2)
-        mc_classify_kernel<MCG_VOXEL_SHORT2><<<(int)grid, THREADS, 0, s>>>(
-            (const short2 *)vol->data, vol->nx, vol->ny, vol->nz, g.nbx, g.nby, g.nbricks,
-            ctx->brick_tris, ctx->brick_occ);
-    else
-        mc_classify_kernel<MCG_VOXEL_FLOAT2><<<(int)grid, THREADS, 0, s>>>(
-            (const float2 *)vol->data, vol->nx, vol->ny, vol->nz, g.nbx, g.nby, g.nbricks,
-            ctx->brick_tris, ctx->brick_occ);
-    mc_scan_kernel<<<1, SCAN_THREADS, 0, s>>>(ctx->brick_tris, ctx->brick_occ, g.nbricks,
-                                              ctx->brick_vofs, ctx->active, ctx->d_totals);
-    e = cudaGetLastError();
+    e = launch_count_phase(vol, g, ctx_scratch(ctx), ctx->num_sms, s);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(ctx->h_totals, ctx->d_totals, sizeof(MeshTotals), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaEventRecord(ctx->counts_ready, s);
@@ -701,7 +1033,9 @@ mcg_status mcg_mc_counts(mcg_context *ctx, mcg_mesh_counts *out) {
     out->triangles = (int64_t)ctx->h_totals->triangles;
     out->vertices = (int64_t)ctx->h_totals->vertices;
     out->active_bricks = (int64_t)ctx->h_totals->active_bricks;
-    out->status = (ctx->last_capacity >= 0 && out->vertices > ctx->last_capacity) ? MCG_ERR_CAPACITY : MCG_OK;
+    out->status = MCG_OK;
+    if (ctx->h_totals->flags & 1u) out->status = MCG_ERR_TIMEOUT;
+    else if (ctx->last_capacity >= 0 && out->vertices > ctx->last_capacity) out->status = MCG_ERR_CAPACITY;
     out->reserved = 0;
     return (mcg_status)out->status;
 }
@@ -719,35 +1053,10 @@ mcg_status mcg_mc_generate(mcg_context *ctx, const mcg_volume *vol, const mcg_me
     cudaError_t e = cudaSetDevice(ctx->device);
     if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
     const Geometry g = geometry(vol->nx, vol->ny, vol->nz);
-    if (out->ver_voxel) {
-        e = cudaMemsetAsync(out->ver_voxel, 0, sizeof(int16_t) * (size_t)vol->nx * vol->ny * vol->nz, s);
-        if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
-    }
-    GenParams p;
-    p.vol = vol->data;
-    p.nx = vol->nx;
-    p.ny = vol->ny;
-    p.nz = vol->nz;
-    p.cell = vol->cell;
-    p.nbx = g.nbx;
-    p.nby = g.nby;
-    p.active = ctx->active;
-    p.brick_vofs = ctx->brick_vofs;
-    p.totals = ctx->d_totals;
-    p.soup = out->soup;
-    p.normals = out->soup_normals;
-    p.vi2vox = out->vi2vox;
-    p.ver_voxel = out->ver_voxel;
-    p.tri_cube = out->tri_cube;
-    p.cap = out->capacity_vertices;
-    if (vol->voxel_type == MCG_VOXEL_SHORT2) {
-        const int grid = gen_grid<MCG_VOXEL_SHORT2>(ctx, g.nbricks);
-        mc_generate_kernel<MCG_VOXEL_SHORT2><<<grid, THREADS, gen_smem<MCG_VOXEL_SHORT2>(), s>>>(p);
-    } else {
-        const int grid = gen_grid<MCG_VOXEL_FLOAT2>(ctx, g.nbricks);
-        mc_generate_kernel<MCG_VOXEL_FLOAT2><<<grid, THREADS, gen_smem<MCG_VOXEL_FLOAT2>(), s>>>(p);
-    }
-    e = cudaGetLastError();
+    e = launch_generate_phase(vol, g, ctx_scratch(ctx), out, ctx->num_sms, s);
+    // the totals are re-read so a timeout flagged by generate is reported
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(ctx->h_totals, ctx->d_totals, sizeof(MeshTotals), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaEventRecord(ctx->counts_ready, s);
     if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
     ctx->counts_pending = true;
@@ -790,6 +1099,7 @@ namespace {
 constexpr long long kNoAllocBricks = MCG_NOALLOC_MAX_BRICKS;
 constexpr size_t kNoAllocTrisOff = 0;
 constexpr size_t kNoAllocOccOff = kNoAllocTrisOff + sizeof(uint32_t) * kNoAllocBricks;
+static_assert(3 * ((kNoAllocBricks + CHUNK - 1) / CHUNK) <= kNoAllocBricks, "chunk sums fit their region");
 constexpr size_t kNoAllocVofsOff = kNoAllocOccOff + sizeof(uint32_t) * kNoAllocBricks;
 constexpr size_t kNoAllocActiveOff = kNoAllocVofsOff + sizeof(unsigned long long) * kNoAllocBricks;
 constexpr size_t kNoAllocTotalsOff = kNoAllocActiveOff + sizeof(uint32_t) * kNoAllocBricks;
@@ -826,79 +1136,33 @@ extern "C" mcg_status mcg_mc_extract_noalloc(const mcg_volume *vol, const mcg_me
     e = upload_tables(dev);
     if (e != cudaSuccess) { cudaGetLastError(); return MCG_ERR_CUDA; }
     unsigned char *base = g_noalloc_addr[dev];
-    uint32_t *tris = reinterpret_cast<uint32_t *>(base + kNoAllocTrisOff);
-    uint32_t *occ = reinterpret_cast<uint32_t *>(base + kNoAllocOccOff);
-    unsigned long long *vofs = reinterpret_cast<unsigned long long *>(base + kNoAllocVofsOff);
-    uint32_t *active = reinterpret_cast<uint32_t *>(base + kNoAllocActiveOff);
-    MeshTotals *totals = reinterpret_cast<MeshTotals *>(base + kNoAllocTotalsOff);
+    Scratch sc;
+    sc.tris = reinterpret_cast<uint32_t *>(base + kNoAllocTrisOff);
+    sc.chunk = reinterpret_cast<uint32_t *>(base + kNoAllocOccOff);  // 3 * 256 chunk sums at most
+    sc.vofs = reinterpret_cast<unsigned long long *>(base + kNoAllocVofsOff);
+    sc.active = reinterpret_cast<uint32_t *>(base + kNoAllocActiveOff);
+    sc.totals = reinterpret_cast<MeshTotals *>(base + kNoAllocTotalsOff);
     int sms = 0;
     e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) { cudaGetLastError(); return MCG_ERR_CUDA; }
     cudaStream_t s = (cudaStream_t)stream;
-    // every scratch entry read later is written first by these launches, so
-    // nothing carried over from an earlier call is used
-    long long cgrid = (long long)sms * 8;
-    if (cgrid > g.nbricks) cgrid = g.nbricks;
-    if (vol->voxel_type == MCG_VOXEL_SHORT2)
-        mc_classify_kernel<MCG_VOXEL_SHORT2><<<(int)cgrid, THREADS, 0, s>>>(
-            (const short2 *)vol->data, vol->nx, vol->ny, vol->nz, g.nbx, g.nby, g.nbricks, tris, occ);
-    else
-        mc_classify_kernel<MCG_VOXEL_FLOAT2><<<(int)cgrid, THREADS, 0, s>>>(
-            (const float2 *)vol->data, vol->nx, vol->ny, vol->nz, g.nbx, g.nby, g.nbricks, tris, occ);
-    mc_scan_kernel<<<1, SCAN_THREADS, 0, s>>>(tris, occ, g.nbricks, vofs, active, totals);
-    if (out->ver_voxel) {
-        e = cudaMemsetAsync(out->ver_voxel, 0, sizeof(int16_t) * (size_t)vol->nx * vol->ny * vol->nz, s);
-        if (e != cudaSuccess) { cudaGetLastError(); return MCG_ERR_CUDA; }
-    }
-    GenParams p;
-    p.vol = vol->data;
-    p.nx = vol->nx;
-    p.ny = vol->ny;
-    p.nz = vol->nz;
-    p.cell = vol->cell;
-    p.nbx = g.nbx;
-    p.nby = g.nby;
-    p.active = active;
-    p.brick_vofs = vofs;
-    p.totals = totals;
-    p.soup = out->soup;
-    p.normals = out->soup_normals;
-    p.vi2vox = out->vi2vox;
-    p.ver_voxel = out->ver_voxel;
-    p.tri_cube = out->tri_cube;
-    p.cap = out->capacity_vertices;
-    int occb = 1;
-    if (vol->voxel_type == MCG_VOXEL_SHORT2) {
-        cudaFuncSetAttribute(mc_generate_kernel<MCG_VOXEL_SHORT2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)gen_smem<MCG_VOXEL_SHORT2>());
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occb, mc_generate_kernel<MCG_VOXEL_SHORT2>, THREADS,
-                                                          gen_smem<MCG_VOXEL_SHORT2>()) != cudaSuccess || occb < 1)
-            occb = 1;
-        long long grid = (long long)sms * occb;
-        if (grid > g.nbricks) grid = g.nbricks;
-        mc_generate_kernel<MCG_VOXEL_SHORT2><<<(int)grid, THREADS, gen_smem<MCG_VOXEL_SHORT2>(), s>>>(p);
-    } else {
-        cudaFuncSetAttribute(mc_generate_kernel<MCG_VOXEL_FLOAT2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)gen_smem<MCG_VOXEL_FLOAT2>());
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occb, mc_generate_kernel<MCG_VOXEL_FLOAT2>, THREADS,
-                                                          gen_smem<MCG_VOXEL_FLOAT2>()) != cudaSuccess || occb < 1)
-            occb = 1;
-        long long grid = (long long)sms * occb;
-        if (grid > g.nbricks) grid = g.nbricks;
-        mc_generate_kernel<MCG_VOXEL_FLOAT2><<<(int)grid, THREADS, gen_smem<MCG_VOXEL_FLOAT2>(), s>>>(p);
-    }
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return MCG_ERR_CUDA;
+    // the timeout flag is cleared by the count phase; every other scratch
+    // entry read later is written first by these launches
+    e = launch_count_phase(vol, g, sc, sms, s);
+    if (e == cudaSuccess) e = launch_generate_phase(vol, g, sc, out, sms, s);
+    if (e != cudaSuccess) { cudaGetLastError(); return MCG_ERR_CUDA; }
     // counts: copy the totals out of the array into a host variable and wait
     MeshTotals t;
-    e = cudaMemcpyAsync(&t, totals, sizeof(MeshTotals), cudaMemcpyDeviceToHost, s);
+    e = cudaMemcpyAsync(&t, sc.totals, sizeof(MeshTotals), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) { cudaGetLastError(); return MCG_ERR_CUDA; }
     counts->occupied = (int64_t)t.occupied;
     counts->triangles = (int64_t)t.triangles;
     counts->vertices = (int64_t)t.vertices;
     counts->active_bricks = (int64_t)t.active_bricks;
-    counts->status = counts->vertices > out->capacity_vertices ? MCG_ERR_CAPACITY : MCG_OK;
+    counts->status = MCG_OK;
+    if (t.flags & 1u) counts->status = MCG_ERR_TIMEOUT;
+    else if (counts->vertices > out->capacity_vertices) counts->status = MCG_ERR_CAPACITY;
     counts->reserved = 0;
     return (mcg_status)counts->status;
 }

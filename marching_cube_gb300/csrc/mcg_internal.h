@@ -18,7 +18,7 @@ struct MeshTotals {
     unsigned long long triangles;
     unsigned long long vertices;
     unsigned int active_bricks;
-    unsigned int pad;
+    unsigned int flags;  // bit 0: a bounded device wait expired (set by the kernels, cleared by the host)
 };
 
 // Grows a device allocation; returns false on cudaMalloc failure.
@@ -44,7 +44,7 @@ struct mcg_context {
     // marching-cubes scratch (one entry per brick)
     uint32_t *brick_tris = nullptr;
     size_t brick_tris_cap = 0;
-    uint32_t *brick_occ = nullptr;
+    uint32_t *brick_occ = nullptr;  // per-chunk sums (triangles, active bricks, occupied cubes)
     size_t brick_occ_cap = 0;
     unsigned long long *brick_vofs = nullptr;
     size_t brick_vofs_cap = 0;

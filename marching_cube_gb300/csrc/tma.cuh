@@ -1,0 +1,88 @@
+// TMA (cp.async.bulk.tensor) and mbarrier helpers for sm_103a, inline PTX.
+//
+// Every wait is bounded by wall-clock time (%globaltimer): a wait that
+// expires returns false and the caller records MCG_ERR_TIMEOUT instead of
+// spinning forever on a shared GPU.
+#pragma once
+
+#include <cuda.h>
+#include <stdint.h>
+
+#if defined(__CUDACC__)
+namespace mcg {
+
+// 2 s: several orders of magnitude above any legitimate tile load
+constexpr unsigned long long kWaitLimitNs = 2000000000ull;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+// make the initialised barriers visible to the async (TMA) proxy
+__device__ __forceinline__ void fence_barrier_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n"
+        ".reg .pred p;\n"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        "selp.u32 %0, 1, 0, p;\n"
+        "}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Wait for phase `parity` of bar; false if limit_ns elapsed first.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity,
+                                          unsigned long long limit_ns = kWaitLimitNs) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const unsigned long long t0 = globaltimer_ns();
+    while (!mbar_try_wait(bar, parity)) {
+        if (globaltimer_ns() - t0 > limit_ns) return false;
+    }
+    return true;
+}
+
+// 3-D tiled bulk tensor load of the box at element coordinates (x, y, z)
+// into shared memory; completion is signalled on bar (complete_tx).  The
+// caller guarantees x * element size is a multiple of 16 bytes.
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, uint64_t *bar, int x, int y,
+                                            int z) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+        : "memory");
+}
+
+}  // namespace mcg
+#endif  // __CUDACC__
+
+// host side: tensor-map encoding through the driver entry point
+namespace mcg {
+// Encodes a 3-D tiled map over a dense [z][y][x] volume of elem_bytes-sized
+// voxels with the given box; false if TMA cannot describe it (alignment,
+// strides) or the driver entry point is unavailable.
+bool encode_volume_map(CUtensorMap *map, const void *data, int nx, int ny, int nz, int elem_bytes,
+                       int box_x, int box_y, int box_z);
+}  // namespace mcg

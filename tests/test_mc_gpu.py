@@ -38,8 +38,12 @@ def test_sphere_fp64_tolerance(mcg, orc):
     assert nerr <= NRM_TOL, nerr
 
 
+# (nz, ny, nx): nx*4 a multiple of 16 and every dim >= the tile box takes the
+# TMA path; the others take the plain-load path
 @pytest.mark.parametrize("shape,seed", [((2, 2, 2), 1), ((3, 5, 7), 2), ((9, 33, 65), 3),
-                                        ((17, 40, 31), 4), ((8, 8, 96), 5), ((40, 3, 2), 6)])
+                                        ((17, 40, 31), 4), ((8, 8, 96), 5), ((40, 3, 2), 6),
+                                        ((11, 13, 40), 7), ((30, 17, 100), 8), ((12, 12, 64), 9),
+                                        ((19, 41, 200), 10)])
 def test_random_volumes(mcg, orc, shape, seed):
     vol = synthetic.random_volume(shape, seed=seed)
     cell = 0.0037
@@ -90,10 +94,11 @@ def test_surface_through_max_faces(mcg, orc):
     assert_same_mesh(g, o)
 
 
-def test_float2_volume(mcg, orc):
+@pytest.mark.parametrize("shape", [(13, 17, 45), (14, 20, 46)])
+def test_float2_volume(mcg, orc, shape):
     rng = np.random.default_rng(7)
-    vol = np.stack([rng.standard_normal((13, 17, 45)).astype(np.float32),
-                    (rng.random((13, 17, 45)) > 0.03).astype(np.float32)], axis=-1)
+    vol = np.stack([rng.standard_normal(shape).astype(np.float32),
+                    (rng.random(shape) > 0.03).astype(np.float32)], axis=-1)
     g = gpu_extract(mcg, vol, 0.5)
     o = orc.mc_extract(vol, 0.5)
     assert_same_mesh(g, o)
