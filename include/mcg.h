@@ -180,6 +180,10 @@ mcg_status mcg_rle_encode(mcg_context *ctx, const void *vol, int32_t nx, int32_t
                           uint8_t *image, int64_t capacity, int64_t *size, mcg_stream_t stream);
 /* Parse the header of a host file image: dims[3] and params {min_t,max_t,grid_s}. */
 mcg_status mcg_rle_header(const uint8_t *image, int64_t size, int32_t dims[3], float params[3]);
+/* Same codec on host memory (vol: host short2 [z][y][x]); no CUDA needed. */
+mcg_status mcg_rle_encode_host(const void *vol, int32_t nx, int32_t ny, int32_t nz, float min_t, float max_t,
+                               float grid_s, int32_t lossless, uint8_t *image, int64_t capacity, int64_t *size);
+mcg_status mcg_rle_decode_host(const uint8_t *image, int64_t size, void *vol, int64_t capacity_voxels);
 /* Decode a host file image into a device short2 volume of capacity voxels.  Synchronous. */
 mcg_status mcg_rle_decode(mcg_context *ctx, const uint8_t *image, int64_t size, void *vol,
                           int64_t capacity_voxels, mcg_stream_t stream);

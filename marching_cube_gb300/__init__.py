@@ -429,6 +429,34 @@ def rle_decode(image: bytes, device=None, ctx=None, stream=None) -> Voxel:
     return Voxel(data, min_t, max_t, grid_s)
 
 
+def rle_encode_host(vol, min_t, max_t, grid_s, lossless=False) -> bytes:
+    """Encode a host (numpy) short2 volume (nz, ny, nx, 2) int16; no GPU needed."""
+    import numpy as np
+    vol = np.ascontiguousarray(vol, dtype=np.int16)
+    if vol.ndim != 4 or vol.shape[3] != 2:
+        raise ValueError("volume must be (nz, ny, nx, 2)")
+    nz, ny, nx, _ = vol.shape
+    cap = _lib.mcg_rle_bound(nx, ny, nz)
+    buf = (ctypes.c_uint8 * cap)()
+    size = ctypes.c_int64(0)
+    st = _lib.mcg_rle_encode_host(vol.ctypes.data_as(ctypes.c_void_p), nx, ny, nz, float(min_t), float(max_t),
+                                  float(grid_s), 1 if lossless else 0, buf, cap, ctypes.byref(size))
+    if st != MCG_OK:
+        raise MCGError(st, "mcg_rle_encode_host")
+    return ctypes.string_at(buf, size.value)
+
+
+def rle_decode_host(image: bytes):
+    """Decode a file image into a host numpy volume; returns (vol, (min_t, max_t, grid_s))."""
+    import numpy as np
+    (nx, ny, nz), params = rle_header(image)
+    vol = np.empty((nz, ny, nx, 2), np.int16)
+    st = _lib.mcg_rle_decode_host(image, len(image), vol.ctypes.data_as(ctypes.c_void_p), nx * ny * nz)
+    if st != MCG_OK:
+        raise MCGError(st, "mcg_rle_decode_host")
+    return vol, params
+
+
 def run_length_encode(v: Voxel, file_name, lossless=False):
     """cu_voxel_run_length_encode (kf.cu:1451-1478), whole-volume form."""
     img = rle_encode(v, lossless)

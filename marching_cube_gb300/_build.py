@@ -1,6 +1,6 @@
 """Builds libmcg.so (CUDA kernels + C ABI) in-tree for sm_103a.
 
-    python -m marching_cube_gb300._build
+    python marching_cube_gb300/_build.py
 
 Every translation unit is compiled by its own nvcc process in parallel, then
 linked into marching_cube_gb300/libmcg.so.  The CUDA runtime is linked

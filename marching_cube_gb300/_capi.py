@@ -66,6 +66,9 @@ SIGNATURES = {
     "mcg_rle_bound": (c_int64, [c_int32, c_int32, c_int32]),
     "mcg_rle_encode": (c_int, [c_void_p, c_void_p, c_int32, c_int32, c_int32, c_float, c_float, c_float,
                                c_int32, c_void_p, c_int64, ctypes.POINTER(c_int64), c_void_p]),
+    "mcg_rle_encode_host": (c_int, [c_void_p, c_int32, c_int32, c_int32, c_float, c_float, c_float, c_int32,
+                                    c_void_p, c_int64, ctypes.POINTER(c_int64)]),
+    "mcg_rle_decode_host": (c_int, [c_void_p, c_int64, c_void_p, c_int64]),
     "mcg_rle_header": (c_int, [c_void_p, c_int64, ctypes.POINTER(c_int32), ctypes.POINTER(c_float)]),
     "mcg_rle_decode": (c_int, [c_void_p, c_void_p, c_int64, c_void_p, c_int64, c_void_p]),
 }
@@ -74,7 +77,7 @@ SIGNATURES = {
 def load(path=LIB_PATH):
     if not os.path.exists(path):
         raise ImportError(
-            "libmcg.so is not built (%s); run `python -m marching_cube_gb300._build` "
+            "libmcg.so is not built (%s); run `python marching_cube_gb300/_build.py` "
             "(or __graft_entry__.build())" % path)
     lib = ctypes.CDLL(path)
     for name, (res, args) in SIGNATURES.items():

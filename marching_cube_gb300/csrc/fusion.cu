@@ -21,6 +21,7 @@
 #include <stdint.h>
 
 #include "mcg_internal.h"
+#include "unpack.h"
 
 namespace mcg {
 namespace {
@@ -251,7 +252,7 @@ __global__ void __launch_bounds__(256) integrate_short2_kernel(IntegParams p, sh
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
         if (!(upd & (1u << i))) continue;
-        const float sdf1 = (float)cur[i].x / (float)kMaxTsdf;
+        const float sdf1 = mcg_unpack_tsdf(cur[i].x);  // (float)tsdf / 32766, exact
         const float w1 = unpack_weight((unsigned short)cur[i].y);
         float s2, w2;
         fuse(p, sdf[i], wt[i], sdf1, w1, s2, w2);

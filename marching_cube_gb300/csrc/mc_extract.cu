@@ -47,6 +47,7 @@
 #include "mc_tables.h"
 #include "mcg_internal.h"
 #include "tma.cuh"
+#include "unpack.h"
 
 namespace mcg {
 namespace {
@@ -95,8 +96,8 @@ struct Vox<MCG_VOXEL_SHORT2> {
     static __device__ __forceinline__ T fill() { return make_short2(0, 0); }
     static __device__ __forceinline__ bool neg(T v) { return v.x < 0; }
     static __device__ __forceinline__ bool w0(T v) { return v.y == 0; }
-    // d_unpack_tsdf (cu_kinect_fusion_v1.h:253-256)
-    static __device__ __forceinline__ float f(T v) { return (float)v.x / (float)kMaxTsdf; }
+    // d_unpack_tsdf (cu_kinect_fusion_v1.h:253-256), division-free and exact
+    static __device__ __forceinline__ float f(T v) { return mcg_unpack_tsdf(v.x); }
     static __device__ __forceinline__ bool sentinel(T v) { return v.x == kMaxTsdf || v.x == -kMaxTsdf; }
     static __device__ __forceinline__ short tsdf(T v) { return v.x; }
     static __device__ __forceinline__ short wt(T v) { return v.y; }

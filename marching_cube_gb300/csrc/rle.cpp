@@ -150,6 +150,70 @@ mcg_status mcg_rle_header(const uint8_t *image, int64_t size, int32_t dims[3], f
     return MCG_OK;
 }
 
+mcg_status mcg_rle_encode_host(const void *vol, int32_t nx, int32_t ny, int32_t nz, float min_t, float max_t,
+                               float grid_s, int32_t lossless, uint8_t *image, int64_t capacity, int64_t *size) {
+    if (!vol || !image || !size || nx <= 0 || ny <= 0 || nz <= 0) return MCG_ERR_INVALID_ARG;
+    *size = 0;
+    if (capacity < 40) return MCG_ERR_CAPACITY;
+    memcpy(image, lossless ? kTagLossless : kTagRef, 16);
+    const int32_t dims[3] = {nx, ny, nz};
+    memcpy(image + 16, dims, 12);
+    memcpy(image + 28, &min_t, 4);
+    memcpy(image + 32, &max_t, 4);
+    memcpy(image + 36, &grid_s, 4);
+    const int64_t xy = (int64_t)nx * ny;
+    const HVox *v = static_cast<const HVox *>(vol);
+    // encode slices in parallel into private buffers, then concatenate in order
+    const int batch = std::max(1, std::min(nz, 4 * host_threads()));
+    std::vector<std::vector<uint8_t>> enc(batch);
+    std::vector<int64_t> sz(batch);
+    int64_t o = 40;
+    for (int z0 = 0; z0 < nz; z0 += batch) {
+        const int ns = std::min(batch, nz - z0);
+        parallel_for(ns, [&](int i) {
+            enc[i].resize((size_t)(6 * xy + 16));
+            sz[i] = encode_slice(v + (int64_t)(z0 + i) * xy, xy, lossless != 0, enc[i].data());
+        });
+        for (int i = 0; i < ns; ++i) {
+            if (o + 4 + sz[i] > capacity) return MCG_ERR_CAPACITY;
+            const uint32_t s32 = (uint32_t)sz[i];
+            memcpy(image + o, &s32, 4);
+            memcpy(image + o + 4, enc[i].data(), (size_t)sz[i]);
+            o += 4 + sz[i];
+        }
+    }
+    *size = o;
+    return MCG_OK;
+}
+
+mcg_status mcg_rle_decode_host(const uint8_t *image, int64_t size, void *vol, int64_t capacity_voxels) {
+    if (!image || !vol) return MCG_ERR_INVALID_ARG;
+    int32_t dims[3];
+    float params[3];
+    mcg_status st = mcg_rle_header(image, size, dims, params);
+    if (st != MCG_OK) return st;
+    const int64_t xy = (int64_t)dims[0] * dims[1];
+    if (xy * dims[2] > capacity_voxels) return MCG_ERR_CAPACITY;
+    std::vector<int64_t> off(dims[2]), len(dims[2]);
+    int64_t p = 40;
+    for (int z = 0; z < dims[2]; ++z) {
+        if (p + 4 > size) return MCG_ERR_FORMAT;
+        uint32_t s32;
+        memcpy(&s32, image + p, 4);
+        p += 4;
+        if (p + (int64_t)s32 > size) return MCG_ERR_FORMAT;
+        off[z] = p;
+        len[z] = s32;
+        p += s32;
+    }
+    HVox *v = static_cast<HVox *>(vol);
+    std::atomic<bool> bad(false);
+    parallel_for(dims[2], [&](int z) {
+        if (!decode_slice(image + off[z], len[z], v + (int64_t)z * xy, xy)) bad = true;
+    });
+    return bad ? MCG_ERR_FORMAT : MCG_OK;
+}
+
 mcg_status mcg_rle_encode(mcg_context *ctx, const void *vol, int32_t nx, int32_t ny, int32_t nz,
                           float min_t, float max_t, float grid_s, int32_t lossless, uint8_t *image,
                           int64_t capacity, int64_t *size, mcg_stream_t stream) {
