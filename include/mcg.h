@@ -117,6 +117,16 @@ mcg_status mcg_mc_generate(mcg_context *ctx, const mcg_volume *vol, const mcg_me
 /* classify + generate in one call, no host synchronisation */
 mcg_status mcg_mc_extract(mcg_context *ctx, const mcg_volume *vol, const mcg_mesh_out *out,
                           mcg_stream_t stream);
+/* Batched extraction: nvol volumes of any sizes (same voxel type) in one
+ * launch per pass (replaces a loop of MarchingCubes::run calls).  Outputs
+ * of volume v go to outs[v], in the same order and bit-identical to a
+ * single-volume extraction of that volume.  counts: nvol entries. */
+mcg_status mcg_mc_classify_batched(mcg_context *ctx, const mcg_volume *vols, int32_t nvol, mcg_stream_t stream);
+mcg_status mcg_mc_counts_batched(mcg_context *ctx, mcg_mesh_counts *counts, int32_t nvol);
+mcg_status mcg_mc_generate_batched(mcg_context *ctx, const mcg_volume *vols, const mcg_mesh_out *outs,
+                                   int32_t nvol, mcg_stream_t stream);
+mcg_status mcg_mc_extract_batched(mcg_context *ctx, const mcg_volume *vols, const mcg_mesh_out *outs,
+                                  int32_t nvol, mcg_stream_t stream);
 /* No counterpart in the reference.  The same extraction as mcg_mc_extract
  * for callers that cannot allocate device memory -- a process whose device
  * memory is owned by another allocator (a caching allocator or an arena

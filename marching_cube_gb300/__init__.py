@@ -288,6 +288,64 @@ def extract_into(volume, cell, outputs: dict, capacity, ctx=None, stream=None):
     return ctx
 
 
+def extract_batched(volumes, cells, *, soup=True, normals=True, vi2vox=False, ver_voxel=False, tri_cube=False,
+                    ctx=None, stream=None):
+    """Marching cubes over many volumes (same voxel type, any sizes) with one
+    launch per pass; returns one Mesh per volume, identical to extract() of
+    that volume."""
+    if not volumes:
+        return []
+    if not isinstance(cells, (list, tuple)):
+        cells = [cells] * len(volumes)
+    ctx = ctx or default_context(volumes[0].device.index)
+    n = len(volumes)
+    cvs = (_capi.Volume * n)(*[_cvol(v, c) for v, c in zip(volumes, cells)])
+    s = _stream(stream)
+    ctx.check(_lib.mcg_mc_classify_batched(ctx.handle, cvs, n, s), "mcg_mc_classify_batched")
+    cnt = (_capi.MeshCounts * n)()
+    st = _lib.mcg_mc_counts_batched(ctx.handle, cnt, n)
+    if st not in (MCG_OK, MCG_ERR_CAPACITY):
+        ctx.check(st, "mcg_mc_counts_batched")
+    allocs, outs = [], (_capi.MeshOut * n)()
+    for i, v in enumerate(volumes):
+        nz, ny, nx, _ = v.shape
+        o = _alloc_outputs(cnt[i].vertices, nx * ny * nz, v.device, soup, normals, vi2vox, ver_voxel, tri_cube)
+        allocs.append(o)
+        outs[i] = _mesh_out(o, cnt[i].vertices)
+    ctx.check(_lib.mcg_mc_generate_batched(ctx.handle, cvs, outs, n, s), "mcg_mc_generate_batched")
+    meshes = []
+    for i, o in enumerate(allocs):
+        c = {"occupied": cnt[i].occupied, "triangles": cnt[i].triangles, "vertices": cnt[i].vertices,
+             "active_bricks": 0, "status": 0}
+        meshes.append(Mesh(o["soup"], o["normals"], o["vi2vox"], o["ver_voxel"], o["tri_cube"], c))
+    return meshes
+
+
+def extract_batched_into(volumes, cells, outputs, capacities, ctx=None, stream=None):
+    """Asynchronous batched extraction into preallocated buffers (no host
+    synchronisation); outputs[i] is a dict like extract_into's."""
+    if not isinstance(cells, (list, tuple)):
+        cells = [cells] * len(volumes)
+    ctx = ctx or default_context(volumes[0].device.index)
+    n = len(volumes)
+    cvs = (_capi.Volume * n)(*[_cvol(v, c) for v, c in zip(volumes, cells)])
+    outs = (_capi.MeshOut * n)()
+    for i in range(n):
+        o = {k: outputs[i].get(k) for k in ("soup", "normals", "vi2vox", "ver_voxel", "tri_cube")}
+        outs[i] = _mesh_out(o, capacities[i])
+    ctx.check(_lib.mcg_mc_extract_batched(ctx.handle, cvs, outs, n, _stream(stream)), "mcg_mc_extract_batched")
+    return ctx
+
+
+def counts_batched(ctx, n):
+    cnt = (_capi.MeshCounts * n)()
+    st = _lib.mcg_mc_counts_batched(ctx.handle, cnt, n)
+    if st not in (MCG_OK, MCG_ERR_CAPACITY):
+        ctx.check(st, "mcg_mc_counts_batched")
+    return [{"occupied": c.occupied, "triangles": c.triangles, "vertices": c.vertices, "status": c.status}
+            for c in cnt]
+
+
 class MarchingCubes:
     """cu_marching_cubes_v1.h:28-65.  run() returns the triangle soup; if the
     caller's buffer is empty it is sized from the count phase."""

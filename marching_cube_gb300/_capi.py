@@ -52,6 +52,12 @@ SIGNATURES = {
     "mcg_mc_counts": (c_int, [c_void_p, ctypes.POINTER(MeshCounts)]),
     "mcg_mc_generate": (c_int, [c_void_p, ctypes.POINTER(Volume), ctypes.POINTER(MeshOut), c_void_p]),
     "mcg_mc_extract": (c_int, [c_void_p, ctypes.POINTER(Volume), ctypes.POINTER(MeshOut), c_void_p]),
+    "mcg_mc_classify_batched": (c_int, [c_void_p, ctypes.POINTER(Volume), c_int32, c_void_p]),
+    "mcg_mc_counts_batched": (c_int, [c_void_p, ctypes.POINTER(MeshCounts), c_int32]),
+    "mcg_mc_generate_batched": (c_int, [c_void_p, ctypes.POINTER(Volume), ctypes.POINTER(MeshOut), c_int32,
+                                        c_void_p]),
+    "mcg_mc_extract_batched": (c_int, [c_void_p, ctypes.POINTER(Volume), ctypes.POINTER(MeshOut), c_int32,
+                                       c_void_p]),
     "mcg_mc_extract_noalloc": (c_int, [ctypes.POINTER(Volume), ctypes.POINTER(MeshOut),
                                        ctypes.POINTER(MeshCounts), c_void_p]),
     "mcg_mc_normals": (c_int, [c_void_p, ctypes.POINTER(Volume), c_void_p, c_int64, c_void_p, c_void_p]),

@@ -46,6 +46,7 @@ mcg_status mcg_create(mcg_context **out, int device) {
     if (e == cudaSuccess) e = cudaMemset(ctx->d_totals, 0, sizeof(mcg::MeshTotals));
     if (e == cudaSuccess) e = cudaMallocHost((void **)&ctx->h_totals, sizeof(mcg::MeshTotals));
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->counts_ready, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->btab_copied, cudaEventDisableTiming);
     if (e != cudaSuccess) {
         cudaGetLastError();
         mcg_destroy(ctx);
@@ -67,6 +68,13 @@ mcg_status mcg_destroy(mcg_context *ctx) {
     cudaFree(ctx->d_totals);
     if (ctx->h_totals) cudaFreeHost(ctx->h_totals);
     if (ctx->counts_ready) cudaEventDestroy(ctx->counts_ready);
+    if (ctx->btab_copied) cudaEventSynchronize(ctx->btab_copied);
+    cudaFree(ctx->d_btab);
+    if (ctx->h_btab) cudaFreeHost(ctx->h_btab);
+    if (ctx->btab_copied) cudaEventDestroy(ctx->btab_copied);
+    cudaFree(ctx->d_vol_sums);
+    if (ctx->h_vol_sums) cudaFreeHost(ctx->h_vol_sums);
+    delete[] ctx->batch_caps;
     cudaFree(ctx->depth_scaled);
     cudaFree(ctx->ray_x);
     if (ctx->h_ray_x) cudaFreeHost(ctx->h_ray_x);

@@ -138,7 +138,7 @@ __device__ __forceinline__ BrickPos brick_pos(long long b, int nbx, int nby) {
 template <int VT, int DX, int DY, int DZ>
 __device__ __forceinline__ void fill_tile(typename Vox<VT>::T *tile, const typename Vox<VT>::T *__restrict__ vol,
                                           int nx, int ny, int nz, int ox, int oy, int oz) {
-    for (int i = threadIdx.x; i < DX * DY * DZ; i += THREADS) {
+    for (int i = threadIdx.x; i < DX * DY * DZ; i += blockDim.x) {
         const int lx = i % DX, t = i / DX, ly = t % DY, lz = t / DY;
         const int gx = ox + lx, gy = oy + ly, gz = oz + lz;
         typename Vox<VT>::T v = Vox<VT>::fill();
@@ -247,6 +247,37 @@ struct ClsSmem {
     int abort;
 };
 
+// Pass-1 work on one brick tile: row masks, cube rows, per-warp sums into
+// S.red (read after the caller's next __syncthreads).  Called by every
+// thread of the CTA.
+template <int VT, class Smem>
+__device__ __forceinline__ void classify_brick(Smem &S, const typename Vox<VT>::T *tile, int nx, int ny, int nz,
+                                               BrickPos bp) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid < ROWS) RowMask<VT>::build(tile + tid * CTX, S.neg[tid], S.dead[tid]);
+        __syncthreads();
+        if (tid < CUBE_ROWS) {
+            const int cy = tid & (BY - 1), cz = tid / BY;
+            unsigned int tri = 0, occ = 0;
+            if (bp.y0 + cy < ny - 1 && bp.z0 + cz < nz - 1) {
+                const CubeRow cr = cube_row(S.neg, S.dead, cy, cz, valid_mask(bp.x0, nx));
+                occ = __popc(cr.occ);
+                unsigned int m = cr.occ;
+                while (m) {
+                    const int x = __ffs(m) - 1;
+                    m &= m - 1;
+                    tri += S.ntri[cube_index(cr, x)];
+                }
+            }
+            tri = __reduce_add_sync(0xffffffffu, tri);
+            occ = __reduce_add_sync(0xffffffffu, occ);
+            if (lane == 0) {
+                S.red[warp][0] = tri;
+                S.red[warp][1] = occ;
+            }
+        }
+}
+
 template <int VT, bool TMA, int CSTAGES>
 __global__ void __launch_bounds__(CTHREADS)
     mc_classify_kernel(const __grid_constant__ CUtensorMap map, const typename Vox<VT>::T *__restrict__ vol,
@@ -257,7 +288,7 @@ __global__ void __launch_bounds__(CTHREADS)
     using T = typename V::T;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     ClsSmem<VT, CSTAGES> &S = *reinterpret_cast<ClsSmem<VT, CSTAGES> *>(smem_raw);
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int tid = threadIdx.x;
     const long long stride = gridDim.x;
     for (int c = tid; c < 256; c += CTHREADS) S.ntri[c] = (c == 0 || c == 255) ? 0 : c_nverts[c] / 3;
     if (tid == 0) {
@@ -295,28 +326,7 @@ __global__ void __launch_bounds__(CTHREADS)
         }
         __syncthreads();
         if (S.abort) break;
-        if (tid < ROWS) RowMask<VT>::build(tile + tid * CTX, S.neg[tid], S.dead[tid]);
-        __syncthreads();
-        if (tid < CUBE_ROWS) {
-            const int cy = tid & (BY - 1), cz = tid / BY;
-            unsigned int tri = 0, occ = 0;
-            if (bp.y0 + cy < ny - 1 && bp.z0 + cz < nz - 1) {
-                const CubeRow cr = cube_row(S.neg, S.dead, cy, cz, valid_mask(bp.x0, nx));
-                occ = __popc(cr.occ);
-                unsigned int m = cr.occ;
-                while (m) {
-                    const int x = __ffs(m) - 1;
-                    m &= m - 1;
-                    tri += S.ntri[cube_index(cr, x)];
-                }
-            }
-            tri = __reduce_add_sync(0xffffffffu, tri);
-            occ = __reduce_add_sync(0xffffffffu, occ);
-            if (lane == 0) {
-                S.red[warp][0] = tri;
-                S.red[warp][1] = occ;
-            }
-        }
+        classify_brick<VT>(S, tile, nx, ny, nz, bp);
         __syncthreads();  // tile s consumed, red[] complete
         if (tid == 0) {
             const unsigned int t = S.red[0][0] + S.red[1][0], o = S.red[0][1] + S.red[1][1];
@@ -527,63 +537,28 @@ struct GenSmem {
 
 __device__ __forceinline__ int tidx(int lx, int ly, int lz) { return (lz * TY + ly) * TX + lx; }
 
-template <int VT, bool TMA>
-__global__ void __launch_bounds__(THREADS, 4) mc_generate_kernel(const __grid_constant__ CUtensorMap map, GenParams p) {
+// Output arrays of one volume (device pointers, any may be null).
+struct GenOut {
+    mcg_vertex_voxel *soup;
+    float *normals;
+    int32_t *vi2vox;
+    int16_t *ver_voxel;
+    int64_t *tri_cube;
+    long long cap;
+};
+
+// All per-brick work of pass 2 once the brick's tile is in shared memory:
+// occupied-cube list with vertex offsets, then one soup vertex per thread.
+// Called by every thread of the CTA (contains __syncthreads).
+template <int VT>
+__device__ __forceinline__ void generate_brick(GenSmem<VT> &S, const typename Vox<VT>::T *tile,
+                                               const typename Vox<VT>::T *__restrict__ vol, int nx, int ny,
+                                               int nz, float cell, int x0, int y0, int z0,
+                                               unsigned long long vbase, const GenOut &o) {
     using V = Vox<VT>;
     using T = typename V::T;
-    extern __shared__ __align__(128) unsigned char smem_raw[];
-    GenSmem<VT> &S = *reinterpret_cast<GenSmem<VT> *>(smem_raw);
-    const T *__restrict__ vol = static_cast<const T *>(p.vol);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int nx = p.nx, ny = p.ny, nz = p.nz;
     const long long N = (long long)nx * ny * nz;
-    const float cell = p.cell;
-
-    for (int i = tid; i < 256 * 16; i += THREADS) (&S.tri[0][0])[i] = (&c_tri[0][0])[i];
-    S.nv[tid] = (tid == 0 || tid == 255) ? 0 : c_nverts[tid];
-    if (tid == 0) {
-        S.abort = 0;
-        if (TMA) {
-            for (int s = 0; s < GSTAGES; ++s) mbar_init(&S.bars[s], 1);
-            fence_barrier_init();
-        }
-    }
-    __syncthreads();
-    const unsigned int nactive = p.totals->active_bricks;
-    if (TMA && tid == 0) {
-        for (int s = 0; s < GSTAGES; ++s) {
-            const unsigned int w = blockIdx.x + s * gridDim.x;
-            if (w >= nactive) break;
-            const long long b = p.active[w];
-            S.sbrick[s] = b;
-            S.svbase[s] = p.brick_vofs[b];
-            const BrickPos bp = brick_pos(b, p.nbx, p.nby);
-            mbar_arrive_expect_tx(&S.bars[s], GTILE * V::bytes);
-            tma_load_3d(S.tiles[s], &map, &S.bars[s], bp.x0 - TXO, bp.y0 - TYO, bp.z0 - TZO);
-        }
-    }
-    int it = 0;
-    for (unsigned int w = blockIdx.x; w < nactive; w += gridDim.x, ++it) {
-        const int s = TMA ? it % GSTAGES : 0;
-        const T *tile = reinterpret_cast<const T *>(S.tiles[s]);
-        long long b;
-        unsigned long long vbase;
-        if (TMA) {
-            if (tid == 0 && !mbar_wait(&S.bars[s], (uint32_t)((it / GSTAGES) & 1))) S.abort = 1;
-            __syncthreads();
-            if (S.abort) break;
-            b = S.sbrick[s];
-            vbase = S.svbase[s];
-        } else {
-            b = p.active[w];
-            vbase = p.brick_vofs[b];
-            const BrickPos fp = brick_pos(b, p.nbx, p.nby);
-            fill_tile<VT, TX, TY, TZ>(reinterpret_cast<T *>(S.tiles[s]), vol, nx, ny, nz, fp.x0 - TXO,
-                                      fp.y0 - TYO, fp.z0 - TZO);
-            __syncthreads();
-        }
-        const BrickPos bp = brick_pos(b, p.nbx, p.nby);
-        const int x0 = bp.x0, y0 = bp.y0, z0 = bp.z0;
 
         // occupied cubes of the brick, from row masks (voxel rows y0..y0+8, z0..z0+8)
         if (tid < ROWS) {
@@ -713,9 +688,9 @@ __global__ void __launch_bounds__(THREADS, 4) mc_generate_kernel(const __grid_co
                     vt = V::tsdf(vv);
                     vw = V::wt(vv);
                 }
-                if (p.ver_voxel && li >= 0 && li < N && vbase + v < (unsigned long long)p.cap)
-                    p.ver_voxel[li] = vt;
-                if (p.normals) {
+                if (o.ver_voxel && li >= 0 && li < N && vbase + v < (unsigned long long)o.cap)
+                    o.ver_voxel[li] = vt;
+                if (o.normals) {
                     const float fx = pf[0], fy = pf[1], fz = pf[2];
                     const int ix = (int)fx, iy = (int)fy, iz = (int)fz;
                     const int lx = ix - org[0], ly = iy - org[1], lz = iz - org[2];
@@ -740,10 +715,10 @@ __global__ void __launch_bounds__(THREADS, 4) mc_generate_kernel(const __grid_co
             }
             // ---- coalesced stores through the warp stage ----
             const unsigned long long g0 = vbase + v0;  // first record of this warp
-            const long long room = p.cap - (long long)g0;
+            const long long room = o.cap - (long long)g0;
             const int nrec = (int)min((long long)min(32u, T_brick - v0), room > 0 ? room : 0ll);
             unsigned int *st = S.stage[warp];
-            if (p.soup) {
+            if (o.soup) {
                 st[lane * 7 + 0] = __float_as_uint(P[0]);
                 st[lane * 7 + 1] = __float_as_uint(P[1]);
                 st[lane * 7 + 2] = __float_as_uint(P[2]);
@@ -752,7 +727,7 @@ __global__ void __launch_bounds__(THREADS, 4) mc_generate_kernel(const __grid_co
                 st[lane * 7 + 5] = (unsigned int)vox[2];
                 st[lane * 7 + 6] = (unsigned int)(unsigned short)vt | ((unsigned int)(unsigned short)vw << 16);
                 __syncwarp();
-                unsigned int *dst = reinterpret_cast<unsigned int *>(p.soup) + g0 * 7;
+                unsigned int *dst = reinterpret_cast<unsigned int *>(o.soup) + g0 * 7;
 #pragma unroll
                 for (int q = 0; q < 7; ++q) {
                     const int word = q * 32 + lane;
@@ -760,12 +735,12 @@ __global__ void __launch_bounds__(THREADS, 4) mc_generate_kernel(const __grid_co
                 }
                 __syncwarp();
             }
-            if (p.normals) {
+            if (o.normals) {
                 st[lane * 3 + 0] = __float_as_uint(nrm.x);
                 st[lane * 3 + 1] = __float_as_uint(nrm.y);
                 st[lane * 3 + 2] = __float_as_uint(nrm.z);
                 __syncwarp();
-                unsigned int *dst = reinterpret_cast<unsigned int *>(p.normals) + g0 * 3;
+                unsigned int *dst = reinterpret_cast<unsigned int *>(o.normals) + g0 * 3;
 #pragma unroll
                 for (int q = 0; q < 3; ++q) {
                     const int word = q * 32 + lane;
@@ -773,12 +748,12 @@ __global__ void __launch_bounds__(THREADS, 4) mc_generate_kernel(const __grid_co
                 }
                 __syncwarp();
             }
-            if (p.vi2vox) {
+            if (o.vi2vox) {
                 st[lane * 3 + 0] = (unsigned int)vox[0];
                 st[lane * 3 + 1] = (unsigned int)vox[1];
                 st[lane * 3 + 2] = (unsigned int)vox[2];
                 __syncwarp();
-                unsigned int *dst = reinterpret_cast<unsigned int *>(p.vi2vox) + g0 * 3;
+                unsigned int *dst = reinterpret_cast<unsigned int *>(o.vi2vox) + g0 * 3;
 #pragma unroll
                 for (int q = 0; q < 3; ++q) {
                     const int word = q * 32 + lane;
@@ -787,9 +762,74 @@ __global__ void __launch_bounds__(THREADS, 4) mc_generate_kernel(const __grid_co
                 __syncwarp();
             }
             // a triangle's cube id is written only when the whole triangle fits
-            if (p.tri_cube && valid && kslot == 0 && (long long)(g0 + lane) + 2 < p.cap)
-                p.tri_cube[(g0 + lane) / 3] = cube_lin;
+            if (o.tri_cube && valid && kslot == 0 && (long long)(g0 + lane) + 2 < o.cap)
+                o.tri_cube[(g0 + lane) / 3] = cube_lin;
         }
+}
+
+template <int VT, bool TMA>
+__global__ void __launch_bounds__(THREADS, 4) mc_generate_kernel(const __grid_constant__ CUtensorMap map, GenParams p) {
+    using V = Vox<VT>;
+    using T = typename V::T;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    GenSmem<VT> &S = *reinterpret_cast<GenSmem<VT> *>(smem_raw);
+    const T *__restrict__ vol = static_cast<const T *>(p.vol);
+    const int tid = threadIdx.x;
+    const int nx = p.nx, ny = p.ny, nz = p.nz;
+    const float cell = p.cell;
+
+    for (int i = tid; i < 256 * 16; i += THREADS) (&S.tri[0][0])[i] = (&c_tri[0][0])[i];
+    S.nv[tid] = (tid == 0 || tid == 255) ? 0 : c_nverts[tid];
+    if (tid == 0) {
+        S.abort = 0;
+        if (TMA) {
+            for (int s = 0; s < GSTAGES; ++s) mbar_init(&S.bars[s], 1);
+            fence_barrier_init();
+        }
+    }
+    __syncthreads();
+    const unsigned int nactive = p.totals->active_bricks;
+    if (TMA && tid == 0) {
+        for (int s = 0; s < GSTAGES; ++s) {
+            const unsigned int w = blockIdx.x + s * gridDim.x;
+            if (w >= nactive) break;
+            const long long b = p.active[w];
+            S.sbrick[s] = b;
+            S.svbase[s] = p.brick_vofs[b];
+            const BrickPos bp = brick_pos(b, p.nbx, p.nby);
+            mbar_arrive_expect_tx(&S.bars[s], GTILE * V::bytes);
+            tma_load_3d(S.tiles[s], &map, &S.bars[s], bp.x0 - TXO, bp.y0 - TYO, bp.z0 - TZO);
+        }
+    }
+    int it = 0;
+    for (unsigned int w = blockIdx.x; w < nactive; w += gridDim.x, ++it) {
+        const int s = TMA ? it % GSTAGES : 0;
+        const T *tile = reinterpret_cast<const T *>(S.tiles[s]);
+        long long b;
+        unsigned long long vbase;
+        if (TMA) {
+            if (tid == 0 && !mbar_wait(&S.bars[s], (uint32_t)((it / GSTAGES) & 1))) S.abort = 1;
+            __syncthreads();
+            if (S.abort) break;
+            b = S.sbrick[s];
+            vbase = S.svbase[s];
+        } else {
+            b = p.active[w];
+            vbase = p.brick_vofs[b];
+            const BrickPos fp = brick_pos(b, p.nbx, p.nby);
+            fill_tile<VT, TX, TY, TZ>(reinterpret_cast<T *>(S.tiles[s]), vol, nx, ny, nz, fp.x0 - TXO,
+                                      fp.y0 - TYO, fp.z0 - TZO);
+            __syncthreads();
+        }
+        const BrickPos bp = brick_pos(b, p.nbx, p.nby);
+        GenOut o;
+        o.soup = p.soup;
+        o.normals = p.normals;
+        o.vi2vox = p.vi2vox;
+        o.ver_voxel = p.ver_voxel;
+        o.tri_cube = p.tri_cube;
+        o.cap = p.cap;
+        generate_brick<VT>(S, tile, vol, nx, ny, nz, cell, bp.x0, bp.y0, bp.z0, vbase, o);
         __syncthreads();  // tile s, the list and the stage are free again
         if (TMA && tid == 0) {
             const unsigned int wn = w + GSTAGES * gridDim.x;
@@ -806,6 +846,216 @@ __global__ void __launch_bounds__(THREADS, 4) mc_generate_kernel(const __grid_co
     if (S.abort && tid == 0) {
         atomicOr(&p.totals->flags, 1u);
         for (int s = 0; s < GSTAGES; ++s) mbar_wait(&S.bars[s], 0, 100000000ull);
+    }
+}
+
+
+// ---- batched extraction: many volumes, one launch per pass ------------------------
+// Bricks of all volumes form one index space: volume v owns bricks
+// [brick_base, brick_base + nbricks).  A brick's volume is found by binary
+// search over the descriptor table; tiles come by TMA through the volume's
+// own tensor map (global memory) when TMA can describe it, by plain loads
+// otherwise.  Soup offsets come from one scan over all bricks; each volume's
+// offsets start at its first brick's offset.
+struct VolDesc {
+    const void *data;
+    int nx, ny, nz;
+    float cell;
+    int nbx, nby;
+    int tma;
+    int pad;
+    long long brick_base;
+    long long nbricks;
+    mcg_vertex_voxel *soup;
+    float *normals;
+    int32_t *vi2vox;
+    int16_t *ver_voxel;
+    int64_t *tri_cube;
+    long long cap;
+};
+
+__device__ __forceinline__ int find_volume(const VolDesc *__restrict__ vols, int nvol, long long b) {
+    int lo = 0, hi = nvol - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (vols[mid].brick_base <= b) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+template <int VT>
+struct ClsSmemMulti {
+    static constexpr int STAGE_BYTES = pad128(CTILE * Vox<VT>::bytes);
+    unsigned char tiles[2][STAGE_BYTES];
+    unsigned long long neg[ROWS], dead[ROWS];
+    uint64_t bars[2];
+    unsigned int red[2][2];
+    unsigned char ntri[256];
+    int svol[2];
+    int stma[2];
+    int abort;
+};
+
+template <int VT>
+__device__ __forceinline__ void issue_cls_tile(ClsSmemMulti<VT> &S, int s, const VolDesc *__restrict__ vols, int nvol,
+                                               const CUtensorMap *maps, long long b) {
+    const int v = find_volume(vols, nvol, b);
+    S.svol[s] = v;
+    S.stma[s] = vols[v].tma;
+    if (vols[v].tma) {
+        const BrickPos bp = brick_pos(b - vols[v].brick_base, vols[v].nbx, vols[v].nby);
+        mbar_arrive_expect_tx(&S.bars[s], CTILE * Vox<VT>::bytes);
+        tma_load_3d(S.tiles[s], maps + v, &S.bars[s], bp.x0, bp.y0, bp.z0);
+    }
+}
+
+template <int VT>
+__global__ void __launch_bounds__(CTHREADS)
+    mc_classify_multi_kernel(const VolDesc *__restrict__ vols, const CUtensorMap *maps, int nvol, long long nbricks,
+                             uint32_t *__restrict__ brick_tris, uint32_t *__restrict__ chunk,
+                             unsigned long long *__restrict__ vol_sums, unsigned int *__restrict__ flags) {
+    using V = Vox<VT>;
+    using T = typename V::T;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    ClsSmemMulti<VT> &S = *reinterpret_cast<ClsSmemMulti<VT> *>(smem_raw);
+    const int tid = threadIdx.x;
+    const long long stride = gridDim.x;
+    uint32_t phase[2] = {0, 0};
+    for (int c = tid; c < 256; c += CTHREADS) S.ntri[c] = (c == 0 || c == 255) ? 0 : c_nverts[c] / 3;
+    if (tid == 0) {
+        S.abort = 0;
+        for (int s = 0; s < 2; ++s) mbar_init(&S.bars[s], 1);
+        fence_barrier_init();
+        for (int s = 0; s < 2; ++s) {
+            const long long b = blockIdx.x + s * stride;
+            if (b < nbricks) issue_cls_tile<VT>(S, s, vols, nvol, maps, b);
+        }
+    }
+    __syncthreads();
+    for (int i = 0;; ++i) {
+        const long long b = blockIdx.x + (long long)i * stride;
+        if (b >= nbricks) break;
+        const int s = i & 1;
+        T *tile = reinterpret_cast<T *>(S.tiles[s]);
+        const int v = S.svol[s];
+        const VolDesc &d = vols[v];
+        const BrickPos bp = brick_pos(b - d.brick_base, d.nbx, d.nby);
+        if (S.stma[s]) {
+            if (tid == 0) {
+                if (!mbar_wait(&S.bars[s], phase[s])) S.abort = 1;
+            }
+            phase[s] ^= 1u;
+        } else {
+            fill_tile<VT, CTX, CTY, CTZ>(tile, static_cast<const T *>(d.data), d.nx, d.ny, d.nz, bp.x0, bp.y0, bp.z0);
+        }
+        __syncthreads();
+        if (S.abort) break;
+        classify_brick<VT>(S, tile, d.nx, d.ny, d.nz, bp);
+        __syncthreads();  // tile s consumed, red[] complete
+        if (tid == 0) {
+            const unsigned int t = S.red[0][0] + S.red[1][0], o = S.red[0][1] + S.red[1][1];
+            brick_tris[b] = t;
+            if (t) {
+                atomicAdd(&chunk[(b / CHUNK) * 3 + 0], t);
+                atomicAdd(&chunk[(b / CHUNK) * 3 + 1], 1u);
+                atomicAdd(&chunk[(b / CHUNK) * 3 + 2], o);
+                atomicAdd(&vol_sums[2 * v + 0], (unsigned long long)t);
+                atomicAdd(&vol_sums[2 * v + 1], (unsigned long long)o);
+            }
+            const long long nb = b + 2 * stride;
+            if (nb < nbricks) issue_cls_tile<VT>(S, s, vols, nvol, maps, nb);
+        }
+    }
+    if (S.abort && tid == 0) {
+        atomicOr(flags, 1u);
+        for (int s = 0; s < 2; ++s) mbar_wait(&S.bars[s], phase[s], 100000000ull);
+    }
+}
+
+template <int VT>
+struct GenSmemMulti : GenSmem<VT> {
+    int svol[2];
+    int stma[2];
+};
+
+template <int VT>
+__device__ __forceinline__ void issue_gen_tile(GenSmemMulti<VT> &S, int s, const VolDesc *__restrict__ vols, int nvol,
+                                               const CUtensorMap *maps, const unsigned long long *__restrict__ vofs,
+                                               long long b) {
+    const int v = find_volume(vols, nvol, b);
+    S.svol[s] = v;
+    S.stma[s] = vols[v].tma;
+    S.sbrick[s] = b;
+    S.svbase[s] = vofs[b] - vofs[vols[v].brick_base];
+    if (vols[v].tma) {
+        const BrickPos bp = brick_pos(b - vols[v].brick_base, vols[v].nbx, vols[v].nby);
+        mbar_arrive_expect_tx(&S.bars[s], GTILE * Vox<VT>::bytes);
+        tma_load_3d(S.tiles[s], maps + v, &S.bars[s], bp.x0 - TXO, bp.y0 - TYO, bp.z0 - TZO);
+    }
+}
+
+template <int VT>
+__global__ void __launch_bounds__(THREADS, 4)
+    mc_generate_multi_kernel(const VolDesc *__restrict__ vols, const CUtensorMap *maps, int nvol,
+                             const uint32_t *__restrict__ active, const unsigned long long *__restrict__ vofs,
+                             MeshTotals *totals) {
+    using V = Vox<VT>;
+    using T = typename V::T;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    GenSmemMulti<VT> &S = *reinterpret_cast<GenSmemMulti<VT> *>(smem_raw);
+    const int tid = threadIdx.x;
+    uint32_t phase[2] = {0, 0};
+    for (int i = tid; i < 256 * 16; i += THREADS) (&S.tri[0][0])[i] = (&c_tri[0][0])[i];
+    S.nv[tid] = (tid == 0 || tid == 255) ? 0 : c_nverts[tid];
+    const unsigned int nactive = totals->active_bricks;
+    if (tid == 0) {
+        S.abort = 0;
+        for (int s = 0; s < 2; ++s) mbar_init(&S.bars[s], 1);
+        fence_barrier_init();
+        for (int s = 0; s < 2; ++s) {
+            const unsigned int w = blockIdx.x + s * gridDim.x;
+            if (w < nactive) issue_gen_tile<VT>(S, s, vols, nvol, maps, vofs, active[w]);
+        }
+    }
+    __syncthreads();
+    int it = 0;
+    for (unsigned int w = blockIdx.x; w < nactive; w += gridDim.x, ++it) {
+        const int s = it & 1;
+        T *tile = reinterpret_cast<T *>(S.tiles[s]);
+        const long long b = S.sbrick[s];
+        const unsigned long long vbase = S.svbase[s];
+        const int v = S.svol[s];
+        const VolDesc &d = vols[v];
+        const BrickPos bp = brick_pos(b - d.brick_base, d.nbx, d.nby);
+        if (S.stma[s]) {
+            if (tid == 0) {
+                if (!mbar_wait(&S.bars[s], phase[s])) S.abort = 1;
+            }
+            phase[s] ^= 1u;
+        } else {
+            fill_tile<VT, TX, TY, TZ>(tile, static_cast<const T *>(d.data), d.nx, d.ny, d.nz, bp.x0 - TXO,
+                                      bp.y0 - TYO, bp.z0 - TZO);
+        }
+        __syncthreads();
+        if (S.abort) break;
+        GenOut o;
+        o.soup = d.soup;
+        o.normals = d.normals;
+        o.vi2vox = d.vi2vox;
+        o.ver_voxel = d.ver_voxel;
+        o.tri_cube = d.tri_cube;
+        o.cap = d.cap;
+        generate_brick<VT>(S, tile, static_cast<const T *>(d.data), d.nx, d.ny, d.nz, d.cell, bp.x0, bp.y0, bp.z0,
+                           vbase, o);
+        __syncthreads();  // tile s, the list and the stage are free again
+        if (tid == 0) {
+            const unsigned int wn = w + 2 * gridDim.x;
+            if (wn < nactive) issue_gen_tile<VT>(S, s, vols, nvol, maps, vofs, active[wn]);
+        }
+    }
+    if (S.abort && tid == 0) {
+        atomicOr(&totals->flags, 1u);
+        for (int s = 0; s < 2; ++s) mbar_wait(&S.bars[s], phase[s], 100000000ull);
     }
 }
 
@@ -1013,6 +1263,7 @@ mcg_status mcg_mc_classify(mcg_context *ctx, const mcg_volume *vol, mcg_stream_t
     if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
     ctx->counts_pending = true;
     ctx->classified = true;
+    ctx->batch_classified = false;
     ctx->cls_data = vol->data;
     ctx->cls_nx = vol->nx;
     ctx->cls_ny = vol->ny;
@@ -1088,6 +1339,247 @@ mcg_status mcg_mc_normals(mcg_context *ctx, const mcg_volume *vol, const mcg_ver
             (const float2 *)vol->data, vol->nx, vol->ny, vol->nz, vol->cell, verts, n, normals);
     e = cudaGetLastError();
     return e == cudaSuccess ? MCG_OK : mcg_cuda_fail(ctx, e);
+}
+
+
+// ---- batched extraction host side -------------------------------------------------
+namespace mcg {
+namespace {
+
+// Device table layout: [VolDesc x nvol][pad to 64][classify maps x nvol][generate maps x nvol]
+size_t btab_desc_bytes(int nvol) { return ((sizeof(VolDesc) * (size_t)nvol + 63) / 64) * 64; }
+size_t btab_bytes(int nvol) { return btab_desc_bytes(nvol) + 2 * sizeof(CUtensorMap) * (size_t)nvol; }
+
+mcg_status grow_pinned(mcg_context *ctx, unsigned char **p, size_t *cap, size_t n) {
+    if (*cap >= n && *p) return MCG_OK;
+    if (*p) {
+        if (ctx->btab_pending) cudaEventSynchronize(ctx->btab_copied);
+        cudaFreeHost(*p);
+    }
+    *p = nullptr;
+    *cap = 0;
+    if (cudaMallocHost((void **)p, n) != cudaSuccess) return mcg_cuda_fail(ctx, cudaErrorMemoryAllocation);
+    *cap = n;
+    return MCG_OK;
+}
+
+bool batch_ok(const mcg_volume *vols, int32_t nvol) {
+    if (!vols || nvol < 1) return false;
+    for (int v = 0; v < nvol; ++v) {
+        if (!vol_ok(&vols[v])) return false;
+        if (vols[v].voxel_type != vols[0].voxel_type) return false;
+    }
+    return true;
+}
+
+// host copy of the table into pinned staging, then to the device on stream s
+mcg_status upload_btab(mcg_context *ctx, const mcg_volume *vols, const mcg_mesh_out *outs, int32_t nvol,
+                       bool with_maps, cudaStream_t s, long long *total_bricks) {
+    const size_t bytes = btab_bytes(nvol);
+    if (!ensure(&ctx->d_btab, &ctx->d_btab_cap, bytes)) return mcg_cuda_fail(ctx, cudaErrorMemoryAllocation);
+    mcg_status st = grow_pinned(ctx, &ctx->h_btab, &ctx->h_btab_cap, bytes);
+    if (st != MCG_OK) return st;
+    if (ctx->btab_pending) {
+        cudaError_t e = cudaEventSynchronize(ctx->btab_copied);
+        if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
+        ctx->btab_pending = false;
+    }
+    VolDesc *desc = reinterpret_cast<VolDesc *>(ctx->h_btab);
+    CUtensorMap *cmaps = reinterpret_cast<CUtensorMap *>(ctx->h_btab + btab_desc_bytes(nvol));
+    CUtensorMap *gmaps = cmaps + nvol;
+    long long base = 0;
+    const int eb = vols[0].voxel_type == MCG_VOXEL_SHORT2 ? 4 : 8;
+    for (int v = 0; v < nvol; ++v) {
+        const Geometry g = geometry(vols[v].nx, vols[v].ny, vols[v].nz);
+        VolDesc &d = desc[v];
+        memset(&d, 0, sizeof(d));
+        d.data = vols[v].data;
+        d.nx = vols[v].nx;
+        d.ny = vols[v].ny;
+        d.nz = vols[v].nz;
+        d.cell = vols[v].cell;
+        d.nbx = g.nbx;
+        d.nby = g.nby;
+        d.brick_base = base;
+        d.nbricks = g.nbricks;
+        base += g.nbricks;
+        if (outs) {
+            d.soup = outs[v].soup;
+            d.normals = outs[v].soup_normals;
+            d.vi2vox = outs[v].vi2vox;
+            d.ver_voxel = outs[v].ver_voxel;
+            d.tri_cube = outs[v].tri_cube;
+            d.cap = outs[v].capacity_vertices;
+        }
+        // TMA only when both boxes can be described (the flag serves both passes)
+        const bool tc = encode_volume_map(&cmaps[v], vols[v].data, vols[v].nx, vols[v].ny, vols[v].nz, eb, CTX, CTY, CTZ);
+        const bool tg = encode_volume_map(&gmaps[v], vols[v].data, vols[v].nx, vols[v].ny, vols[v].nz, eb, TX, TY, TZ);
+        d.tma = tc && tg ? 1 : 0;
+        if (!d.tma) {
+            memset(&cmaps[v], 0, sizeof(CUtensorMap));
+            memset(&gmaps[v], 0, sizeof(CUtensorMap));
+        }
+    }
+    *total_bricks = base;
+    const size_t n = with_maps ? bytes : btab_desc_bytes(nvol);
+    cudaError_t e = cudaMemcpyAsync(ctx->d_btab, ctx->h_btab, n, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaEventRecord(ctx->btab_copied, s);
+    if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
+    ctx->btab_pending = true;
+    return MCG_OK;
+}
+
+template <int VT>
+void launch_classify_multi(mcg_context *ctx, int nvol, long long nbricks, cudaStream_t s) {
+    const size_t smem = sizeof(ClsSmemMulti<VT>);
+    static int occ = 0;
+    if (!occ) occ = occupancy(mc_classify_multi_kernel<VT>, CTHREADS, smem);
+    long long grid = (long long)ctx->num_sms * occ;
+    if (grid > nbricks) grid = nbricks;
+    const VolDesc *desc = reinterpret_cast<const VolDesc *>(ctx->d_btab);
+    const CUtensorMap *cmaps = reinterpret_cast<const CUtensorMap *>(ctx->d_btab + btab_desc_bytes(nvol));
+    mc_classify_multi_kernel<VT><<<(int)grid, CTHREADS, smem, s>>>(desc, cmaps, nvol, nbricks, ctx->brick_tris,
+                                                                    ctx->brick_occ, ctx->d_vol_sums,
+                                                                    &ctx->d_totals->flags);
+}
+
+template <int VT>
+void launch_generate_multi(mcg_context *ctx, int nvol, long long nbricks, cudaStream_t s) {
+    const size_t smem = sizeof(GenSmemMulti<VT>);
+    static int occ = 0;
+    if (!occ) occ = occupancy(mc_generate_multi_kernel<VT>, THREADS, smem);
+    long long grid = (long long)ctx->num_sms * occ;
+    if (grid > nbricks) grid = nbricks;
+    const VolDesc *desc = reinterpret_cast<const VolDesc *>(ctx->d_btab);
+    const CUtensorMap *gmaps = reinterpret_cast<const CUtensorMap *>(ctx->d_btab + btab_desc_bytes(nvol)) + nvol;
+    mc_generate_multi_kernel<VT><<<(int)grid, THREADS, smem, s>>>(desc, gmaps, nvol, ctx->active, ctx->brick_vofs,
+                                                                   ctx->d_totals);
+}
+
+}  // namespace
+}  // namespace mcg
+
+mcg_status mcg_mc_classify_batched(mcg_context *ctx, const mcg_volume *vols, int32_t nvol, mcg_stream_t stream) {
+    if (!ctx || !batch_ok(vols, nvol)) return MCG_ERR_INVALID_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e == cudaSuccess) e = upload_tables(ctx->device);
+    if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
+    long long nbricks = 0;
+    for (int v = 0; v < nvol; ++v) nbricks += geometry(vols[v].nx, vols[v].ny, vols[v].nz).nbricks;
+    if (nbricks >= (1ll << 32)) return MCG_ERR_INVALID_ARG;
+    if (!ensure(&ctx->brick_tris, &ctx->brick_tris_cap, (size_t)nbricks) ||
+        !ensure(&ctx->brick_occ, &ctx->brick_occ_cap, (size_t)(3 * num_chunks(nbricks))) ||
+        !ensure(&ctx->brick_vofs, &ctx->brick_vofs_cap, (size_t)nbricks) ||
+        !ensure(&ctx->active, &ctx->active_cap, (size_t)nbricks) ||
+        !ensure(&ctx->d_vol_sums, &ctx->d_vol_sums_cap, (size_t)(2 * nvol)))
+        return mcg_cuda_fail(ctx, cudaErrorMemoryAllocation);
+    if (ctx->h_vol_sums_cap < (size_t)(2 * nvol)) {
+        if (ctx->counts_pending) cudaEventSynchronize(ctx->counts_ready);
+        if (ctx->h_vol_sums) cudaFreeHost(ctx->h_vol_sums);
+        ctx->h_vol_sums = nullptr;
+        ctx->h_vol_sums_cap = 0;
+        if (cudaMallocHost((void **)&ctx->h_vol_sums, sizeof(unsigned long long) * 2 * nvol) != cudaSuccess)
+            return mcg_cuda_fail(ctx, cudaErrorMemoryAllocation);
+        ctx->h_vol_sums_cap = 2 * nvol;
+    }
+    long long total = 0;
+    mcg_status st = upload_btab(ctx, vols, nullptr, nvol, true, s, &total);
+    if (st != MCG_OK) return st;
+    e = cudaMemsetAsync(&ctx->d_totals->flags, 0, sizeof(unsigned int), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(ctx->brick_occ, 0, sizeof(uint32_t) * 3 * num_chunks(nbricks), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(ctx->d_vol_sums, 0, sizeof(unsigned long long) * 2 * nvol, s);
+    if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
+    if (vols[0].voxel_type == MCG_VOXEL_SHORT2) launch_classify_multi<MCG_VOXEL_SHORT2>(ctx, nvol, nbricks, s);
+    else launch_classify_multi<MCG_VOXEL_FLOAT2>(ctx, nvol, nbricks, s);
+    mc_scan_kernel<<<(unsigned int)num_chunks(nbricks), CHUNK, 0, s>>>(ctx->brick_tris, ctx->brick_occ, nbricks,
+                                                                      ctx->brick_vofs, ctx->active, ctx->d_totals);
+    e = cudaGetLastError();
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(ctx->h_totals, ctx->d_totals, sizeof(MeshTotals), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(ctx->h_vol_sums, ctx->d_vol_sums, sizeof(unsigned long long) * 2 * nvol,
+                            cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaEventRecord(ctx->counts_ready, s);
+    if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
+    ctx->counts_pending = true;
+    ctx->batch_classified = true;
+    ctx->batch_nvol = nvol;
+    ctx->batch_nbricks = nbricks;
+    ctx->batch_vtype = vols[0].voxel_type;
+    ctx->batch_first_data = vols[0].data;
+    if (ctx->batch_caps_cap < (size_t)nvol) {
+        delete[] ctx->batch_caps;
+        ctx->batch_caps = new int64_t[nvol];
+        ctx->batch_caps_cap = nvol;
+    }
+    for (int v = 0; v < nvol; ++v) ctx->batch_caps[v] = -1;
+    ctx->classified = false;  // the single-volume state no longer matches the scratch
+    return MCG_OK;
+}
+
+mcg_status mcg_mc_counts_batched(mcg_context *ctx, mcg_mesh_counts *out, int32_t nvol) {
+    if (!ctx || !out) return MCG_ERR_INVALID_ARG;
+    if (!ctx->batch_classified) return MCG_ERR_STATE;
+    if (nvol != ctx->batch_nvol) return MCG_ERR_INVALID_ARG;
+    if (ctx->counts_pending) {
+        cudaError_t e = cudaEventSynchronize(ctx->counts_ready);
+        if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
+        ctx->counts_pending = false;
+    }
+    mcg_status worst = MCG_OK;
+    for (int v = 0; v < nvol; ++v) {
+        mcg_mesh_counts &c = out[v];
+        c.triangles = (int64_t)ctx->h_vol_sums[2 * v];
+        c.vertices = 3 * c.triangles;
+        c.occupied = (int64_t)ctx->h_vol_sums[2 * v + 1];
+        c.active_bricks = 0;
+        c.status = MCG_OK;
+        if (ctx->h_totals->flags & 1u) c.status = MCG_ERR_TIMEOUT;
+        else if (ctx->batch_caps[v] >= 0 && c.vertices > ctx->batch_caps[v]) c.status = MCG_ERR_CAPACITY;
+        c.reserved = 0;
+        if (c.status != MCG_OK && worst != MCG_ERR_TIMEOUT) worst = (mcg_status)c.status;
+    }
+    return worst;
+}
+
+mcg_status mcg_mc_generate_batched(mcg_context *ctx, const mcg_volume *vols, const mcg_mesh_out *outs, int32_t nvol,
+                                   mcg_stream_t stream) {
+    if (!ctx || !batch_ok(vols, nvol) || !outs) return MCG_ERR_INVALID_ARG;
+    if (!ctx->batch_classified || nvol != ctx->batch_nvol || vols[0].voxel_type != ctx->batch_vtype ||
+        vols[0].data != ctx->batch_first_data)
+        return MCG_ERR_STATE;
+    for (int v = 0; v < nvol; ++v)
+        if (outs[v].capacity_vertices < 0) return MCG_ERR_INVALID_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
+    for (int v = 0; v < nvol; ++v)
+        if (outs[v].ver_voxel) {
+            e = cudaMemsetAsync(outs[v].ver_voxel, 0, sizeof(int16_t) * (size_t)vols[v].nx * vols[v].ny * vols[v].nz, s);
+            if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
+        }
+    long long total = 0;
+    mcg_status st = upload_btab(ctx, vols, outs, nvol, false, s, &total);
+    if (st != MCG_OK) return st;
+    if (total != ctx->batch_nbricks) return MCG_ERR_STATE;
+    if (vols[0].voxel_type == MCG_VOXEL_SHORT2) launch_generate_multi<MCG_VOXEL_SHORT2>(ctx, nvol, total, s);
+    else launch_generate_multi<MCG_VOXEL_FLOAT2>(ctx, nvol, total, s);
+    e = cudaGetLastError();
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(ctx->h_totals, ctx->d_totals, sizeof(MeshTotals), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaEventRecord(ctx->counts_ready, s);
+    if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
+    ctx->counts_pending = true;
+    for (int v = 0; v < nvol; ++v) ctx->batch_caps[v] = outs[v].capacity_vertices;
+    return MCG_OK;
+}
+
+mcg_status mcg_mc_extract_batched(mcg_context *ctx, const mcg_volume *vols, const mcg_mesh_out *outs, int32_t nvol,
+                                  mcg_stream_t stream) {
+    mcg_status st = mcg_mc_classify_batched(ctx, vols, nvol, stream);
+    if (st != MCG_OK) return st;
+    return mcg_mc_generate_batched(ctx, vols, outs, nvol, stream);
 }
 
 // ---- extraction without any allocation ------------------------------------------

@@ -61,6 +61,26 @@ struct mcg_context {
     int cls_nx = 0, cls_ny = 0, cls_nz = 0, cls_vtype = 0;
     int64_t last_capacity = -1;
 
+    // batched extraction: device tables (volume descriptors, classify and
+    // generate tensor maps), pinned staging for them, per-volume sums
+    unsigned char *d_btab = nullptr;
+    size_t d_btab_cap = 0;
+    unsigned char *h_btab = nullptr;  // pinned
+    size_t h_btab_cap = 0;
+    cudaEvent_t btab_copied = nullptr;
+    bool btab_pending = false;
+    unsigned long long *d_vol_sums = nullptr;
+    size_t d_vol_sums_cap = 0;
+    unsigned long long *h_vol_sums = nullptr;  // pinned
+    size_t h_vol_sums_cap = 0;
+    int batch_nvol = 0;
+    long long batch_nbricks = 0;
+    bool batch_classified = false;
+    int batch_vtype = 0;
+    const void *batch_first_data = nullptr;
+    int64_t *batch_caps = nullptr;  // host, last generate's capacities
+    size_t batch_caps_cap = 0;
+
     // integrate scratch
     float *depth_scaled = nullptr;
     size_t depth_scaled_cap = 0;

@@ -51,6 +51,41 @@ def random_volume(shape, seed=0, p_zero_weight=0.05, sentinel_frac=0.1):
     return np.stack([t.astype(np.int16), w.astype(np.uint16).view(np.int16)], axis=-1)
 
 
+def batch_volumes(n=64, seed=0, lo=32, hi=256, device="cpu", trunc=5.0):
+    """n short2 volumes (nz, ny, nx, 2), each axis round(exp(U[ln lo, ln hi])),
+    each the truncated SDF (trunc voxels, scaled to 32767) of 1-8 random
+    spheres and boxes (union), weights uniform in [1, 128]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        dims = np.round(np.exp(rng.uniform(np.log(lo), np.log(hi), size=3))).astype(int)
+        nx, ny, nz = (int(d) for d in dims)
+        nobj = int(rng.integers(1, 9))
+        dev = torch.device(device)
+        z = torch.arange(nz, device=dev, dtype=torch.float32)[:, None, None] + 0.5
+        y = torch.arange(ny, device=dev, dtype=torch.float32)[None, :, None] + 0.5
+        x = torch.arange(nx, device=dev, dtype=torch.float32)[None, None, :] + 0.5
+        sd = torch.full((nz, ny, nx), 1e9, device=dev)
+        for _ in range(nobj):
+            c = rng.uniform(0.2, 0.8, size=3) * np.array([nx, ny, nz])
+            if rng.random() < 0.5:
+                r = rng.uniform(0.1, 0.35) * min(nx, ny, nz)
+                d = torch.sqrt((x - c[0]) ** 2 + (y - c[1]) ** 2 + (z - c[2]) ** 2) - r
+            else:
+                h = rng.uniform(0.05, 0.3, size=3) * np.array([nx, ny, nz])
+                qx, qy, qz = (x - c[0]).abs() - h[0], (y - c[1]).abs() - h[1], (z - c[2]).abs() - h[2]
+                outside = torch.sqrt(qx.clamp(min=0) ** 2 + qy.clamp(min=0) ** 2 + qz.clamp(min=0) ** 2)
+                inside = torch.clamp(torch.maximum(torch.maximum(qx, qy), qz), max=0)
+                d = outside + inside
+            sd = torch.minimum(sd, d)
+        t = torch.trunc(torch.clamp(sd / trunc, -1, 1) * 32767).to(torch.int16)
+        g = torch.Generator(device=dev)
+        g.manual_seed(seed * 100003 + i)
+        w = torch.randint(1, 129, (nz, ny, nx), generator=g, device=dev, dtype=torch.int32).to(torch.int16)
+        out.append(torch.stack([t, w], dim=-1).contiguous())
+    return out
+
+
 # ---------------------------------------------------------------------------
 # fusion scene
 # ---------------------------------------------------------------------------
