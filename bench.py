@@ -47,6 +47,8 @@ def parse():
     ap.add_argument("--n", type=int, default=N_VOX, help="volume edge (default 512)")
     ap.add_argument("--frames", type=int, default=N_FRAMES)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-graph", action="store_true")
     return ap.parse_args()
 
 
@@ -150,6 +152,108 @@ def cpu_baseline(orc, vol_np, cell, target_s=8.0):
             "sample": "oracle FP32-mirror extraction (classify+scan+generate+normals) of the whole %s volume, "
                       "%d triangles, median of %d runs (%.3f s each)" % ("x".join(map(str, vol_np.shape[:3])),
                                                                          ntri, len(times), dt)}
+
+
+def bench_batched(mcg, synthetic, torch, ctx, n=64, reps=10):
+    """64 volumes, each axis log-uniform in [32, 256], 1-8 spheres/boxes:
+    one batched extraction vs a loop of single-volume extractions (both
+    asynchronous, into preallocated soup + normal buffers)."""
+    vols = synthetic.batch_volumes(n, seed=7, lo=32, hi=256, device="cuda")
+    cells = [0.01] * n
+    meshes = mcg.extract_batched(vols, cells, normals=True)
+    caps = [max(m.num_vertices, 1) for m in meshes]
+    outs = [{"soup": torch.empty((c, 28), dtype=torch.uint8, device="cuda"),
+             "normals": torch.empty((c, 3), dtype=torch.float32, device="cuda")} for c in caps]
+    del meshes
+    ctxs = ctx
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def loop():
+        for v, o, c in zip(vols, outs, caps):
+            mcg.extract_into(v, 0.01, o, c, ctx=ctxs)
+
+    def batch():
+        mcg.extract_batched_into(vols, cells, outs, caps, ctx=ctxs)
+
+    res = {}
+    for name, fn in (("loop", loop), ("batched", batch)):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        res[name + "_ms"] = e0.elapsed_time(e1) / reps
+    vox = sum(int(v.shape[0]) * int(v.shape[1]) * int(v.shape[2]) for v in vols)
+    tris = sum(c // 3 for c in caps)
+    return {"volumes": n, "voxels": vox, "triangles": tris, "loop_ms": res["loop_ms"],
+            "batched_ms": res["batched_ms"], "speedup": res["loop_ms"] / res["batched_ms"],
+            "batched_gvoxels_per_s": vox / (res["batched_ms"] * 1e-3) / 1e9}
+
+
+def bench_graph(mcg, synthetic, torch, n=256, frames=20):
+    """Per-frame depth maps + integrate + extract of a 256^3 fusion volume,
+    eager launches vs one captured CUDA graph replayed per frame."""
+    scene = synthetic.FusionScene(seed=1, extent=EXTENT)
+    k = mcg.intrinsic(FX, FY, CX, CY)
+    depths = []
+    poses = []
+    for i in range(frames):
+        R, t = scene.pose(i, frames)
+        depths.append(synthetic.mm_to_u16_bits(scene.depth_frame(R, t, w=W, h=H, fx=FX, fy=FY, cx=CX, cy=CY,
+                                                                  seed=i, device="cuda")))
+        poses.append(mcg.extrinsic(R, t))
+    ctx = mcg.Context()
+    v = mcg.voxel_new((n, n, n), TRUNC, TRUNC, EXTENT / n)
+    cap = 4 * 1000 * 1000
+    out = {"soup": torch.empty((cap, 28), dtype=torch.uint8, device="cuda"),
+           "normals": torch.empty((cap, 3), dtype=torch.float32, device="cuda")}
+    d_in = torch.empty_like(depths[0])
+    meter = torch.empty((H, W), dtype=torch.float32, device="cuda")
+    import ctypes
+    from marching_cube_gb300 import _capi
+    lib = mcg._lib
+    pose_all = torch.stack([mcg.extrinsic_tensor(*scene.pose(i, frames)) for i in range(frames)])
+    pose_dev = torch.empty(12, dtype=torch.float32, device="cuda")
+
+    def frame(stream):
+        mcg.depth_to_maps(d_in, k, vertex=False, normal=False, ctx=ctx, stream=stream, out_meter=meter)
+        mcg.volumetric_integration_device_pose(v, k, pose_dev, meter, ctx=ctx, stream=stream)
+        mcg.extract_into(v.data, EXTENT / n, out, cap, ctx=ctx, stream=stream)
+
+    st = torch.cuda.Stream()
+    with torch.cuda.stream(st):
+        d_in.copy_(depths[0])
+        pose_dev.copy_(pose_all[0])
+        frame(st)  # warm-up: scratch allocation, tables
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(st):
+        e0.record(st)
+        for i in range(frames):
+            d_in.copy_(depths[i])
+            pose_dev.copy_(pose_all[i])
+            frame(st)
+        e1.record(st)
+    torch.cuda.synchronize()
+    eager_ms = e0.elapsed_time(e1) / frames
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=st):
+        frame(st)
+    torch.cuda.synchronize()
+    with torch.cuda.stream(st):
+        e0.record(st)
+        for i in range(frames):
+            d_in.copy_(depths[i])
+            pose_dev.copy_(pose_all[i])
+            g.replay()
+        e1.record(st)
+    torch.cuda.synchronize()
+    graph_ms = e0.elapsed_time(e1) / frames
+    return {"volume": [n, n, n], "frames": frames, "eager_ms_per_frame": eager_ms, "graph_ms_per_frame": graph_ms}
+
 
 
 def run_reference(args):
@@ -329,6 +433,19 @@ def main():
     except Exception as ex:  # pragma: no cover
         e2e = {"value": None, "unit": UNIT, "error": str(ex)}
 
+    batched = None
+    if not args.no_batched:
+        try:
+            batched = bench_batched(mcg, synthetic, torch, ctx)
+        except Exception as ex:  # pragma: no cover
+            batched = {"error": str(ex)}
+    graph = None
+    if not args.no_graph:
+        try:
+            graph = bench_graph(mcg, synthetic, torch)
+        except Exception as ex:  # pragma: no cover
+            graph = {"error": str(ex)}
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         try:
@@ -350,6 +467,8 @@ def main():
         "clocks": clk.summary(), "gpu_launches": 3 * args.steps,
         "triangles_per_s": ntri * world / (ms_per_step * 1e-3),
         "integrate": integ,
+        "batched": batched,
+        "graph": graph,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -177,6 +177,15 @@ mcg_status mcg_integrate(mcg_context *ctx, void *vol, int32_t voxel_type, int32_
                          const float *depth_m, const float *normals, int32_t is_dynamic,
                          mcg_stream_t stream);
 
+/* Same update with the camera pose read from device memory: pose_dev holds
+ * 12 floats, the rotation column-major (r[9]) then t[3], as mcg_extrinsic.
+ * A CUDA graph captured around this call stays valid when the pose buffer
+ * is rewritten between replays. */
+mcg_status mcg_integrate_device_pose(mcg_context *ctx, void *vol, int32_t voxel_type, int32_t nx, int32_t ny,
+                                     int32_t nz, float min_t, float max_t, float grid_s, const mcg_intrinsic *k,
+                                     const float *pose_dev, int32_t w, int32_t h, const float *depth_m,
+                                     const float *normals, int32_t is_dynamic, mcg_stream_t stream);
+
 /* ---- RLE volume codec: kf.cu:1303-1600 ----------------------------------- */
 /* upper bound of the encoded file image size */
 int64_t mcg_rle_bound(int32_t nx, int32_t ny, int32_t nz);

@@ -396,17 +396,22 @@ def extrinsic(R, t):
 
 
 def depth_to_maps(depth_mm, k, depth_min=KINECT_DEPTH_MIN, depth_max=KINECT_DEPTH_MAX, meter=True,
-                  vertex=True, normal=True, ctx=None, stream=None):
-    """uint16-mm depth (h, w) -> metre (h, w), vertex (h, w, 3), normal (h, w, 3)."""
+                  vertex=True, normal=True, ctx=None, stream=None, out_meter=None, out_vertex=None,
+                  out_normal=None):
+    """uint16-mm depth (h, w) -> metre (h, w), vertex (h, w, 3), normal (h, w, 3).
+    out_* may supply preallocated outputs (e.g. inside a CUDA graph capture)."""
     if depth_mm.dtype not in (torch.int16, torch.uint16) or not depth_mm.is_cuda or depth_mm.dim() != 2:
         raise ValueError("depth_mm must be a (h, w) 16-bit CUDA tensor")
     depth_mm = depth_mm.contiguous()
     ctx = ctx or default_context(depth_mm.device.index)
     h, w = depth_mm.shape
     dev = depth_mm.device
-    m = torch.empty((h, w), dtype=torch.float32, device=dev) if meter else None
-    v = torch.empty((h, w, 3), dtype=torch.float32, device=dev) if vertex else None
-    n = torch.empty((h, w, 3), dtype=torch.float32, device=dev) if normal else None
+    m = out_meter if out_meter is not None else (
+        torch.empty((h, w), dtype=torch.float32, device=dev) if meter else None)
+    v = out_vertex if out_vertex is not None else (
+        torch.empty((h, w, 3), dtype=torch.float32, device=dev) if vertex else None)
+    n = out_normal if out_normal is not None else (
+        torch.empty((h, w, 3), dtype=torch.float32, device=dev) if normal else None)
     ctx.check(_lib.mcg_depth_to_maps(ctx.handle, ctypes.byref(k), w, h, _ptr(depth_mm), float(depth_min),
                                      float(depth_max), _ptr(m), _ptr(v), _ptr(n), _stream(stream)),
               "mcg_depth_to_maps")
@@ -447,6 +452,31 @@ def volumetric_integration(v: Voxel, k, e, depth_m, normals=None, is_dynamic=Fal
                                  ctypes.byref(k), ctypes.byref(e), w, h, _ptr(depth_m), _ptr(normals),
                                  1 if is_dynamic else 0, _stream(stream)),
               "mcg_integrate")
+
+
+def extrinsic_tensor(R, t, device=None):
+    """Pose as a 12-float device tensor (rotation column-major, then t) for
+    volumetric_integration_device_pose."""
+    import numpy as np
+    e = extrinsic(R, t)
+    host = torch.tensor(list(e.r) + list(e.t), dtype=torch.float32)
+    return host.to(device or torch.device("cuda", torch.cuda.current_device()))
+
+
+def volumetric_integration_device_pose(v: Voxel, k, pose_dev, depth_m, normals=None, is_dynamic=False, ctx=None,
+                                       stream=None):
+    """volumetric_integration with the pose read from a device tensor (12
+    floats), so a captured CUDA graph can be replayed with new poses."""
+    vt = _check_volume(v.data)
+    if pose_dev.dtype != torch.float32 or pose_dev.numel() != 12 or not pose_dev.is_cuda:
+        raise ValueError("pose_dev must be 12 float32 values on the device")
+    ctx = ctx or default_context(v.data.device.index)
+    h, w = depth_m.shape
+    nx, ny, nz = v.size
+    ctx.check(_lib.mcg_integrate_device_pose(ctx.handle, _ptr(v.data), vt, nx, ny, nz, v.min_t, v.max_t, v.grid_s,
+                                             ctypes.byref(k), _ptr(pose_dev), w, h, _ptr(depth_m), _ptr(normals),
+                                             1 if is_dynamic else 0, _stream(stream)),
+              "mcg_integrate_device_pose")
 
 
 # ---------------------------------------------------------------------------

@@ -69,6 +69,9 @@ SIGNATURES = {
     "mcg_integrate": (c_int, [c_void_p, c_void_p, c_int32, c_int32, c_int32, c_int32, c_float, c_float,
                               c_float, ctypes.POINTER(Intrinsic), ctypes.POINTER(Extrinsic), c_int32,
                               c_int32, c_void_p, c_void_p, c_int32, c_void_p]),
+    "mcg_integrate_device_pose": (c_int, [c_void_p, c_void_p, c_int32, c_int32, c_int32, c_int32, c_float, c_float,
+                                          c_float, ctypes.POINTER(Intrinsic), c_void_p, c_int32, c_int32, c_void_p,
+                                          c_void_p, c_int32, c_void_p]),
     "mcg_rle_bound": (c_int64, [c_int32, c_int32, c_int32]),
     "mcg_rle_encode": (c_int, [c_void_p, c_void_p, c_int32, c_int32, c_int32, c_float, c_float, c_float,
                                c_int32, c_void_p, c_int64, ctypes.POINTER(c_int64), c_void_p]),

@@ -156,8 +156,22 @@ struct IntegParams {
     const float *ds;        // ray-length depth
     const float3 *normals;  // optional normal map
     const float *ray_x;     // accumulated x coordinate per voxel column
+    const float *pose_dev;  // if set: r[9], t[3] read from device memory (graph replay)
     int is_dynamic;
 };
+
+// pose from device memory into the block's copy of the parameters
+__device__ __forceinline__ void load_pose(IntegParams &p) {
+    __shared__ float pose[12];
+    if (p.pose_dev) {
+        if (threadIdx.x < 12) pose[threadIdx.x] = p.pose_dev[threadIdx.x];
+        __syncthreads();
+#pragma unroll
+        for (int i = 0; i < 9; ++i) p.r[i] = pose[i];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) p.t[i] = pose[9 + i];
+    }
+}
 
 // d_pack_tsdf / d_pack_weight / d_unpack_weight (cu_kinect_fusion_v1.h:152-171)
 __device__ __forceinline__ short pack_tsdf(float f) { return (short)(int)(f * (float)kMaxTsdf); }
@@ -219,6 +233,7 @@ __device__ __forceinline__ void fuse(const IntegParams &p, float sdf, float weig
 
 // short2 volume, 4 voxels per thread; vec = 16-byte path usable
 __global__ void __launch_bounds__(256) integrate_short2_kernel(IntegParams p, short2 *__restrict__ vol, int vec) {
+    load_pose(p);
     const int groups = (p.nx + 3) >> 2;
     const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long rows = (long long)p.ny * p.nz;
@@ -275,6 +290,7 @@ __global__ void __launch_bounds__(256) integrate_short2_kernel(IntegParams p, sh
 
 // float2 volume (FP32 tsdf and weight, no packing), 2 voxels per thread
 __global__ void __launch_bounds__(256) integrate_float2_kernel(IntegParams p, float2 *__restrict__ vol, int vec) {
+    load_pose(p);
     const int groups = (p.nx + 1) >> 1;
     const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long rows = (long long)p.ny * p.nz;
@@ -405,12 +421,12 @@ mcg_status mcg_vertex_to_normal(mcg_context *ctx, int32_t w, int32_t h, const fl
     return e == cudaSuccess ? MCG_OK : mcg_cuda_fail(ctx, e);
 }
 
-mcg_status mcg_integrate(mcg_context *ctx, void *vol, int32_t voxel_type, int32_t nx, int32_t ny,
-                         int32_t nz, float min_t, float max_t, float grid_s,
-                         const mcg_intrinsic *k, const mcg_extrinsic *ext, int32_t w, int32_t h,
-                         const float *depth_m, const float *normals, int32_t is_dynamic,
-                         mcg_stream_t stream) {
-    if (!ctx || !vol || !k || !ext || !depth_m || nx <= 0 || ny <= 0 || nz <= 0 || w <= 0 || h <= 0)
+static mcg_status integrate_impl(mcg_context *ctx, void *vol, int32_t voxel_type, int32_t nx, int32_t ny,
+                                 int32_t nz, float min_t, float max_t, float grid_s, const mcg_intrinsic *k,
+                                 const mcg_extrinsic *ext, const float *pose_dev, int32_t w, int32_t h,
+                                 const float *depth_m, const float *normals, int32_t is_dynamic,
+                                 mcg_stream_t stream) {
+    if (!ctx || !vol || !k || (!ext && !pose_dev) || !depth_m || nx <= 0 || ny <= 0 || nz <= 0 || w <= 0 || h <= 0)
         return MCG_ERR_INVALID_ARG;
     if (voxel_type != MCG_VOXEL_SHORT2 && voxel_type != MCG_VOXEL_FLOAT2) return MCG_ERR_INVALID_ARG;
     if (!(min_t > 0.0f) || !(max_t > 0.0f) || !(grid_s > 0.0f)) return MCG_ERR_INVALID_ARG;
@@ -447,8 +463,9 @@ mcg_status mcg_integrate(mcg_context *ctx, void *vol, int32_t voxel_type, int32_
     p.nx = nx; p.ny = ny; p.nz = nz;
     p.min_t = min_t; p.max_t = max_t; p.grid_s = grid_s;
     p.k = intr_of(k);
-    for (int i = 0; i < 9; ++i) p.r[i] = ext->r[i];
-    for (int i = 0; i < 3; ++i) p.t[i] = ext->t[i];
+    for (int i = 0; i < 9; ++i) p.r[i] = ext ? ext->r[i] : 0.0f;
+    for (int i = 0; i < 3; ++i) p.t[i] = ext ? ext->t[i] : 0.0f;
+    p.pose_dev = ext ? nullptr : pose_dev;
     p.w = w; p.h = h;
     p.ds = ctx->depth_scaled;
     p.normals = (const float3 *)normals;
@@ -468,6 +485,25 @@ mcg_status mcg_integrate(mcg_context *ctx, void *vol, int32_t voxel_type, int32_
     }
     e = cudaGetLastError();
     return e == cudaSuccess ? MCG_OK : mcg_cuda_fail(ctx, e);
+}
+
+mcg_status mcg_integrate(mcg_context *ctx, void *vol, int32_t voxel_type, int32_t nx, int32_t ny,
+                         int32_t nz, float min_t, float max_t, float grid_s,
+                         const mcg_intrinsic *k, const mcg_extrinsic *ext, int32_t w, int32_t h,
+                         const float *depth_m, const float *normals, int32_t is_dynamic,
+                         mcg_stream_t stream) {
+    if (!ext) return MCG_ERR_INVALID_ARG;
+    return integrate_impl(ctx, vol, voxel_type, nx, ny, nz, min_t, max_t, grid_s, k, ext, nullptr, w, h, depth_m,
+                          normals, is_dynamic, stream);
+}
+
+mcg_status mcg_integrate_device_pose(mcg_context *ctx, void *vol, int32_t voxel_type, int32_t nx, int32_t ny,
+                                     int32_t nz, float min_t, float max_t, float grid_s, const mcg_intrinsic *k,
+                                     const float *pose_dev, int32_t w, int32_t h, const float *depth_m,
+                                     const float *normals, int32_t is_dynamic, mcg_stream_t stream) {
+    if (!pose_dev) return MCG_ERR_INVALID_ARG;
+    return integrate_impl(ctx, vol, voxel_type, nx, ny, nz, min_t, max_t, grid_s, k, nullptr, pose_dev, w, h,
+                          depth_m, normals, is_dynamic, stream);
 }
 
 }  // extern "C"

@@ -1259,9 +1259,8 @@ mcg_status mcg_mc_classify(mcg_context *ctx, const mcg_volume *vol, mcg_stream_t
     e = launch_count_phase(vol, g, ctx_scratch(ctx), ctx->num_sms, s);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(ctx->h_totals, ctx->d_totals, sizeof(MeshTotals), cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaEventRecord(ctx->counts_ready, s);
+    if (e == cudaSuccess) e = mcg_counts_event(ctx, s);
     if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
-    ctx->counts_pending = true;
     ctx->classified = true;
     ctx->batch_classified = false;
     ctx->cls_data = vol->data;
@@ -1309,9 +1308,8 @@ mcg_status mcg_mc_generate(mcg_context *ctx, const mcg_volume *vol, const mcg_me
     // the totals are re-read so a timeout flagged by generate is reported
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(ctx->h_totals, ctx->d_totals, sizeof(MeshTotals), cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaEventRecord(ctx->counts_ready, s);
+    if (e == cudaSuccess) e = mcg_counts_event(ctx, s);
     if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
-    ctx->counts_pending = true;
     ctx->last_capacity = out->capacity_vertices;
     return MCG_OK;
 }
@@ -1423,9 +1421,12 @@ mcg_status upload_btab(mcg_context *ctx, const mcg_volume *vols, const mcg_mesh_
     *total_bricks = base;
     const size_t n = with_maps ? bytes : btab_desc_bytes(nvol);
     cudaError_t e = cudaMemcpyAsync(ctx->d_btab, ctx->h_btab, n, cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaEventRecord(ctx->btab_copied, s);
+    // during capture the staging copy becomes a graph node that reads the
+    // staging buffer at every replay: it must then stay untouched
+    const bool cap = mcg_capturing(s);
+    if (e == cudaSuccess && !cap) e = cudaEventRecord(ctx->btab_copied, s);
     if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
-    ctx->btab_pending = true;
+    ctx->btab_pending = !cap;
     return MCG_OK;
 }
 
@@ -1500,9 +1501,8 @@ mcg_status mcg_mc_classify_batched(mcg_context *ctx, const mcg_volume *vols, int
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(ctx->h_vol_sums, ctx->d_vol_sums, sizeof(unsigned long long) * 2 * nvol,
                             cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaEventRecord(ctx->counts_ready, s);
+    if (e == cudaSuccess) e = mcg_counts_event(ctx, s);
     if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
-    ctx->counts_pending = true;
     ctx->batch_classified = true;
     ctx->batch_nvol = nvol;
     ctx->batch_nbricks = nbricks;
@@ -1568,9 +1568,8 @@ mcg_status mcg_mc_generate_batched(mcg_context *ctx, const mcg_volume *vols, con
     e = cudaGetLastError();
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(ctx->h_totals, ctx->d_totals, sizeof(MeshTotals), cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaEventRecord(ctx->counts_ready, s);
+    if (e == cudaSuccess) e = mcg_counts_event(ctx, s);
     if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
-    ctx->counts_pending = true;
     for (int v = 0; v < nvol; ++v) ctx->batch_caps[v] = outs[v].capacity_vertices;
     return MCG_OK;
 }

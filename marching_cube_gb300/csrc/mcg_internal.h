@@ -96,3 +96,26 @@ struct mcg_context {
 
 // records a CUDA failure on ctx and returns the matching status
 mcg_status mcg_cuda_fail(mcg_context *ctx, cudaError_t e);
+
+// true while `s` is being captured into a CUDA graph
+inline bool mcg_capturing(cudaStream_t s) {
+    cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &st) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return st == cudaStreamCaptureStatusActive;
+}
+
+// Marks the counts copied to pinned memory on stream s as pending.  During
+// capture no event is recorded: the copy is a node of the graph, and the
+// caller reads the counts after synchronising the graph's stream.
+inline cudaError_t mcg_counts_event(mcg_context *ctx, cudaStream_t s) {
+    if (mcg_capturing(s)) {
+        ctx->counts_pending = false;
+        return cudaSuccess;
+    }
+    cudaError_t e = cudaEventRecord(ctx->counts_ready, s);
+    if (e == cudaSuccess) ctx->counts_pending = true;
+    return e;
+}
