@@ -153,6 +153,16 @@ mcg_status mcg_mc_extract_noalloc(const mcg_volume *vol, const mcg_mesh_out *out
 mcg_status mcg_mc_normals(mcg_context *ctx, const mcg_volume *vol, const mcg_vertex_voxel *verts,
                           int64_t n, float *normals, mcg_stream_t stream);
 
+/* Adjoint of the soup positions (no counterpart in the reference; the
+ * positions follow mc.cu:243-264).  grad_pos: dL/dP, float3 per soup vertex
+ * in the order of the last mcg_mc_generate on ctx for this volume, the first
+ * n_vertices of them.  Accumulates dL/df into grad_f (one float per voxel,
+ * f = tsdf for FLOAT2 volumes, tsdf/32766 for SHORT2); the caller
+ * initialises grad_f.  Topology is held fixed (the derivative of the cube
+ * cases is zero almost everywhere).  FP32 accumulation with atomics. */
+mcg_status mcg_mc_backward(mcg_context *ctx, const mcg_volume *vol, const float *grad_pos, int64_t n_vertices,
+                           float *grad_f, mcg_stream_t stream);
+
 /* ---- depth maps: kf.cu:99-151 (d_kinect_depth_to_meter, d_img_meter_to_vertex,
  * d_img_vertex_to_normal), fused --------------------------------------------- */
 /* depth_mm: uint16 millimetres [h][w] (device).  meter/vertex/normal may be
@@ -185,6 +195,26 @@ mcg_status mcg_integrate_device_pose(mcg_context *ctx, void *vol, int32_t voxel_
                                      int32_t nz, float min_t, float max_t, float grid_s, const mcg_intrinsic *k,
                                      const float *pose_dev, int32_t w, int32_t h, const float *depth_m,
                                      const float *normals, int32_t is_dynamic, mcg_stream_t stream);
+
+/* Adjoint of n_frames integrate steps on a FLOAT2 volume (no counterpart in
+ * the reference; the forward is kf.cu:427-532 as mcg_integrate computes it).
+ * vol0: the volume before the first frame (nx*ny*nz float2), or NULL for the
+ * initial state (tsdf -1, weight 0).  poses_dev: n_frames x 12 floats on the
+ * device (rotation column-major, then t, as mcg_integrate_device_pose).
+ * depth_m: n_frames x h x w z-depth in metres; normals: NULL or
+ * n_frames x h x w float3 (held constant).  grad_f / grad_w: dL/dtsdf and
+ * dL/dweight after the last frame (grad_w may be NULL = 0).  Accumulates
+ * dL/ddepth into grad_depth (n_frames x h x w; the caller initialises it);
+ * grad_f0 / grad_w0 (may be NULL) receive dL/dtsdf and dL/dweight of vol0.
+ * The pixel choices, truncation and clamping of the forward are held fixed.
+ * MCG_ERR_TOO_LARGE above 512 frames per call: split the sequence and chain
+ * the calls through vol0 / grad_f0 / grad_w0. */
+mcg_status mcg_integrate_backward(mcg_context *ctx, const void *vol0, int32_t nx, int32_t ny, int32_t nz,
+                                  float min_t, float max_t, float grid_s, const mcg_intrinsic *k, int32_t n_frames,
+                                  const float *poses_dev, int32_t w, int32_t h, const float *depth_m,
+                                  const float *normals, int32_t is_dynamic, const float *grad_f,
+                                  const float *grad_w, float *grad_depth, float *grad_f0, float *grad_w0,
+                                  mcg_stream_t stream);
 
 /* ---- RLE volume codec: kf.cu:1303-1600 ----------------------------------- */
 /* upper bound of the encoded file image size */

@@ -13,6 +13,9 @@ reference's C++ interface:
     extract_surface_normals           cu_kinect_fusion_v1.cu:3227-3242
     run_length_encode / _decode       cu_kinect_fusion_v1.h:218-219
 
+Adjoints (no counterpart in the reference): mc_backward / integrate_backward
+and the autograd Functions behind mesh_positions / integrate_frames.
+
 Volumes are torch tensors of shape (nz, ny, nx, 2): int16 for the reference's
 short2 voxels {tsdf, w} (w reinterpreted as uint16), float32 for the FP32
 volume of the differentiable path.
@@ -36,6 +39,7 @@ MCG_ERR_TIMEOUT = 4
 MCG_ERR_IO = 5
 MCG_ERR_FORMAT = 6
 MCG_ERR_STATE = 7
+MCG_ERR_TOO_LARGE = 8
 
 VOXEL_SHORT2 = 0
 VOXEL_FLOAT2 = 1
@@ -477,6 +481,154 @@ def volumetric_integration_device_pose(v: Voxel, k, pose_dev, depth_m, normals=N
                                              ctypes.byref(k), _ptr(pose_dev), w, h, _ptr(depth_m), _ptr(normals),
                                              1 if is_dynamic else 0, _stream(stream)),
               "mcg_integrate_device_pose")
+
+
+# ---------------------------------------------------------------------------
+# adjoints: soup positions -> voxel values -> depth pixels
+# ---------------------------------------------------------------------------
+def mc_backward(volume, cell, grad_pos, grad_f=None, *, reclassify=True, ctx=None, stream=None):
+    """dL/df per voxel, (nz, ny, nx) float32, for dL/dP of the soup vertices
+    of extract(volume, cell) in the same order (grad_pos (n, 3) float32).
+    f is the tsdf of a float32 volume, tsdf/32766 of an int16 one.  grad_f,
+    if given, is accumulated into.  reclassify=False reuses the count phase
+    the last extraction on ctx ran for this volume (the volume must be
+    unchanged since)."""
+    ctx = ctx or default_context(volume.device.index)
+    cv = _cvol(volume, cell)
+    s = _stream(stream)
+    nz, ny, nx, _ = volume.shape
+    if grad_f is None:
+        grad_f = torch.zeros((nz, ny, nx), dtype=torch.float32, device=volume.device)
+    elif grad_f.dtype != torch.float32 or grad_f.numel() != nx * ny * nz or not grad_f.is_contiguous():
+        raise ValueError("grad_f must be a contiguous float32 tensor of nz*ny*nx values")
+    grad_pos = grad_pos.to(torch.float32).contiguous()
+    if grad_pos.dim() != 2 or grad_pos.shape[1] != 3:
+        raise ValueError("grad_pos must be (n, 3)")
+    if reclassify:
+        ctx.check(_lib.mcg_mc_classify(ctx.handle, ctypes.byref(cv), s), "mcg_mc_classify")
+    ctx.check(_lib.mcg_mc_backward(ctx.handle, ctypes.byref(cv), _ptr(grad_pos), grad_pos.shape[0], _ptr(grad_f),
+                                   s), "mcg_mc_backward")
+    return grad_f
+
+
+def _poses_tensor(poses, device):
+    if isinstance(poses, torch.Tensor):
+        p = poses.to(device=device, dtype=torch.float32).reshape(-1, 12).contiguous()
+    else:
+        p = torch.stack([extrinsic_tensor(R, t, device) for R, t in poses]).contiguous()
+    return p
+
+
+def integrate_backward(shape, min_t, max_t, grid_s, k, poses, depth, grad_f, grad_w=None, vol0=None, normals=None,
+                       is_dynamic=False, grad_depth=None, want_grad_vol0=False, ctx=None, stream=None):
+    """Adjoint of integrating depth frames (K, h, w) into a float32 volume of
+    shape (nz, ny, nx) with poses (K, 12) (see integrate_frames).  Returns
+    (grad_depth, grad_f0, grad_w0); the last two are None unless
+    want_grad_vol0.  Pixel choices, truncation and clamping are held fixed;
+    normal maps are constants."""
+    nz, ny, nx = shape
+    dev = depth.device
+    ctx = ctx or default_context(dev.index)
+    depth = depth.to(torch.float32).contiguous()
+    nf, h, w = depth.shape
+    pt = _poses_tensor(poses, dev)
+    if pt.shape[0] != nf:
+        raise ValueError("one pose per depth frame")
+    if grad_depth is None:
+        grad_depth = torch.zeros_like(depth)
+    gf = grad_f.to(torch.float32).contiguous()
+    gw = grad_w.to(torch.float32).contiguous() if grad_w is not None else None
+    if gf.numel() != nx * ny * nz or (gw is not None and gw.numel() != nx * ny * nz):
+        raise ValueError("grad_f / grad_w must hold one value per voxel")
+    if vol0 is not None:
+        if vol0.dtype != torch.float32 or tuple(vol0.shape) != (nz, ny, nx, 2) or not vol0.is_contiguous():
+            raise ValueError("vol0 must be a contiguous float32 (nz, ny, nx, 2) tensor")
+    nrm = normals.to(torch.float32).contiguous() if normals is not None else None
+    gf0 = torch.empty((nz, ny, nx), dtype=torch.float32, device=dev) if want_grad_vol0 else None
+    gw0 = torch.empty((nz, ny, nx), dtype=torch.float32, device=dev) if want_grad_vol0 else None
+    ctx.check(_lib.mcg_integrate_backward(ctx.handle, _ptr(vol0), nx, ny, nz, min_t, max_t, grid_s, ctypes.byref(k),
+                                          nf, _ptr(pt), w, h, _ptr(depth), _ptr(nrm), 1 if is_dynamic else 0,
+                                          _ptr(gf), _ptr(gw), _ptr(grad_depth), _ptr(gf0), _ptr(gw0),
+                                          _stream(stream)),
+              "mcg_integrate_backward")
+    return grad_depth, gf0, gw0
+
+
+class MarchingCubesFunction(torch.autograd.Function):
+    """volume (nz, ny, nx, 2) float32 -> soup positions (n, 3); the gradient
+    flows into the tsdf channel (the weight channel only selects cubes)."""
+
+    @staticmethod
+    def forward(fctx, volume, cell):
+        mesh = extract(volume, cell, soup=True, normals=False)
+        pos = mesh.positions.contiguous() if mesh.num_vertices else torch.zeros(
+            (0, 3), dtype=torch.float32, device=volume.device)
+        fctx.save_for_backward(volume)
+        fctx.cell = float(cell)
+        return pos
+
+    @staticmethod
+    def backward(fctx, grad_pos):
+        (volume,) = fctx.saved_tensors
+        if not fctx.needs_input_grad[0]:
+            return None, None
+        gv = torch.zeros_like(volume)
+        if grad_pos.shape[0]:
+            gf = mc_backward(volume, fctx.cell, grad_pos)
+            gv[..., 0] = gf
+        return gv, None
+
+
+def mesh_positions(volume, cell):
+    """Differentiable soup positions of a float32 volume."""
+    if volume.dtype != torch.float32:
+        raise TypeError("the differentiable path takes float32 (float2) volumes")
+    return MarchingCubesFunction.apply(volume, cell)
+
+
+class IntegrateFunction(torch.autograd.Function):
+    """depth frames (K, h, w) [+ initial volume] -> float32 volume
+    (nz, ny, nx, 2) after integrating every frame in order."""
+
+    @staticmethod
+    def forward(fctx, depth, vol0, poses, shape, min_t, max_t, grid_s, k, normals, is_dynamic):
+        nz, ny, nx = shape
+        dev = depth.device
+        depth_c = depth.to(torch.float32).contiguous()
+        pt = _poses_tensor(poses, dev)
+        if vol0 is not None:
+            vol = vol0.detach().clone()
+        else:
+            vol = torch.empty((nz, ny, nx, 2), dtype=torch.float32, device=dev)
+            voxel_init(vol)
+        v = Voxel(vol, min_t, max_t, grid_s)
+        nrm = normals.to(torch.float32).contiguous() if normals is not None else None
+        for f in range(depth_c.shape[0]):
+            volumetric_integration_device_pose(v, k, pt[f], depth_c[f], None if nrm is None else nrm[f],
+                                               is_dynamic)
+        fctx.save_for_backward(depth_c, pt, vol0 if vol0 is not None else None, nrm)
+        fctx.params = (tuple(shape), min_t, max_t, grid_s, k, is_dynamic)
+        return vol
+
+    @staticmethod
+    def backward(fctx, grad_vol):
+        depth, pt, vol0, nrm = fctx.saved_tensors
+        shape, min_t, max_t, grid_s, k, is_dynamic = fctx.params
+        grad_vol = grad_vol.contiguous()
+        want0 = vol0 is not None and fctx.needs_input_grad[1]
+        gd, gf0, gw0 = integrate_backward(shape, min_t, max_t, grid_s, k, pt, depth, grad_vol[..., 0], grad_vol[..., 1],
+                                          vol0=vol0.detach().contiguous() if vol0 is not None else None,
+                                          normals=nrm, is_dynamic=is_dynamic, want_grad_vol0=want0)
+        g0 = torch.stack([gf0, gw0], dim=-1) if want0 else None
+        return (gd if fctx.needs_input_grad[0] else None), g0, None, None, None, None, None, None, None, None
+
+
+def integrate_frames(depth, poses, shape, min_t, max_t, grid_s, k, vol0=None, normals=None, is_dynamic=False):
+    """Differentiable fusion of depth frames (K, h, w metres, z-depth) with
+    camera -> global poses (K, 12 device tensor, or a list of (R, t)) into a
+    float32 volume (nz, ny, nx, 2), starting from vol0 or the initial state."""
+    return IntegrateFunction.apply(depth, vol0, poses, tuple(shape), float(min_t), float(max_t), float(grid_s), k,
+                                   normals, bool(is_dynamic))
 
 
 # ---------------------------------------------------------------------------

@@ -60,6 +60,7 @@ SIGNATURES = {
                                        c_void_p]),
     "mcg_mc_extract_noalloc": (c_int, [ctypes.POINTER(Volume), ctypes.POINTER(MeshOut),
                                        ctypes.POINTER(MeshCounts), c_void_p]),
+    "mcg_mc_backward": (c_int, [c_void_p, ctypes.POINTER(Volume), c_void_p, c_int64, c_void_p, c_void_p]),
     "mcg_mc_normals": (c_int, [c_void_p, ctypes.POINTER(Volume), c_void_p, c_int64, c_void_p, c_void_p]),
     "mcg_depth_to_maps": (c_int, [c_void_p, ctypes.POINTER(Intrinsic), c_int32, c_int32, c_void_p,
                                   c_float, c_float, c_void_p, c_void_p, c_void_p, c_void_p]),
@@ -69,6 +70,10 @@ SIGNATURES = {
     "mcg_integrate": (c_int, [c_void_p, c_void_p, c_int32, c_int32, c_int32, c_int32, c_float, c_float,
                               c_float, ctypes.POINTER(Intrinsic), ctypes.POINTER(Extrinsic), c_int32,
                               c_int32, c_void_p, c_void_p, c_int32, c_void_p]),
+    "mcg_integrate_backward": (c_int, [c_void_p, c_void_p, c_int32, c_int32, c_int32, c_float, c_float, c_float,
+                                       ctypes.POINTER(Intrinsic), c_int32, c_void_p, c_int32, c_int32, c_void_p,
+                                       c_void_p, c_int32, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                       c_void_p]),
     "mcg_integrate_device_pose": (c_int, [c_void_p, c_void_p, c_int32, c_int32, c_int32, c_int32, c_float, c_float,
                                           c_float, ctypes.POINTER(Intrinsic), c_void_p, c_int32, c_int32, c_void_p,
                                           c_void_p, c_int32, c_void_p]),

@@ -181,54 +181,93 @@ __device__ __forceinline__ unsigned short pack_weight(float w) {
 }
 __device__ __forceinline__ float unpack_weight(unsigned short w) { return (float)w / (float)kMaxW * kUbW; }
 
+// One observation of a voxel: truncated sdf, weight before the dynamic term,
+// ray-length depth at the pixel, ds/dz (0 where the sdf is clamped at 1),
+// the pixel's ray scale and the pixel index.
+struct Obs {
+    float s, w0, z, dsdz, c;
+    long long pix;
+};
+
 // Per-voxel part of :442-529 up to the update.  Returns false when the voxel
-// is not updated; otherwise the new observation (sdf, weight before the
-// dynamic term).
-__device__ __forceinline__ bool observe(const IntegParams &p, float px, float py, float pz,
-                                        float &sdf, float &weight) {
+// is not updated.  zat(u, v, pix, c) gives the ray-length depth at the pixel
+// (and its ray scale c).
+template <class ZAt>
+__device__ __forceinline__ bool observe_core(const float *r, const float *t, const Intr &k, int w, int h,
+                                             float min_t, float max_t, const float3 *normals, ZAt zat,
+                                             float px, float py, float pz, Obs &o) {
     // float_camera_extrinsic_backward (cu_geometry_functions.h:125-129), matrix33_tv
-    const float v0 = px - p.t[0], v1 = py - p.t[1], v2 = pz - p.t[2];
-    const float q0 = p.r[0] * v0 + p.r[1] * v1 + p.r[2] * v2;
-    const float q1 = p.r[3] * v0 + p.r[4] * v1 + p.r[5] * v2;
-    const float q2 = p.r[6] * v0 + p.r[7] * v1 + p.r[8] * v2;
+    const float v0 = px - t[0], v1 = py - t[1], v2 = pz - t[2];
+    const float q0 = r[0] * v0 + r[1] * v1 + r[2] * v2;
+    const float q1 = r[3] * v0 + r[4] * v1 + r[5] * v2;
+    const float q2 = r[6] * v0 + r[7] * v1 + r[8] * v2;
     if (q2 < FLT_MIN) return false;
     // float_camera_intrinsic_project_3 (cu_geometry_functions.h:232-235)
-    const float uf = p.k.fx * (q0 / q2) + p.k.cx;
-    const float vf = p.k.fy * (q1 / q2) + p.k.cy;
+    const float uf = k.fx * (q0 / q2) + k.cx;
+    const float vf = k.fy * (q1 / q2) + k.cy;
     const int u = __float2int_rn(uf), v = __float2int_rn(vf);
-    if (u < 0 || v < 0 || u >= (p.w - 2) || v >= (p.h - 2)) return false;
-    const long long pix = (long long)v * p.w + u;
-    const float z_val = p.ds[pix];
+    if (u < 0 || v < 0 || u >= (w - 2) || v >= (h - 2)) return false;
+    const long long pix = (long long)v * w + u;
+    float c = 1.0f;
+    const float z_val = zat(u, v, pix, c);
     if (!(z_val > FLT_MIN)) return false;
     const float qn = sqrtf(q0 * q0 + q1 * q1 + q2 * q2);
     float s = z_val - qn;
-    if (!(s >= -p.min_t)) return false;
+    if (!(s >= -min_t)) return false;
+    float dsdz;
     if (s > 0.0f) {
-        s = s / p.max_t;
-        if (s > 1.0f) s = 1.0f;
+        s = s / max_t;
+        dsdz = 1.0f / max_t;
+        if (s > 1.0f) {
+            s = 1.0f;
+            dsdz = 0.0f;
+        }
     } else {
-        s = s / p.min_t;
+        s = s / min_t;
+        dsdz = 1.0f / min_t;
     }
     float wgt = 1.0f;
-    if (p.normals) {
-        const float3 n = p.normals[pix];
+    if (normals) {
+        const float3 n = normals[pix];
         if (!vvalid(n)) return false;
         wgt = -(n.x * (q0 / qn) + n.y * (q1 / qn) + n.z * (q2 / qn));
         if (wgt < FLT_MIN) return false;
     }
-    weight = wgt / z_val;
-    sdf = s;
+    o.w0 = wgt / z_val;
+    o.s = s;
+    o.z = z_val;
+    o.dsdz = dsdz;
+    o.c = c;
+    o.pix = pix;
     return true;
 }
 
-__device__ __forceinline__ void fuse(const IntegParams &p, float sdf, float weight, float sdf1,
-                                     float w1, float &sdf2, float &w2) {
-    if (p.is_dynamic) {
+__device__ __forceinline__ bool observe(const IntegParams &p, float px, float py, float pz,
+                                        float &sdf, float &weight) {
+    Obs o;
+    const float *ds = p.ds;
+    if (!observe_core(p.r, p.t, p.k, p.w, p.h, p.min_t, p.max_t, p.normals,
+                      [ds](int, int, long long pix, float &) { return ds[pix]; }, px, py, pz, o))
+        return false;
+    sdf = o.s;
+    weight = o.w0;
+    return true;
+}
+
+// :509-529 weighted running average (FP32 path)
+__device__ __forceinline__ void fuse_core(int is_dynamic, float sdf, float weight, float sdf1, float w1,
+                                          float &sdf2, float &w2) {
+    if (is_dynamic) {
         const float d = fabsf(sdf - sdf1);
         weight = weight * (1.0f + d * d * 10.0f);
     }
     w2 = w1 + weight;
     sdf2 = (w1 * sdf1 + weight * sdf) / w2;
+}
+
+__device__ __forceinline__ void fuse(const IntegParams &p, float sdf, float weight, float sdf1,
+                                     float w1, float &sdf2, float &w2) {
+    fuse_core(p.is_dynamic, sdf, weight, sdf1, w1, sdf2, w2);
 }
 
 // short2 volume, 4 voxels per thread; vec = 16-byte path usable
@@ -335,6 +374,127 @@ __global__ void __launch_bounds__(256) integrate_float2_kernel(IntegParams p, fl
     }
 }
 
+// ---- integrate adjoint ----------------------------------------------------------
+// Reverse of a sequence of float2 integrate steps (no counterpart in the
+// reference).  Per voxel, step k (observation s, weight w) maps
+//   W' = W + w,  F' = (W F + w s) / W'
+// so, holding the discrete choices (pixel, truncation, clamp) fixed,
+//   dF'/dF = W/W',  dF'/dW = (F - F')/W',  dF'/ds = w/W',  dF'/dw = (s - F')/W'
+// and s = (c d - |q|)/m (m = max_t or min_t, ds/dz = 0 where clamped),
+// w = wgt / (c d) (dw/dd = -w c / z) with d the pixel's z-depth and c its
+// ray scale.  The dynamic term multiplies w by 1 + 10 (s - F)^2.  Normal maps
+// are held constant.
+constexpr int BW_SEG = 16;                    // frames whose (F, W) one thread keeps while reversing
+constexpr int BW_MAX_FRAMES = BW_SEG * 32;    // frames per call (checkpoint every BW_SEG)
+
+struct IntegBwParams {
+    int nx, ny, nz;
+    float min_t, max_t, grid_s;
+    Intr k;
+    int w, h, n_frames;
+    const float *poses;    // n_frames x (r[9] column-major, t[3])
+    const float *depth;    // n_frames x h x w metres (z-depth)
+    const float3 *normals; // n_frames x h x w, or null
+    const float *ray_x;
+    int is_dynamic;
+    const float2 *vol0;    // volume before the first frame, or null: (-1, 0)
+    const float *grad_f;   // dL/dF after the last frame
+    const float *grad_w;   // dL/dW after the last frame, or null: 0
+    float *grad_depth;     // n_frames x h x w, accumulated
+    float *grad_f0;        // dL/dF before the first frame, or null
+    float *grad_w0;
+};
+
+__device__ __forceinline__ bool bw_observe(const IntegBwParams &p, const float *pose, int f, float px,
+                                           float py, float pz, Obs &o) {
+    const long long plane = (long long)p.w * p.h;
+    const float *dep = p.depth + f * plane;
+    const Intr k = p.k;
+    return observe_core(pose, pose + 9, k, p.w, p.h, p.min_t, p.max_t, p.normals ? p.normals + f * plane : nullptr,
+                        [dep, k](int u, int v, long long pix, float &c) {
+                            // d_voxel_volumetric_depth_scaling (:416-425) for one pixel
+                            const float cx = ((float)u - k.cx) / k.fx;
+                            const float cy = ((float)v - k.cy) / k.fy;
+                            c = sqrtf(cx * cx + cy * cy + 1.0f);
+                            return dep[pix] * c;
+                        },
+                        px, py, pz, o);
+}
+
+__global__ void __launch_bounds__(128) integrate_backward_kernel(IntegBwParams p) {
+    extern __shared__ float s_pose[];
+    for (int i = threadIdx.x; i < p.n_frames * 12; i += blockDim.x) s_pose[i] = p.poses[i];
+    __syncthreads();
+    const long long n = (long long)p.nx * p.ny * p.nz;
+    const int nseg = (p.n_frames + BW_SEG - 1) / BW_SEG;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        float gF = p.grad_f[i];
+        float gW = p.grad_w ? p.grad_w[i] : 0.0f;
+        if (gF != 0.0f || gW != 0.0f) {
+            const int x = (int)(i % p.nx);
+            const long long row = i / p.nx;
+            const int y = (int)(row % p.ny), z = (int)(row / p.ny);
+            const float px = p.ray_x[x], py = (float)y * p.grid_s, pz = (float)z * p.grid_s;
+            float F = p.vol0 ? p.vol0[i].x : -1.0f;
+            float W = p.vol0 ? p.vol0[i].y : 0.0f;
+            // forward sweep: (F, W) at the start of every segment
+            float ckF[BW_MAX_FRAMES / BW_SEG], ckW[BW_MAX_FRAMES / BW_SEG];
+            for (int f = 0; f < p.n_frames; ++f) {
+                if (f % BW_SEG == 0) {
+                    ckF[f / BW_SEG] = F;
+                    ckW[f / BW_SEG] = W;
+                }
+                Obs o;
+                if (bw_observe(p, s_pose + 12 * f, f, px, py, pz, o)) fuse_core(p.is_dynamic, o.s, o.w0, F, W, F, W);
+            }
+            for (int sg = nseg - 1; sg >= 0; --sg) {
+                const int f0 = sg * BW_SEG;
+                const int f1 = min(p.n_frames, f0 + BW_SEG);
+                float sF[BW_SEG], sW[BW_SEG];
+                float cF = ckF[sg], cW = ckW[sg];
+                for (int f = f0; f < f1; ++f) {
+                    sF[f - f0] = cF;
+                    sW[f - f0] = cW;
+                    Obs o;
+                    if (bw_observe(p, s_pose + 12 * f, f, px, py, pz, o))
+                        fuse_core(p.is_dynamic, o.s, o.w0, cF, cW, cF, cW);
+                }
+                for (int f = f1 - 1; f >= f0; --f) {
+                    Obs o;
+                    if (!bw_observe(p, s_pose + 12 * f, f, px, py, pz, o)) continue;
+                    const float Fp = sF[f - f0], Wp = sW[f - f0];
+                    float wv = o.w0, mult = 1.0f, d = 0.0f;
+                    if (p.is_dynamic) {
+                        d = o.s - Fp;
+                        mult = 1.0f + d * d * 10.0f;
+                        wv = wv * mult;
+                    }
+                    const float Wn = Wp + wv;
+                    const float Fn = (Wp * Fp + wv * o.s) / Wn;
+                    float gs = gF * wv / Wn;
+                    const float gw = gF * (o.s - Fn) / Wn + gW;
+                    float gFp = gF * Wp / Wn;
+                    const float gWp = gF * (Fp - Fn) / Wn + gW;
+                    float gw0 = gw;
+                    if (p.is_dynamic) {
+                        const float t = gw * o.w0 * 20.0f * d;
+                        gs += t;
+                        gFp -= t;
+                        gw0 = gw * mult;
+                    }
+                    const float gz = gs * o.dsdz - gw0 * o.w0 / o.z;
+                    atomicAdd(p.grad_depth + f * (long long)p.w * p.h + o.pix, gz * o.c);
+                    gF = gFp;
+                    gW = gWp;
+                }
+            }
+        }
+        if (p.grad_f0) p.grad_f0[i] = gF;
+        if (p.grad_w0) p.grad_w0[i] = gW;
+    }
+}
+
 Intr intr_of(const mcg_intrinsic *k) { return Intr{k->fx, k->fy, k->cx, k->cy}; }
 
 }  // namespace
@@ -421,21 +581,9 @@ mcg_status mcg_vertex_to_normal(mcg_context *ctx, int32_t w, int32_t h, const fl
     return e == cudaSuccess ? MCG_OK : mcg_cuda_fail(ctx, e);
 }
 
-static mcg_status integrate_impl(mcg_context *ctx, void *vol, int32_t voxel_type, int32_t nx, int32_t ny,
-                                 int32_t nz, float min_t, float max_t, float grid_s, const mcg_intrinsic *k,
-                                 const mcg_extrinsic *ext, const float *pose_dev, int32_t w, int32_t h,
-                                 const float *depth_m, const float *normals, int32_t is_dynamic,
-                                 mcg_stream_t stream) {
-    if (!ctx || !vol || !k || (!ext && !pose_dev) || !depth_m || nx <= 0 || ny <= 0 || nz <= 0 || w <= 0 || h <= 0)
-        return MCG_ERR_INVALID_ARG;
-    if (voxel_type != MCG_VOXEL_SHORT2 && voxel_type != MCG_VOXEL_FLOAT2) return MCG_ERR_INVALID_ARG;
-    if (!(min_t > 0.0f) || !(max_t > 0.0f) || !(grid_s > 0.0f)) return MCG_ERR_INVALID_ARG;
-    cudaStream_t s = (cudaStream_t)stream;
-    cudaError_t e = cudaSetDevice(ctx->device);
-    if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
-    if (!ensure(&ctx->depth_scaled, &ctx->depth_scaled_cap, (size_t)w * h))
-        return mcg_cuda_fail(ctx, cudaErrorMemoryAllocation);
-    // x coordinate table, accumulated exactly as :434/:444 do
+// x coordinate table, accumulated exactly as :434/:444 do
+static mcg_status ensure_ray_x(mcg_context *ctx, int32_t nx, float grid_s, cudaStream_t s) {
+    cudaError_t e;
     if (ctx->ray_x_n != nx || ctx->ray_x_g != grid_s || !ctx->ray_x) {
         if (!ensure(&ctx->ray_x, &ctx->ray_x_cap, (size_t)nx)) return mcg_cuda_fail(ctx, cudaErrorMemoryAllocation);
         if (ctx->h_ray_x_cap < (size_t)nx) {
@@ -458,6 +606,27 @@ static mcg_status integrate_impl(mcg_context *ctx, void *vol, int32_t voxel_type
         if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
         ctx->ray_x_n = nx;
         ctx->ray_x_g = grid_s;
+    }
+    return MCG_OK;
+}
+
+static mcg_status integrate_impl(mcg_context *ctx, void *vol, int32_t voxel_type, int32_t nx, int32_t ny,
+                                 int32_t nz, float min_t, float max_t, float grid_s, const mcg_intrinsic *k,
+                                 const mcg_extrinsic *ext, const float *pose_dev, int32_t w, int32_t h,
+                                 const float *depth_m, const float *normals, int32_t is_dynamic,
+                                 mcg_stream_t stream) {
+    if (!ctx || !vol || !k || (!ext && !pose_dev) || !depth_m || nx <= 0 || ny <= 0 || nz <= 0 || w <= 0 || h <= 0)
+        return MCG_ERR_INVALID_ARG;
+    if (voxel_type != MCG_VOXEL_SHORT2 && voxel_type != MCG_VOXEL_FLOAT2) return MCG_ERR_INVALID_ARG;
+    if (!(min_t > 0.0f) || !(max_t > 0.0f) || !(grid_s > 0.0f)) return MCG_ERR_INVALID_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
+    if (!ensure(&ctx->depth_scaled, &ctx->depth_scaled_cap, (size_t)w * h))
+        return mcg_cuda_fail(ctx, cudaErrorMemoryAllocation);
+    {
+        const mcg_status st = ensure_ray_x(ctx, nx, grid_s, s);
+        if (st != MCG_OK) return st;
     }
     IntegParams p;
     p.nx = nx; p.ny = ny; p.nz = nz;
@@ -504,6 +673,48 @@ mcg_status mcg_integrate_device_pose(mcg_context *ctx, void *vol, int32_t voxel_
     if (!pose_dev) return MCG_ERR_INVALID_ARG;
     return integrate_impl(ctx, vol, voxel_type, nx, ny, nz, min_t, max_t, grid_s, k, nullptr, pose_dev, w, h,
                           depth_m, normals, is_dynamic, stream);
+}
+
+
+mcg_status mcg_integrate_backward(mcg_context *ctx, const void *vol0, int32_t nx, int32_t ny, int32_t nz,
+                                  float min_t, float max_t, float grid_s, const mcg_intrinsic *k, int32_t n_frames,
+                                  const float *poses_dev, int32_t w, int32_t h, const float *depth_m,
+                                  const float *normals, int32_t is_dynamic, const float *grad_f,
+                                  const float *grad_w, float *grad_depth, float *grad_f0, float *grad_w0,
+                                  mcg_stream_t stream) {
+    if (!ctx || !k || !poses_dev || !depth_m || !grad_f || !grad_depth || nx <= 0 || ny <= 0 || nz <= 0 ||
+        w <= 0 || h <= 0 || n_frames <= 0)
+        return MCG_ERR_INVALID_ARG;
+    if (!(min_t > 0.0f) || !(max_t > 0.0f) || !(grid_s > 0.0f)) return MCG_ERR_INVALID_ARG;
+    if (n_frames > BW_MAX_FRAMES) return MCG_ERR_TOO_LARGE;
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
+    const mcg_status st = ensure_ray_x(ctx, nx, grid_s, s);
+    if (st != MCG_OK) return st;
+    IntegBwParams p;
+    p.nx = nx; p.ny = ny; p.nz = nz;
+    p.min_t = min_t; p.max_t = max_t; p.grid_s = grid_s;
+    p.k = intr_of(k);
+    p.w = w; p.h = h; p.n_frames = n_frames;
+    p.poses = poses_dev;
+    p.depth = depth_m;
+    p.normals = (const float3 *)normals;
+    p.ray_x = ctx->ray_x;
+    p.is_dynamic = is_dynamic ? 1 : 0;
+    p.vol0 = (const float2 *)vol0;
+    p.grad_f = grad_f;
+    p.grad_w = grad_w;
+    p.grad_depth = grad_depth;
+    p.grad_f0 = grad_f0;
+    p.grad_w0 = grad_w0;
+    const long long n = (long long)nx * ny * nz;
+    long long grid = (n + 127) / 128;
+    const long long cap = (long long)ctx->num_sms * 16;
+    if (grid > cap) grid = cap;
+    integrate_backward_kernel<<<(unsigned int)grid, 128, sizeof(float) * 12 * n_frames, s>>>(p);
+    e = cudaGetLastError();
+    return e == cudaSuccess ? MCG_OK : mcg_cuda_fail(ctx, e);
 }
 
 }  // extern "C"

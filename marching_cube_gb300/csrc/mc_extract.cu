@@ -513,6 +513,10 @@ struct GenParams {
     int16_t *ver_voxel;
     int64_t *tri_cube;
     long long cap;
+    // adjoint (MODE 1): dL/dP per soup vertex in, dL/df per voxel accumulated
+    const float *grad_pos;
+    float *grad_f;
+    long long n_grad;
 };
 
 template <int VT>
@@ -550,16 +554,14 @@ struct GenOut {
 // All per-brick work of pass 2 once the brick's tile is in shared memory:
 // occupied-cube list with vertex offsets, then one soup vertex per thread.
 // Called by every thread of the CTA (contains __syncthreads).
+// Occupied-cube list of a brick whose tile is in shared memory: S.occ_cube /
+// occ_ci / occ_off in (z, y, x) order, S.nocc entries, S.total soup
+// vertices, and S.vmap when the brick has at most 2048 of them.  Called by
+// every thread (contains __syncthreads); the list is valid after return.
 template <int VT>
-__device__ __forceinline__ void generate_brick(GenSmem<VT> &S, const typename Vox<VT>::T *tile,
-                                               const typename Vox<VT>::T *__restrict__ vol, int nx, int ny,
-                                               int nz, float cell, int x0, int y0, int z0,
-                                               unsigned long long vbase, const GenOut &o) {
-    using V = Vox<VT>;
-    using T = typename V::T;
+__device__ __forceinline__ void occupied_list(GenSmem<VT> &S, const typename Vox<VT>::T *tile, int nx, int ny, int nz,
+                                              int x0, int y0, int z0) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const long long N = (long long)nx * ny * nz;
-
         // occupied cubes of the brick, from row masks (voxel rows y0..y0+8, z0..z0+8)
         if (tid < ROWS) {
             const int ry = tid % (BY + 1), rz = tid / (BY + 1);
@@ -616,6 +618,19 @@ __device__ __forceinline__ void generate_brick(GenSmem<VT> &S, const typename Vo
             }
         }
         __syncthreads();
+}
+
+template <int VT>
+__device__ __forceinline__ void generate_brick(GenSmem<VT> &S, const typename Vox<VT>::T *tile,
+                                               const typename Vox<VT>::T *__restrict__ vol, int nx, int ny,
+                                               int nz, float cell, int x0, int y0, int z0,
+                                               unsigned long long vbase, const GenOut &o) {
+    using V = Vox<VT>;
+    using T = typename V::T;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const long long N = (long long)nx * ny * nz;
+
+        occupied_list<VT>(S, tile, nx, ny, nz, x0, y0, z0);
         const unsigned int nocc = S.nocc, T_brick = S.total;
         const bool use_map = T_brick <= BRICK_CUBES;
 
@@ -767,7 +782,64 @@ __device__ __forceinline__ void generate_brick(GenSmem<VT> &S, const typename Vo
         }
 }
 
-template <int VT, bool TMA>
+// Adjoint of the soup positions with respect to the voxel values, for one
+// brick whose tile is in shared memory.  Soup vertex v of the brick lies on
+// edge (a, b) of its cube: P = p_a + t (p_b - p_a), t = -f_a / D,
+// D = f_b - f_a + 1e-15 (cu_marching_cubes_v1.cu:256-264), so
+//   dL/df_a += (dL/dP . (p_b - p_a)) * -(f_b + 1e-15) / D^2
+//   dL/df_b += (dL/dP . (p_b - p_a)) *  f_a / D^2
+// accumulated in FP32 with atomics (a voxel is shared by up to 6 edges).
+// Called by every thread (contains __syncthreads).
+template <int VT>
+__device__ __forceinline__ void backward_brick(GenSmem<VT> &S, const typename Vox<VT>::T *tile, int nx, int ny,
+                                               int nz, float cell, int x0, int y0, int z0, unsigned long long vbase,
+                                               const float *__restrict__ grad_pos, float *__restrict__ grad_f,
+                                               long long n_grad) {
+    using V = Vox<VT>;
+    const int tid = threadIdx.x;
+    occupied_list<VT>(S, tile, nx, ny, nz, x0, y0, z0);
+    const unsigned int nocc = S.nocc, T_brick = S.total;
+    const bool use_map = T_brick <= BRICK_CUBES;
+    for (unsigned int v = tid; v < T_brick; v += THREADS) {
+        const unsigned long long gv = vbase + v;
+        if ((long long)gv >= n_grad) break;
+        int lo = 0;
+        if (use_map) {
+            lo = S.vmap[v];
+        } else {
+            int hi = (int)nocc - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (S.occ_off[mid] <= v) lo = mid; else hi = mid - 1;
+            }
+        }
+        const int c = S.occ_cube[lo];
+        const int lcx = c & (BX - 1), lcy = (c / BX) & (BY - 1), lcz = c / (BX * BY);
+        const unsigned int ci = S.occ_ci[lo];
+        const unsigned int sl = v - S.occ_off[lo];
+        const unsigned int j = sl / 3, k = sl - 3 * j;
+        const int e = S.tri[ci][3 * j + 2 - k];
+        const int a = c_ea(e), bb = c_eb(e);
+        const float f0 = V::f(tile[tidx(lcx + TXO + c_cx(a), lcy + TYO + c_cy(a), lcz + TZO + c_cz(a))]);
+        const float f1 = V::f(tile[tidx(lcx + TXO + c_cx(bb), lcy + TYO + c_cy(bb), lcz + TZO + c_cz(bb))]);
+        const int gx = x0 + lcx, gy = y0 + lcy, gz = z0 + lcz;
+        const int ga[3] = {gx + c_cx(a), gy + c_cy(a), gz + c_cz(a)};
+        const int gb[3] = {gx + c_cx(bb), gy + c_cy(bb), gz + c_cz(bb)};
+        float g = 0.0f;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const float p0 = ((float)ga[d] + 0.5f) * cell;
+            const float p1 = ((float)gb[d] + 0.5f) * cell;
+            g += grad_pos[3 * gv + d] * (p1 - p0);
+        }
+        const float D = f1 - f0 + 1e-15f;
+        const float inv = 1.0f / (D * D);
+        atomicAdd(&grad_f[lin3(nx, ny, ga[0], ga[1], ga[2])], g * (-(f1 + 1e-15f) * inv));
+        atomicAdd(&grad_f[lin3(nx, ny, gb[0], gb[1], gb[2])], g * (f0 * inv));
+    }
+}
+
+template <int VT, bool TMA, int MODE>
 __global__ void __launch_bounds__(THREADS, 4) mc_generate_kernel(const __grid_constant__ CUtensorMap map, GenParams p) {
     using V = Vox<VT>;
     using T = typename V::T;
@@ -822,14 +894,19 @@ __global__ void __launch_bounds__(THREADS, 4) mc_generate_kernel(const __grid_co
             __syncthreads();
         }
         const BrickPos bp = brick_pos(b, p.nbx, p.nby);
-        GenOut o;
-        o.soup = p.soup;
-        o.normals = p.normals;
-        o.vi2vox = p.vi2vox;
-        o.ver_voxel = p.ver_voxel;
-        o.tri_cube = p.tri_cube;
-        o.cap = p.cap;
-        generate_brick<VT>(S, tile, vol, nx, ny, nz, cell, bp.x0, bp.y0, bp.z0, vbase, o);
+        if (MODE == 0) {
+            GenOut o;
+            o.soup = p.soup;
+            o.normals = p.normals;
+            o.vi2vox = p.vi2vox;
+            o.ver_voxel = p.ver_voxel;
+            o.tri_cube = p.tri_cube;
+            o.cap = p.cap;
+            generate_brick<VT>(S, tile, vol, nx, ny, nz, cell, bp.x0, bp.y0, bp.z0, vbase, o);
+        } else {
+            backward_brick<VT>(S, tile, nx, ny, nz, cell, bp.x0, bp.y0, bp.z0, vbase, p.grad_pos, p.grad_f,
+                               p.n_grad);
+        }
         __syncthreads();  // tile s, the list and the stage are free again
         if (TMA && tid == 0) {
             const unsigned int wn = w + GSTAGES * gridDim.x;
@@ -1165,14 +1242,14 @@ void launch_classify_t(const CUtensorMap &map, const mcg_volume *vol, const Geom
     else launch_classify_s<VT, TMA, 2>(map, vol, g, sc, sms, s);
 }
 
-template <int VT, bool TMA>
+template <int VT, bool TMA, int MODE = 0>
 void launch_generate_t(const CUtensorMap &map, const GenParams &p, const Geometry &g, int sms, cudaStream_t s) {
     const size_t smem = sizeof(GenSmem<VT>);
     static int occ = 0;
-    if (!occ) occ = occupancy(mc_generate_kernel<VT, TMA>, THREADS, smem);
+    if (!occ) occ = occupancy(mc_generate_kernel<VT, TMA, MODE>, THREADS, smem);
     long long grid = (long long)sms * occ;
     if (grid > g.nbricks) grid = g.nbricks;
-    mc_generate_kernel<VT, TMA><<<(int)grid, THREADS, smem, s>>>(map, p);
+    mc_generate_kernel<VT, TMA, MODE><<<(int)grid, THREADS, smem, s>>>(map, p);
 }
 
 // classify + scan into sc; clears the timeout flag first
@@ -1221,6 +1298,9 @@ cudaError_t launch_generate_phase(const mcg_volume *vol, const Geometry &g, cons
     p.ver_voxel = out->ver_voxel;
     p.tri_cube = out->tri_cube;
     p.cap = out->capacity_vertices;
+    p.grad_pos = nullptr;
+    p.grad_f = nullptr;
+    p.n_grad = 0;
     CUtensorMap map;
     const int eb = vol->voxel_type == MCG_VOXEL_SHORT2 ? 4 : 8;
     const bool tma = encode_volume_map(&map, vol->data, vol->nx, vol->ny, vol->nz, eb, TX, TY, TZ);
@@ -1339,6 +1419,49 @@ mcg_status mcg_mc_normals(mcg_context *ctx, const mcg_volume *vol, const mcg_ver
     return e == cudaSuccess ? MCG_OK : mcg_cuda_fail(ctx, e);
 }
 
+
+
+mcg_status mcg_mc_backward(mcg_context *ctx, const mcg_volume *vol, const float *grad_pos, int64_t n_vertices,
+                           float *grad_f, mcg_stream_t stream) {
+    if (!ctx || !vol_ok(vol) || n_vertices < 0 || !grad_f || (n_vertices > 0 && !grad_pos))
+        return MCG_ERR_INVALID_ARG;
+    if (!ctx->classified || ctx->cls_data != vol->data || ctx->cls_nx != vol->nx || ctx->cls_ny != vol->ny ||
+        ctx->cls_nz != vol->nz || ctx->cls_vtype != vol->voxel_type)
+        return MCG_ERR_STATE;
+    if (n_vertices == 0) return MCG_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
+    const Geometry g = geometry(vol->nx, vol->ny, vol->nz);
+    GenParams p;
+    memset(&p, 0, sizeof(p));
+    p.vol = vol->data;
+    p.nx = vol->nx;
+    p.ny = vol->ny;
+    p.nz = vol->nz;
+    p.cell = vol->cell;
+    p.nbx = g.nbx;
+    p.nby = g.nby;
+    p.active = ctx->active;
+    p.brick_vofs = ctx->brick_vofs;
+    p.totals = ctx->d_totals;
+    p.grad_pos = grad_pos;
+    p.grad_f = grad_f;
+    p.n_grad = n_vertices;
+    CUtensorMap map;
+    const int eb = vol->voxel_type == MCG_VOXEL_SHORT2 ? 4 : 8;
+    const bool tma = encode_volume_map(&map, vol->data, vol->nx, vol->ny, vol->nz, eb, TX, TY, TZ);
+    if (!tma) memset(&map, 0, sizeof(map));
+    if (vol->voxel_type == MCG_VOXEL_SHORT2) {
+        if (tma) launch_generate_t<MCG_VOXEL_SHORT2, true, 1>(map, p, g, ctx->num_sms, s);
+        else launch_generate_t<MCG_VOXEL_SHORT2, false, 1>(map, p, g, ctx->num_sms, s);
+    } else {
+        if (tma) launch_generate_t<MCG_VOXEL_FLOAT2, true, 1>(map, p, g, ctx->num_sms, s);
+        else launch_generate_t<MCG_VOXEL_FLOAT2, false, 1>(map, p, g, ctx->num_sms, s);
+    }
+    e = cudaGetLastError();
+    return e == cudaSuccess ? MCG_OK : mcg_cuda_fail(ctx, e);
+}
 
 // ---- batched extraction host side -------------------------------------------------
 namespace mcg {

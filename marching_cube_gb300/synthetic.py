@@ -11,6 +11,10 @@ sizes and value ranges of the workloads:
                   1.5 m (pinhole 525/525/319.5/239.5, 640x480), Gaussian
                   noise sigma 2 mm, uint16 millimetres
   random_volume   small random short2 volumes for exhaustive parity cases
+  blended_spheres smooth union (log-sum-exp, sharpness 32/m) of 8 spheres
+                  in a 1 m cube, float depth frames sphere-traced from a
+                  camera orbiting at 1.2 m (pinhole 262.5/262.5, 320x240),
+                  for the differentiable path
 
 Randomness: numpy.random.default_rng(seed) for scene parameters and
 torch.Generator(seed) for per-pixel noise.
@@ -89,6 +93,75 @@ def batch_volumes(n=64, seed=0, lo=32, hi=256, device="cpu", trunc=5.0):
 # ---------------------------------------------------------------------------
 # fusion scene
 # ---------------------------------------------------------------------------
+def orbit_pose(center, frame, n_frames, radius):
+    """camera -> global (R, t) of frame `frame` of an orbit looking at `center`
+    (camera x right, y down, z forward)."""
+    a = 2.0 * math.pi * frame / n_frames
+    elev = 0.25 * math.sin(2.0 * a)
+    eye = np.asarray(center, np.float64) + radius * np.array([math.cos(a) * math.cos(elev), math.sin(elev),
+                                                               math.sin(a) * math.cos(elev)])
+    fwd = center - eye
+    fwd /= np.linalg.norm(fwd)
+    up = np.array([0.0, 1.0, 0.0])
+    right = np.cross(up, fwd)
+    right /= np.linalg.norm(right)
+    down = np.cross(fwd, right)
+    R = np.stack([right, down, fwd], axis=1)  # columns: camera x, y, z in world
+    return R, eye
+
+
+class BlendedSpheres:
+    """Smooth union f(p) = -log(sum_i exp(-k d_i(p))) / k of n spheres inside
+    a cube of side `extent` metres; f is 1-Lipschitz, so sphere tracing on it
+    is safe."""
+
+    def __init__(self, seed=0, n_spheres=8, extent=1.0, sharpness=32.0):
+        rng = np.random.default_rng(seed)
+        c = extent / 2.0
+        self.extent = extent
+        self.center = np.array([c, c, c])
+        self.sph_c = c + rng.uniform(-0.18, 0.18, size=(n_spheres, 3)) * extent
+        self.sph_r = rng.uniform(0.07, 0.15, size=n_spheres) * extent
+        self.k = sharpness / extent
+
+    def sdf(self, p):
+        c = torch.as_tensor(self.sph_c, dtype=p.dtype, device=p.device)
+        r = torch.as_tensor(self.sph_r, dtype=p.dtype, device=p.device)
+        d = torch.linalg.norm(p[:, None, :] - c[None, :, :], dim=-1) - r[None, :]
+        return -torch.logsumexp(-self.k * d, dim=1) / self.k
+
+    def pose(self, frame, n_frames, radius=1.2):
+        return orbit_pose(self.center, frame, n_frames, radius * self.extent)
+
+    def depth_frame(self, R, t, w=320, h=240, fx=262.5, fy=262.5, cx=None, cy=None, steps=160, device="cpu"):
+        """Sphere-traced z-depth (h, w) float64 metres, 0 where the ray misses."""
+        cx = (w - 1) / 2.0 if cx is None else cx
+        cy = (h - 1) / 2.0 if cy is None else cy
+        dev = torch.device(device)
+        dt = torch.float64
+        v, u = torch.meshgrid(torch.arange(h, device=dev, dtype=dt), torch.arange(w, device=dev, dtype=dt),
+                              indexing="ij")
+        dc = torch.stack([(u - cx) / fx, (v - cy) / fy, torch.ones_like(u)], dim=-1).reshape(-1, 3)
+        n = torch.linalg.norm(dc, dim=1)
+        d = (dc / n[:, None]) @ torch.as_tensor(R, dtype=dt, device=dev).T
+        o = torch.as_tensor(t, dtype=dt, device=dev)
+        tr = torch.zeros(d.shape[0], dtype=dt, device=dev)
+        far = 3.0 * self.extent + float(np.linalg.norm(np.asarray(t) - self.center))
+        for _ in range(steps):
+            f = self.sdf(o[None, :] + tr[:, None] * d)
+            tr = torch.clamp(tr + f, max=far)
+        f = self.sdf(o[None, :] + tr[:, None] * d)
+        hit = (f.abs() < 1e-7) & (tr < far)
+        z = torch.where(hit, tr / n, torch.zeros_like(tr))
+        return z.reshape(h, w)
+
+    def frames(self, n_frames, w=320, h=240, fx=262.5, fy=262.5, device="cpu"):
+        """(depth (K, h, w) float64, [(R, t)] * K)."""
+        poses = [self.pose(i, n_frames) for i in range(n_frames)]
+        depth = torch.stack([self.depth_frame(R, t, w, h, fx, fy, device=device) for R, t in poses])
+        return depth, poses
+
+
 class FusionScene:
     """Spheres and boxes inside a cube of side `extent` metres (volume
     coordinates [0, extent)^3, voxel (x, y, z) at (x, y, z) * grid_s as the
@@ -107,18 +180,7 @@ class FusionScene:
 
     def pose(self, frame, n_frames, radius=1.5):
         """camera -> global (R, t) of frame `frame` of an orbit looking at the centre."""
-        a = 2.0 * math.pi * frame / n_frames
-        elev = 0.25 * math.sin(2.0 * a)
-        eye = self.center + radius * np.array([math.cos(a) * math.cos(elev), math.sin(elev),
-                                               math.sin(a) * math.cos(elev)])
-        fwd = self.center - eye
-        fwd /= np.linalg.norm(fwd)
-        up = np.array([0.0, 1.0, 0.0])
-        right = np.cross(up, fwd)
-        right /= np.linalg.norm(right)
-        down = np.cross(fwd, right)
-        R = np.stack([right, down, fwd], axis=1)  # columns: camera x, y, z in world
-        return R, eye
+        return orbit_pose(self.center, frame, n_frames, radius)
 
     def depth_frame(self, R, t, w=640, h=480, fx=525.0, fy=525.0, cx=319.5, cy=239.5,
                     noise_sigma=0.002, seed=0, device="cpu"):

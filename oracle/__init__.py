@@ -60,6 +60,12 @@ def lib():
             "orc_rle_encode_volume": (i64, [vp, i32, i32, i32, f32, f32, f32, i32, vp, i64]),
             "orc_rle_decode_volume": (i32, [vp, i64, vp, i64, vp, vp]),
             "orc_max_threads": (i32, []),
+            "orc_mc_edges": (i64, [vp, i32, i32, i32, i32, vp, vp, i64]),
+            "orc_mc_backward_f64": (i64, [vp, i32, i32, i32, i32, f64, vp, i64, vp]),
+            "orc_integrate_seq_f64": (None, [vp, i32, i32, i32, f32, f32, f32, vp, i32, vp, i32, i32, vp, vp, i32,
+                                             vp, vp, vp, i32]),
+            "orc_integrate_seq_backward_f64": (None, [vp, i32, i32, i32, f32, f32, f32, vp, i32, vp, i32, i32, vp, vp,
+                                                      i32, vp, vp, vp, vp, vp, i32]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -254,3 +260,91 @@ def rle_decode_volume(img: bytes):
     if r != 0:
         raise ValueError("malformed RLE volume (%d)" % r)
     return vol, tuple(float(p) for p in params)
+
+
+# ---------------------------------------------------------------------------
+# adjoints (binary64; discrete choices from the FP32 mirror, held fixed)
+# ---------------------------------------------------------------------------
+def mc_edges(vol):
+    """(va, vb): linear voxel indices of each soup vertex's edge corners,
+    canonical order."""
+    vol, vt, nx, ny, nz = _vol(vol)
+    _, ntri = mc_count(vol)
+    n = 3 * ntri
+    va = np.zeros(n, np.int64)
+    vb = np.zeros(n, np.int64)
+    lib().orc_mc_edges(_p(vol), vt, nx, ny, nz, _p(va), _p(vb), n)
+    return va, vb
+
+
+def mc_positions_f64(F, va, vb, shape, cell):
+    """Soup positions from per-voxel values F (any float array of nz*ny*nx)
+    on a fixed topology (va, vb)."""
+    nz, ny, nx = shape
+    F = np.asarray(F, np.float64).reshape(-1)
+
+    def xyz(li):
+        return np.stack([li % nx, (li // nx) % ny, li // (nx * ny)], axis=1).astype(np.float64)
+
+    pa = (xyz(va) + 0.5) * cell
+    pb = (xyz(vb) + 0.5) * cell
+    fa, fb = F[va], F[vb]
+    t = -fa / (fb - fa + 1e-15)
+    return pa + t[:, None] * (pb - pa)
+
+
+def mc_backward_f64(vol, cell, grad_pos):
+    """dL/df per voxel (nz, ny, nx) for dL/dP in canonical order."""
+    vol, vt, nx, ny, nz = _vol(vol)
+    g = np.ascontiguousarray(grad_pos, np.float64).reshape(-1, 3)
+    out = np.zeros((nz, ny, nx), np.float64)
+    lib().orc_mc_backward_f64(_p(vol), vt, nx, ny, nz, float(cell), _p(g), len(g), _p(out))
+    return out
+
+
+def _poses(poses):
+    arr = (Extrinsic * len(poses))()
+    for i, e in enumerate(poses):
+        arr[i] = e
+    return arr
+
+
+def integrate_seq_f64(shape, min_t, max_t, grid_s, k, poses, depth, vol0=None, normals=None, is_dynamic=False,
+                      nthreads=0):
+    """n_frames integrate steps in binary64 on a float2 volume of shape
+    (nz, ny, nx).  Returns (F, W, signature)."""
+    nz, ny, nx = shape
+    depth = np.ascontiguousarray(depth, np.float64)
+    nf, h, w = depth.shape
+    if vol0 is not None:
+        vol0 = np.ascontiguousarray(vol0, np.float32)
+    if normals is not None:
+        normals = np.ascontiguousarray(normals, np.float32)
+    F = np.zeros(shape, np.float64)
+    W = np.zeros(shape, np.float64)
+    sig = np.zeros(1, np.uint64)
+    lib().orc_integrate_seq_f64(_p(vol0), nx, ny, nz, min_t, max_t, grid_s, ctypes.byref(k), nf, _poses(poses),
+                                w, h, _p(depth), _p(normals), 1 if is_dynamic else 0, _p(F), _p(W), _p(sig),
+                                nthreads)
+    return F, W, int(sig[0])
+
+
+def integrate_seq_backward_f64(shape, min_t, max_t, grid_s, k, poses, depth, grad_f, grad_w=None, vol0=None,
+                               normals=None, is_dynamic=False, nthreads=0):
+    """Adjoint of integrate_seq_f64: (dL/ddepth, dL/dF0, dL/dW0)."""
+    nz, ny, nx = shape
+    depth = np.ascontiguousarray(depth, np.float64)
+    nf, h, w = depth.shape
+    if vol0 is not None:
+        vol0 = np.ascontiguousarray(vol0, np.float32)
+    if normals is not None:
+        normals = np.ascontiguousarray(normals, np.float32)
+    gf = np.ascontiguousarray(grad_f, np.float64)
+    gw = None if grad_w is None else np.ascontiguousarray(grad_w, np.float64)
+    gd = np.zeros_like(depth)
+    gF0 = np.zeros(shape, np.float64)
+    gW0 = np.zeros(shape, np.float64)
+    lib().orc_integrate_seq_backward_f64(_p(vol0), nx, ny, nz, min_t, max_t, grid_s, ctypes.byref(k), nf,
+                                         _poses(poses), w, h, _p(depth), _p(normals), 1 if is_dynamic else 0,
+                                         _p(gf), _p(gw), _p(gd), _p(gF0), _p(gW0), nthreads)
+    return gd, gF0, gW0

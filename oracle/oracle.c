@@ -651,3 +651,271 @@ int orc_rle_decode_volume(const uint8_t *img, int64_t nbytes, orc_voxel *vol, in
     }
     return 0;
 }
+
+/* ------------------------------------------------------------------------ */
+/* adjoints (binary64).  No counterpart in the reference: these are the      */
+/* derivatives of the forward restatements above, with every discrete        */
+/* choice (cube case, pixel, truncation, clamp) taken from the FP32 mirror   */
+/* and held fixed, and every continuous value computed in binary64.          */
+/* ------------------------------------------------------------------------ */
+
+static inline double vox_f64(const void *vol, int vtype, int64_t i) {
+    return vtype == ORC_VOXEL_SHORT2 ? (double)((const orc_voxel *)vol)[i].tsdf / ORC_MAX_TSDF
+                                     : (double)((const orc_voxel_f32 *)vol)[i].tsdf;
+}
+
+int64_t orc_mc_edges(const void *vol, int vtype, int nx, int ny, int nz, int64_t *va, int64_t *vb,
+                     int64_t cap_verts) {
+    int64_t o = 0;
+    for (int z = 0; z + 1 < nz; ++z)
+        for (int y = 0; y + 1 < ny; ++y)
+            for (int x = 0; x + 1 < nx; ++x) {
+                int ci = cube_index(vol, vtype, nx, ny, x, y, z);
+                int nv = cube_nverts(ci);
+                for (int i = 0; i < nv; ++i, ++o) {
+                    if (o >= cap_verts) continue;
+                    int j = i / 3, kk = i % 3;
+                    int e = orc_tri_table[ci][3 * j + 2 - kk];
+                    int a = EA[e], b = EB[e];
+                    va[o] = lin(nx, ny, x + CX[a], y + CY[a], z + CZ[a]);
+                    vb[o] = lin(nx, ny, x + CX[b], y + CY[b], z + CZ[b]);
+                }
+            }
+    return o;
+}
+
+/* P = p_a + t (p_b - p_a), t = -f_a / (f_b - f_a + 1e-15)
+ * (cu_marching_cubes_v1.cu:256-264) */
+int64_t orc_mc_backward_f64(const void *vol, int vtype, int nx, int ny, int nz, double cell,
+                            const double *grad_pos, int64_t n, double *grad_f) {
+    int64_t o = 0;
+    for (int z = 0; z + 1 < nz; ++z)
+        for (int y = 0; y + 1 < ny; ++y)
+            for (int x = 0; x + 1 < nx; ++x) {
+                int ci = cube_index(vol, vtype, nx, ny, x, y, z);
+                int nv = cube_nverts(ci);
+                for (int i = 0; i < nv; ++i, ++o) {
+                    if (o >= n) continue;
+                    int j = i / 3, kk = i % 3;
+                    int e = orc_tri_table[ci][3 * j + 2 - kk];
+                    int a = EA[e], b = EB[e];
+                    int64_t la = lin(nx, ny, x + CX[a], y + CY[a], z + CZ[a]);
+                    int64_t lb = lin(nx, ny, x + CX[b], y + CY[b], z + CZ[b]);
+                    double fa = vox_f64(vol, vtype, la), fb = vox_f64(vol, vtype, lb);
+                    double g = 0.0;
+                    g += grad_pos[3 * o + 0] * (double)(CX[b] - CX[a]) * cell;
+                    g += grad_pos[3 * o + 1] * (double)(CY[b] - CY[a]) * cell;
+                    g += grad_pos[3 * o + 2] * (double)(CZ[b] - CZ[a]) * cell;
+                    double D = fb - fa + 1e-15;
+                    grad_f[la] += g * (-(fb + 1e-15)) / (D * D);
+                    grad_f[lb] += g * fa / (D * D);
+                }
+            }
+    return o;
+}
+
+/* FP32 decisions of one integrate observation, exactly as orc_integrate
+ * takes them.  branch: 0 sdf <= 0, 1 0 < sdf <= max_t, 2 clamped at 1. */
+static int decide32(const orc_extrinsic *e, const orc_intrinsic *k, int w, int h, float min_t, float max_t,
+                    const float *ds, const float *normals, float px, float py, float pz, int64_t *pix,
+                    int *u_out, int *v_out, int *branch) {
+    const float *R = e->r;
+    float v0 = px - e->t[0], v1 = py - e->t[1], v2 = pz - e->t[2];
+    float q0 = R[0] * v0 + R[1] * v1 + R[2] * v2;
+    float q1 = R[3] * v0 + R[4] * v1 + R[5] * v2;
+    float q2 = R[6] * v0 + R[7] * v1 + R[8] * v2;
+    if (q2 < FLT_MIN) return 0;
+    float u_f = k->fx * (q0 / q2) + k->cx;
+    float v_f = k->fy * (q1 / q2) + k->cy;
+    int u = f2i_rn(u_f), v = f2i_rn(v_f);
+    if (u < 0 || v < 0 || u >= (w - 2) || v >= (h - 2)) return 0;
+    int64_t p = (int64_t)v * w + u;
+    float z_val = ds[p];
+    if (!(z_val > FLT_MIN)) return 0;
+    float qn = sqrtf(q0 * q0 + q1 * q1 + q2 * q2);
+    float sdf = z_val - qn;
+    if (!(sdf >= -min_t)) return 0;
+    int br = 0;
+    if (sdf > 0.0f) {
+        br = (sdf / max_t > 1.0f) ? 2 : 1;
+    }
+    if (normals) {
+        const float *n = normals + 3 * p;
+        if (!vertex_valid(n)) return 0;
+        float wgt = -(n[0] * (q0 / qn) + n[1] * (q1 / qn) + n[2] * (q2 / qn));
+        if (wgt < FLT_MIN) return 0;
+    }
+    *pix = p;
+    *u_out = u;
+    *v_out = v;
+    *branch = br;
+    return 1;
+}
+
+/* binary64 values of one observation given its decisions */
+typedef struct {
+    double s, w0, z, dsdz, c;
+} orc_obs64;
+
+static orc_obs64 observe64(const orc_extrinsic *e, const orc_intrinsic *k, double min_t, double max_t,
+                           const float *nrm, int u, int v, int branch, double depth, double px, double py,
+                           double pz) {
+    const float *R = e->r;
+    double v0 = px - e->t[0], v1 = py - e->t[1], v2 = pz - e->t[2];
+    double q0 = R[0] * v0 + R[1] * v1 + R[2] * v2;
+    double q1 = R[3] * v0 + R[4] * v1 + R[5] * v2;
+    double q2 = R[6] * v0 + R[7] * v1 + R[8] * v2;
+    double cx = ((double)u - k->cx) / k->fx, cy = ((double)v - k->cy) / k->fy;
+    orc_obs64 o;
+    o.c = sqrt(cx * cx + cy * cy + 1.0);
+    o.z = depth * o.c;
+    double qn = sqrt(q0 * q0 + q1 * q1 + q2 * q2);
+    double s = o.z - qn;
+    if (branch == 0) { o.s = s / min_t; o.dsdz = 1.0 / min_t; }
+    else if (branch == 1) { o.s = s / max_t; o.dsdz = 1.0 / max_t; }
+    else { o.s = 1.0; o.dsdz = 0.0; }
+    double wgt = 1.0;
+    if (nrm) wgt = -(nrm[0] * (q0 / qn) + nrm[1] * (q1 / qn) + nrm[2] * (q2 / qn));
+    o.w0 = wgt / o.z;
+    return o;
+}
+
+static inline uint64_t mix64(uint64_t x) {
+    x ^= x >> 33; x *= 0xff51afd7ed558ccdULL;
+    x ^= x >> 33; x *= 0xc4ceb9fe1a85ec53ULL;
+    x ^= x >> 33;
+    return x;
+}
+
+/* scaled FP32 depth of every frame, from (float)depth */
+static float *scaled_frames(const orc_intrinsic *k, int n_frames, int w, int h, const double *depth) {
+    size_t plane = (size_t)w * h;
+    float *d32 = (float *)malloc(sizeof(float) * plane);
+    float *ds = (float *)malloc(sizeof(float) * plane * n_frames);
+    for (int f = 0; f < n_frames; ++f) {
+        for (size_t i = 0; i < plane; ++i) d32[i] = (float)depth[f * plane + i];
+        orc_depth_scale(k, w, h, d32, ds + f * plane);
+    }
+    free(d32);
+    return ds;
+}
+
+void orc_integrate_seq_f64(const float *vol0, int nx, int ny, int nz, float min_t, float max_t, float grid_s,
+                           const orc_intrinsic *k, int n_frames, const orc_extrinsic *poses, int w, int h,
+                           const double *depth, const float *normals, int is_dynamic, double *F, double *W,
+                           uint64_t *signature, int nthreads) {
+    nthreads = nthreads_or_default(nthreads);
+    size_t plane = (size_t)w * h;
+    float *ds = scaled_frames(k, n_frames, w, h, depth);
+    uint64_t sig = 0;
+#pragma omp parallel for collapse(2) schedule(static) num_threads(nthreads) reduction(+ : sig)
+    for (int z = 0; z < nz; ++z)
+        for (int y = 0; y < ny; ++y) {
+            float px = -grid_s;
+            for (int x = 0; x < nx; ++x) {
+                px += grid_s;
+                int64_t li = lin(nx, ny, x, y, z);
+                double Fc = vol0 ? vol0[2 * li] : -1.0, Wc = vol0 ? vol0[2 * li + 1] : 0.0;
+                for (int f = 0; f < n_frames; ++f) {
+                    int64_t pix; int u, v, br;
+                    const float *nf = normals ? normals + 3 * plane * f : NULL;
+                    int ok = decide32(poses + f, k, w, h, min_t, max_t, ds + plane * f, nf, px,
+                                      (float)y * grid_s, (float)z * grid_s, &pix, &u, &v, &br);
+                    sig += mix64(((uint64_t)li * (uint64_t)n_frames + (uint64_t)f) * 0x9e3779b97f4a7c15ULL +
+                                 (ok ? (uint64_t)pix * 4u + (uint64_t)br + 1u : 0u));
+                    if (!ok) continue;
+                    orc_obs64 o = observe64(poses + f, k, min_t, max_t, nf ? nf + 3 * pix : NULL, u, v, br,
+                                            depth[plane * f + pix], px, (double)((float)y * grid_s),
+                                            (double)((float)z * grid_s));
+                    double wv = o.w0;
+                    if (is_dynamic) { double d = o.s - Fc; wv = wv * (1.0 + d * d * 10.0); }
+                    double Wn = Wc + wv;
+                    Fc = (Wc * Fc + wv * o.s) / Wn;
+                    Wc = Wn;
+                }
+                F[li] = Fc;
+                W[li] = Wc;
+            }
+        }
+    free(ds);
+    if (signature) *signature = sig;
+}
+
+void orc_integrate_seq_backward_f64(const float *vol0, int nx, int ny, int nz, float min_t, float max_t,
+                                    float grid_s, const orc_intrinsic *k, int n_frames,
+                                    const orc_extrinsic *poses, int w, int h, const double *depth,
+                                    const float *normals, int is_dynamic, const double *gF_end,
+                                    const double *gW_end, double *g_depth, double *gF0, double *gW0,
+                                    int nthreads) {
+    nthreads = nthreads_or_default(nthreads);
+    size_t plane = (size_t)w * h;
+    float *ds = scaled_frames(k, n_frames, w, h, depth);
+#pragma omp parallel num_threads(nthreads)
+    {
+        double *Fp = (double *)malloc(sizeof(double) * n_frames);
+        double *Wp = (double *)malloc(sizeof(double) * n_frames);
+        orc_obs64 *ob = (orc_obs64 *)malloc(sizeof(orc_obs64) * n_frames);
+        int64_t *px_of = (int64_t *)malloc(sizeof(int64_t) * n_frames);
+        int *okf = (int *)malloc(sizeof(int) * n_frames);
+#pragma omp for collapse(2) schedule(dynamic, 4)
+        for (int z = 0; z < nz; ++z)
+            for (int y = 0; y < ny; ++y) {
+                float px = -grid_s;
+                for (int x = 0; x < nx; ++x) {
+                    px += grid_s;
+                    int64_t li = lin(nx, ny, x, y, z);
+                    double gF = gF_end[li], gW = gW_end ? gW_end[li] : 0.0;
+                    if (gF != 0.0 || gW != 0.0) {
+                        double Fc = vol0 ? vol0[2 * li] : -1.0, Wc = vol0 ? vol0[2 * li + 1] : 0.0;
+                        for (int f = 0; f < n_frames; ++f) {
+                            int64_t pix; int u, v, br;
+                            const float *nf = normals ? normals + 3 * plane * f : NULL;
+                            Fp[f] = Fc;
+                            Wp[f] = Wc;
+                            okf[f] = decide32(poses + f, k, w, h, min_t, max_t, ds + plane * f, nf, px,
+                                              (float)y * grid_s, (float)z * grid_s, &pix, &u, &v, &br);
+                            if (!okf[f]) continue;
+                            px_of[f] = pix;
+                            ob[f] = observe64(poses + f, k, min_t, max_t, nf ? nf + 3 * pix : NULL, u, v, br,
+                                              depth[plane * f + pix], px, (double)((float)y * grid_s),
+                                              (double)((float)z * grid_s));
+                            double wv = ob[f].w0;
+                            if (is_dynamic) { double d = ob[f].s - Fc; wv = wv * (1.0 + d * d * 10.0); }
+                            double Wn = Wc + wv;
+                            Fc = (Wc * Fc + wv * ob[f].s) / Wn;
+                            Wc = Wn;
+                        }
+                        for (int f = n_frames - 1; f >= 0; --f) {
+                            if (!okf[f]) continue;
+                            const orc_obs64 o = ob[f];
+                            double mult = 1.0, d = 0.0, wv = o.w0;
+                            if (is_dynamic) { d = o.s - Fp[f]; mult = 1.0 + d * d * 10.0; wv = wv * mult; }
+                            double Wn = Wp[f] + wv;
+                            double Fn = (Wp[f] * Fp[f] + wv * o.s) / Wn;
+                            double gs = gF * wv / Wn;
+                            double gw = gF * (o.s - Fn) / Wn + gW;
+                            double gFp = gF * Wp[f] / Wn;
+                            double gWp = gF * (Fp[f] - Fn) / Wn + gW;
+                            double gw0 = gw;
+                            if (is_dynamic) {
+                                double t = gw * o.w0 * 20.0 * d;
+                                gs += t;
+                                gFp -= t;
+                                gw0 = gw * mult;
+                            }
+                            double gz = gs * o.dsdz - gw0 * o.w0 / o.z;
+                            double add = gz * o.c;
+#pragma omp atomic
+                            g_depth[plane * f + px_of[f]] += add;
+                            gF = gFp;
+                            gW = gWp;
+                        }
+                    }
+                    if (gF0) gF0[li] = gF;
+                    if (gW0) gW0[li] = gW;
+                }
+            }
+        free(Fp); free(Wp); free(ob); free(px_of); free(okf);
+    }
+    free(ds);
+}

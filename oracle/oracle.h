@@ -95,6 +95,30 @@ int64_t orc_rle_encode_volume(const orc_voxel *vol, int nx, int ny, int nz, floa
 int orc_rle_decode_volume(const uint8_t *img, int64_t nbytes, orc_voxel *vol, int64_t cap_voxels,
                           int dims[3], float params[3]);
 
+/* ---- adjoints (binary64; no counterpart in the reference) -------------- */
+/* linear voxel indices of the two corners of each soup vertex's edge,
+ * canonical order; returns the vertex total */
+int64_t orc_mc_edges(const void *vol, int vtype, int nx, int ny, int nz, int64_t *va, int64_t *vb,
+                     int64_t cap_verts);
+/* dL/df (f = tsdf, or tsdf/32766 for short2) += adjoint of the soup
+ * positions for dL/dP (canonical order, n vertices); cube cases fixed */
+int64_t orc_mc_backward_f64(const void *vol, int vtype, int nx, int ny, int nz, double cell,
+                            const double *grad_pos, int64_t n, double *grad_f);
+/* n_frames integrate steps on a float2 volume in binary64 (vol0: float2 or
+ * NULL = (-1, 0)); decisions from the FP32 mirror at (float)depth.
+ * signature: hash of every decision, to tell when a perturbation changes one */
+void orc_integrate_seq_f64(const float *vol0, int nx, int ny, int nz, float min_t, float max_t, float grid_s,
+                           const orc_intrinsic *k, int n_frames, const orc_extrinsic *poses, int w, int h,
+                           const double *depth, const float *normals, int is_dynamic, double *F, double *W,
+                           uint64_t *signature, int nthreads);
+/* its adjoint: dL/ddepth += ..., dL/d(F0, W0) written (may be NULL) */
+void orc_integrate_seq_backward_f64(const float *vol0, int nx, int ny, int nz, float min_t, float max_t,
+                                    float grid_s, const orc_intrinsic *k, int n_frames,
+                                    const orc_extrinsic *poses, int w, int h, const double *depth,
+                                    const float *normals, int is_dynamic, const double *gF_end,
+                                    const double *gW_end, double *g_depth, double *gF0, double *gW0,
+                                    int nthreads);
+
 int orc_max_threads(void);
 
 #ifdef __cplusplus
