@@ -49,6 +49,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-graph", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
     return ap.parse_args()
 
 
@@ -256,6 +257,62 @@ def bench_graph(mcg, synthetic, torch, n=256, frames=20):
 
 
 
+def bench_adjoint(mcg, synthetic, torch, n=256, frames=10, reps=5):
+    """Differentiable fusion of the blended-spheres scene: 10 sphere-traced
+    320x240 depth frames (f 262.5) -> 256^3 float32 volume (trunc 4 voxels)
+    -> soup positions -> L = sum G . P; forward and torch.autograd backward
+    (integrate adjoint + MC adjoint) timed with CUDA events."""
+    scene = synthetic.BlendedSpheres(seed=0)
+    w, h, f = 320, 240, 262.5
+    depth, poses = scene.frames(frames, w=w, h=h, fx=f, fy=f, device="cuda")
+    depth = depth.to(torch.float32).contiguous()
+    k = mcg.intrinsic(f, f, (w - 1) / 2.0, (h - 1) / 2.0)
+    pt = torch.stack([mcg.extrinsic_tensor(R, t) for R, t in poses]).contiguous()
+    shape = (n, n, n)
+    gs = 1.0 / n
+    trunc = 4 * gs
+    G = None
+
+    def fwd(d):
+        vol = mcg.integrate_frames(d, pt, shape, trunc, trunc, gs, k)
+        return vol, mcg.mesh_positions(vol, gs)
+
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    fw, bw = [], []
+    for i in range(reps + 2):
+        d = depth.clone().requires_grad_(True)
+        torch.cuda.synchronize()
+        e[0].record()
+        vol, pos = fwd(d)
+        if G is None:
+            g = torch.Generator(device="cuda")
+            g.manual_seed(0)
+            G = torch.randn(pos.shape, device="cuda", generator=g)
+        loss = (pos * G).sum()
+        e[1].record()
+        loss.backward()
+        e[2].record()
+        torch.cuda.synchronize()
+        if i >= 2:
+            fw.append(e[0].elapsed_time(e[1]))
+            bw.append(e[1].elapsed_time(e[2]))
+    # the two adjoint kernels alone
+    vol = vol.detach()
+    gpos = G.contiguous()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    ev[0].record()
+    gf = mcg.mc_backward(vol, gs, gpos)
+    ev[1].record()
+    mcg.integrate_backward(shape, trunc, trunc, gs, k, pt, depth, gf)
+    ev[2].record()
+    torch.cuda.synchronize()
+    fms, bms = float(np.median(fw)), float(np.median(bw))
+    return {"volume": list(shape), "frames": frames, "image": [w, h], "vertices": int(pos.shape[0]),
+            "forward_ms": fms, "backward_ms": bms, "adjoint_over_forward": bms / fms,
+            "mc_backward_ms": ev[0].elapsed_time(ev[1]), "integrate_backward_ms": ev[1].elapsed_time(ev[2]),
+            "precision": "fp32 accumulate (atomics)"}
+
+
 def run_reference(args):
     """--impl reference: the reference has no CPU marching cubes (MyMarchingCube.h
     is a declaration only); its algorithm restated in C (oracle/) runs on all
@@ -446,6 +503,13 @@ def main():
         except Exception as ex:  # pragma: no cover
             graph = {"error": str(ex)}
 
+    adjoint = None
+    if not args.no_adjoint:
+        try:
+            adjoint = bench_adjoint(mcg, synthetic, torch)
+        except Exception as ex:  # pragma: no cover
+            adjoint = {"error": str(ex)}
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         try:
@@ -469,6 +533,7 @@ def main():
         "integrate": integ,
         "batched": batched,
         "graph": graph,
+        "adjoint": adjoint,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)

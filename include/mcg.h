@@ -37,7 +37,7 @@ typedef enum mcg_status {
     MCG_ERR_IO = 5,          /* file could not be opened / read / written */
     MCG_ERR_FORMAT = 6,      /* malformed RLE stream or file header */
     MCG_ERR_STATE = 7,       /* call order violated (e.g. generate without classify) */
-    MCG_ERR_TOO_LARGE = 8    /* volume larger than the fixed scratch of mcg_mc_extract_noalloc */
+    MCG_ERR_TOO_LARGE = 8    /* input above a fixed limit (mcg_mc_extract_noalloc's scratch, mcg_integrate_backward's frame count) */
 } mcg_status;
 
 /* voxel storage types */

@@ -23,7 +23,7 @@ const char *mcg_status_string(int status) {
         case MCG_ERR_IO: return "I/O error";
         case MCG_ERR_FORMAT: return "malformed stream or header";
         case MCG_ERR_STATE: return "call order violated";
-        case MCG_ERR_TOO_LARGE: return "volume exceeds the fixed scratch of the no-allocation entry point";
+        case MCG_ERR_TOO_LARGE: return "volume exceeds the fixed scratch of the no-allocation entry point, or more than 512 frames per adjoint call";
         default: return "unknown status";
     }
 }
