@@ -260,8 +260,9 @@ def bench_graph(mcg, synthetic, torch, n=256, frames=20):
 def bench_adjoint(mcg, synthetic, torch, n=256, frames=10, reps=5):
     """Differentiable fusion of the blended-spheres scene: 10 sphere-traced
     320x240 depth frames (f 262.5) -> 256^3 float32 volume (trunc 4 voxels)
-    -> soup positions -> L = sum G . P; forward and torch.autograd backward
-    (integrate adjoint + MC adjoint) timed with CUDA events."""
+    -> soup positions P -> L = sum phi(P)^2 with phi the analytic blended
+    field; forward and torch.autograd backward (integrate adjoint + MC
+    adjoint) timed with CUDA events."""
     scene = synthetic.BlendedSpheres(seed=0)
     w, h, f = 320, 240, 262.5
     depth, poses = scene.frames(frames, w=w, h=h, fx=f, fy=f, device="cuda")
@@ -271,11 +272,6 @@ def bench_adjoint(mcg, synthetic, torch, n=256, frames=10, reps=5):
     shape = (n, n, n)
     gs = 1.0 / n
     trunc = 4 * gs
-    G = None
-
-    def fwd(d):
-        vol = mcg.integrate_frames(d, pt, shape, trunc, trunc, gs, k)
-        return vol, mcg.mesh_positions(vol, gs)
 
     e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
     fw, bw = [], []
@@ -283,12 +279,9 @@ def bench_adjoint(mcg, synthetic, torch, n=256, frames=10, reps=5):
         d = depth.clone().requires_grad_(True)
         torch.cuda.synchronize()
         e[0].record()
-        vol, pos = fwd(d)
-        if G is None:
-            g = torch.Generator(device="cuda")
-            g.manual_seed(0)
-            G = torch.randn(pos.shape, device="cuda", generator=g)
-        loss = (pos * G).sum()
+        vol = mcg.integrate_frames(d, pt, shape, trunc, trunc, gs, k)
+        pos = mcg.mesh_positions(vol, gs)
+        loss = (scene.sdf(pos) ** 2).sum()
         e[1].record()
         loss.backward()
         e[2].record()
@@ -296,20 +289,37 @@ def bench_adjoint(mcg, synthetic, torch, n=256, frames=10, reps=5):
         if i >= 2:
             fw.append(e[0].elapsed_time(e[1]))
             bw.append(e[1].elapsed_time(e[2]))
-    # the two adjoint kernels alone
+    # the path alone (no loss evaluation): forward integrate + extract, then
+    # the two adjoint calls (count phase re-run + MC adjoint, integrate adjoint)
     vol = vol.detach()
-    gpos = G.contiguous()
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
-    ev[0].record()
-    gf = mcg.mc_backward(vol, gs, gpos)
-    ev[1].record()
-    mcg.integrate_backward(shape, trunc, trunc, gs, k, pt, depth, gf)
-    ev[2].record()
-    torch.cuda.synchronize()
+    p = pos.detach().requires_grad_(True)
+    (scene.sdf(p) ** 2).sum().backward()
+    gpos = p.grad.contiguous()
+    pf, pb, mb, ib = [], [], [], []
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    for i in range(reps + 2):
+        torch.cuda.synchronize()
+        ev[0].record()
+        v2 = mcg.integrate_frames(depth, pt, shape, trunc, trunc, gs, k)
+        mcg.mesh_positions(v2, gs)
+        ev[1].record()
+        gf = mcg.mc_backward(v2, gs, gpos)
+        ev[2].record()
+        mcg.integrate_backward(shape, trunc, trunc, gs, k, pt, depth, gf)
+        ev[3].record()
+        torch.cuda.synchronize()
+        if i >= 2:
+            pf.append(ev[0].elapsed_time(ev[1]))
+            mb.append(ev[1].elapsed_time(ev[2]))
+            ib.append(ev[2].elapsed_time(ev[3]))
+            pb.append(ev[1].elapsed_time(ev[3]))
     fms, bms = float(np.median(fw)), float(np.median(bw))
+    pfm, pbm = float(np.median(pf)), float(np.median(pb))
     return {"volume": list(shape), "frames": frames, "image": [w, h], "vertices": int(pos.shape[0]),
-            "forward_ms": fms, "backward_ms": bms, "adjoint_over_forward": bms / fms,
-            "mc_backward_ms": ev[0].elapsed_time(ev[1]), "integrate_backward_ms": ev[1].elapsed_time(ev[2]),
+            "loss": "sum phi(P)^2 (phi: analytic field, torch ops)",
+            "autograd_forward_ms": fms, "autograd_backward_ms": bms, "autograd_adjoint_over_forward": bms / fms,
+            "path_forward_ms": pfm, "path_backward_ms": pbm, "path_adjoint_over_forward": pbm / pfm,
+            "mc_backward_ms": float(np.median(mb)), "integrate_backward_ms": float(np.median(ib)),
             "precision": "fp32 accumulate (atomics)"}
 
 

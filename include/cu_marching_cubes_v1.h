@@ -43,6 +43,13 @@ public:
     /* counts of the last run */
     const mcg_mesh_counts &counts() const { return counts_; }
 
+    /* adjoint of the last run's soup positions (no counterpart in the
+     * reference): grad_pos holds dL/dP per soup vertex of that run, in its
+     * order; dL/df (f = tsdf / 32766) is accumulated into grad_tsdf (one
+     * float per voxel, allocated and zeroed here when empty).  The volume
+     * must be unchanged since run(). */
+    void backward(cu_voxel &tsdf, const cu_array<float3> &grad_pos, cu_array<float> &grad_tsdf);
+
 private:
     cu_array<vertex_voxel> run_impl(cu_voxel &tsdf, cu_array<vertex_voxel> &triangles_buffer,
                                     cu_array<int3> &vertexindex_to_voxel, cu_array<short> &ver_voxel,

@@ -7,6 +7,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <fstream>
@@ -325,6 +326,22 @@ cu_array<vertex_voxel> MarchingCubes::run_impl(cu_voxel &tsdf, cu_array<vertex_v
     check_status(mcg_mc_counts(ctx_, &counts_), ctx_, "mcg_mc_counts");
     if (n == 0) return cu_array<vertex_voxel>();
     return cu_array<vertex_voxel>(triangles_buffer.ptr(), n);
+}
+
+void MarchingCubes::backward(cu_voxel &tsdf, const cu_array<float3> &grad_pos, cu_array<float> &grad_tsdf) {
+    const mcg_volume vol = to_volume(tsdf);
+    const size_t nvox = (size_t)tsdf.size.x * tsdf.size.y * tsdf.size.z;
+    if (grad_tsdf.empty()) {
+        grad_tsdf.create(nvox);
+        check(cudaMemset(grad_tsdf.ptr(), 0, nvox * sizeof(float)), "cudaMemset");
+    } else if (grad_tsdf.size() < nvox) {
+        throw std::invalid_argument("MarchingCubes::backward: grad_tsdf smaller than the volume");
+    }
+    const int64_t n = (int64_t)std::min<size_t>(grad_pos.size(), (size_t)counts_.vertices);
+    check_status(mcg_mc_backward(ctx_, &vol, reinterpret_cast<const float *>(grad_pos.ptr()), n, grad_tsdf.ptr(),
+                                 nullptr),
+                 ctx_, "mcg_mc_backward");
+    check(cudaDeviceSynchronize(), "cudaDeviceSynchronize");
 }
 
 // ---------------------------------------------------------------------------

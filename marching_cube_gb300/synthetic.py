@@ -11,10 +11,11 @@ sizes and value ranges of the workloads:
                   1.5 m (pinhole 525/525/319.5/239.5, 640x480), Gaussian
                   noise sigma 2 mm, uint16 millimetres
   random_volume   small random short2 volumes for exhaustive parity cases
-  blended_spheres smooth union (log-sum-exp, sharpness 32/m) of 8 spheres
-                  in a 1 m cube, float depth frames sphere-traced from a
-                  camera orbiting at 1.2 m (pinhole 262.5/262.5, 320x240),
-                  for the differentiable path
+  blended_spheres smooth union (quadratic polynomial smooth-min, blend
+                  radius k = 0.06 m) of 8 spheres in a 1 m cube, float depth
+                  frames sphere-traced from a camera orbiting at 1.2 m
+                  (pinhole 262.5/262.5/159.5/119.5, 320x240), for the
+                  differentiable path
 
 Randomness: numpy.random.default_rng(seed) for scene parameters and
 torch.Generator(seed) for per-pixel noise.
@@ -111,24 +112,32 @@ def orbit_pose(center, frame, n_frames, radius):
 
 
 class BlendedSpheres:
-    """Smooth union f(p) = -log(sum_i exp(-k d_i(p))) / k of n spheres inside
-    a cube of side `extent` metres; f is 1-Lipschitz, so sphere tracing on it
-    is safe."""
+    """Smooth union of n spheres inside a cube of side `extent` metres,
+    folded with the quadratic polynomial smooth-min
+        smin(a, b) = min(a, b) - h^2 k / 4,  h = max(k - |a - b|, 0) / k
+    (blend radius k).  Each fold is a convex combination of its arguments'
+    gradients, so the field is 1-Lipschitz and sphere tracing on it is safe."""
 
-    def __init__(self, seed=0, n_spheres=8, extent=1.0, sharpness=32.0):
+    def __init__(self, seed=0, n_spheres=8, extent=1.0, blend=0.06):
         rng = np.random.default_rng(seed)
         c = extent / 2.0
         self.extent = extent
         self.center = np.array([c, c, c])
         self.sph_c = c + rng.uniform(-0.18, 0.18, size=(n_spheres, 3)) * extent
         self.sph_r = rng.uniform(0.07, 0.15, size=n_spheres) * extent
-        self.k = sharpness / extent
+        self.k = blend * extent
 
     def sdf(self, p):
         c = torch.as_tensor(self.sph_c, dtype=p.dtype, device=p.device)
         r = torch.as_tensor(self.sph_r, dtype=p.dtype, device=p.device)
         d = torch.linalg.norm(p[:, None, :] - c[None, :, :], dim=-1) - r[None, :]
-        return -torch.logsumexp(-self.k * d, dim=1) / self.k
+        k = self.k
+        f = d[:, 0]
+        for i in range(1, d.shape[1]):
+            b = d[:, i]
+            h = torch.clamp(k - (f - b).abs(), min=0.0) / k
+            f = torch.minimum(f, b) - h * h * (k / 4.0)
+        return f
 
     def pose(self, frame, n_frames, radius=1.2):
         return orbit_pose(self.center, frame, n_frames, radius * self.extent)

@@ -52,6 +52,21 @@ int main(int argc, char **argv) {
     // copies share the buffer; the returned view does not own it
     cu_array<vertex_voxel> copy = tri;
     const bool shared = copy.ptr() == tri.ptr() && mesh.ptr() == tri.ptr();
+    // 2b. adjoint of the run's positions for a constant dL/dP (order-free)
+    {
+        std::vector<float3> gp(mesh.size(), make_float3(1.0f, 0.5f, -0.25f));
+        cu_array<float3> grad_pos;
+        grad_pos.upload(gp);
+        cu_array<float> grad_tsdf;
+        mc.backward(vol, grad_pos, grad_tsdf);
+        std::vector<float> g;
+        grad_tsdf.download(g);
+        FILE *f = fopen((dir + "/grad_tsdf.bin").c_str(), "wb");
+        if (f) {
+            fwrite(g.data(), sizeof(float), g.size(), f);
+            fclose(f);
+        }
+    }
     // 3. RLE: write the whole volume, then rewrite a window, read back
     const std::string rle = dir + "/vol.rle";
     remove(rle.c_str());

@@ -195,8 +195,9 @@ def test_autograd_volume_leaf(mcg, orc):
 def test_blended_spheres_full_size(mcg, orc):
     """The differentiable-fusion workload at its full size: 10 sphere-traced
     320x240 frames (f 262.5) of 8 blended spheres -> 256^3 float32 volume ->
-    soup positions; the autograd gradient w.r.t. every depth pixel against
-    the binary64 adjoint chain."""
+    soup positions P -> L = sum phi(P)^2 (phi the analytic field); the
+    autograd gradient w.r.t. every depth pixel against the binary64 adjoint
+    chain fed the same dL/dP."""
     scene = synthetic.BlendedSpheres(seed=0)
     w, h, f, n, frames = 320, 240, 262.5, 256, 10
     depth64, poses = scene.frames(frames, w=w, h=h, fx=f, fy=f, device="cuda")
@@ -209,10 +210,9 @@ def test_blended_spheres_full_size(mcg, orc):
     vol = mcg.integrate_frames(d, pt, shape, trunc, trunc, gs, k)
     pos = mcg.mesh_positions(vol, gs)
     assert pos.shape[0] > 100000
-    g = torch.Generator(device="cuda")
-    g.manual_seed(3)
-    G = torch.randn(pos.shape, device="cuda", generator=g)
-    (pos * G).sum().backward()
+    pos.retain_grad()
+    (scene.sdf(pos) ** 2).sum().backward()
+    G = pos.grad
     vol_np = vol.detach().cpu().numpy()
     idx = _canonical_order(mcg, vol.detach().contiguous(), gs)
     gF = orc.mc_backward_f64(vol_np, gs, G.cpu().numpy()[idx].astype(np.float64))

@@ -47,6 +47,12 @@ def test_cpp_dropin_runs(tmp_path, orc):
     vol = np.stack([t, w.astype(np.int16)], axis=-1)
     _, ntri = orc.mc_count(vol)
     assert res["triangles"] == ntri and res["mesh_size"] == 3 * ntri and res["shared"] == 1
+    # MarchingCubes::backward against the binary64 adjoint (constant dL/dP)
+    g = np.fromfile(os.path.join(str(tmp_path), "grad_tsdf.bin"), np.float32)
+    G = np.tile(np.array([1.0, 0.5, -0.25]), (3 * ntri, 1))
+    g64 = orc.mc_backward_f64(vol, 0.01, G).reshape(-1)
+    assert np.count_nonzero(g64) > 100
+    assert np.linalg.norm(g - g64) <= 1e-4 * np.linalg.norm(g64)
     # PLY: header + 3 vertices per triangle with position and normal
     ply = open(os.path.join(str(tmp_path), "sphere.ply"), "rb").read()
     head, body = ply.split(b"end_header\n", 1)
