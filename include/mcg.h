@@ -117,6 +117,36 @@ mcg_status mcg_mc_generate(mcg_context *ctx, const mcg_volume *vol, const mcg_me
 /* classify + generate in one call, no host synchronisation */
 mcg_status mcg_mc_extract(mcg_context *ctx, const mcg_volume *vol, const mcg_mesh_out *out,
                           mcg_stream_t stream);
+/* Indexed extraction (no counterpart in the reference, whose OBJ writer
+ * merges soup vertices by their printed coordinates, kf.cu:3625-3726): one
+ * vertex per grid edge the surface crosses, shared by every triangle using
+ * it.  A vertex is on the edge from voxel (x, y, z) to its +1 neighbour
+ * along `axis`; vertex_edge names it 3 * (linear index of (x, y, z)) + axis
+ * (0 x, 1 y, 2 z).  Its position is mc.cu:256-264's interpolation taken from
+ * the lower voxel to the upper one; its normal is kf.cu:3146-3242's at that
+ * position.  Triangles are the soup's, in the soup's order and winding,
+ * as 3 vertex indices.  Every output pointer may be NULL. */
+typedef struct mcg_indexed_out {
+    float *positions;      /* 3 floats per vertex */
+    float *normals;        /* 3 floats per vertex */
+    int32_t *vi2vox;       /* 3 ints per vertex: floor(P / cell - 0.5) (mc.cu:336-343) */
+    int64_t *vertex_edge;  /* 1 per vertex */
+    uint32_t *triangles;   /* 3 vertex indices per triangle */
+    int64_t *tri_cube;     /* 1 per triangle: linear index of its cube */
+    int64_t capacity_vertices;   /* <= 2^32 - 1 */
+    int64_t capacity_triangles;
+} mcg_indexed_out;
+/* Count phase of the indexed mesh; mcg_mc_counts then reports triangles
+ * and vertices = unique vertices.  Asynchronous. */
+mcg_status mcg_mc_classify_indexed(mcg_context *ctx, const mcg_volume *vol, mcg_stream_t stream);
+/* Writes at most capacity_vertices vertices and capacity_triangles
+ * triangles; mcg_mc_counts reports MCG_ERR_CAPACITY with the full sizes.
+ * Keeps 12 bytes per voxel of edge -> vertex map in ctx (touched only at
+ * crossed edges). */
+mcg_status mcg_mc_generate_indexed(mcg_context *ctx, const mcg_volume *vol, const mcg_indexed_out *out,
+                                   mcg_stream_t stream);
+mcg_status mcg_mc_extract_indexed(mcg_context *ctx, const mcg_volume *vol, const mcg_indexed_out *out,
+                                  mcg_stream_t stream);
 /* Batched extraction: nvol volumes of any sizes (same voxel type) in one
  * launch per pass (replaces a loop of MarchingCubes::run calls).  Outputs
  * of volume v go to outs[v], in the same order and bit-identical to a

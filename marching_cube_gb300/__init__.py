@@ -278,6 +278,71 @@ def extract(volume, cell, *, soup=True, normals=True, vi2vox=False, ver_voxel=Fa
     return Mesh(o["soup"], o["normals"], o["vi2vox"], o["ver_voxel"], o["tri_cube"], c)
 
 
+class IndexedMesh:
+    """Indexed mesh: vertices shared between triangles (one per crossed grid
+    edge), triangles as (T, 3) int32 vertex indices in the soup's order and
+    winding."""
+
+    def __init__(self, positions=None, normals=None, vi2vox=None, vertex_edge=None, triangles=None, tri_cube=None,
+                 counts=None):
+        self.positions = positions
+        self.normals = normals
+        self.vi2vox = vi2vox
+        self.vertex_edge = vertex_edge
+        self.triangles = triangles
+        self.tri_cube = tri_cube
+        self.counts = counts or {}
+
+    @property
+    def num_vertices(self):
+        return int(self.counts.get("vertices", 0))
+
+    @property
+    def num_triangles(self):
+        return int(self.counts.get("triangles", 0))
+
+
+def _indexed_out(o, capv, capt):
+    def ptr(k):
+        return o[k].data_ptr() if o.get(k) is not None else None
+    return _capi.IndexedOut(ptr("positions"), ptr("normals"), ptr("vi2vox"), ptr("vertex_edge"), ptr("triangles"),
+                            ptr("tri_cube"), int(capv), int(capt))
+
+
+def extract_indexed(volume, cell, *, normals=True, vi2vox=False, vertex_edge=False, tri_cube=False, ctx=None,
+                    stream=None) -> IndexedMesh:
+    """Indexed marching cubes: count phase, one host synchronisation for the
+    sizes, then vertices and triangles into exactly-sized buffers."""
+    ctx = ctx or default_context(volume.device.index)
+    cv = _cvol(volume, cell)
+    s = _stream(stream)
+    ctx.check(_lib.mcg_mc_classify_indexed(ctx.handle, ctypes.byref(cv), s), "mcg_mc_classify_indexed")
+    c = counts(ctx)
+    nv, nt = c["vertices"], c["triangles"]
+    dev = volume.device
+    o = {"positions": torch.empty((nv, 3), dtype=torch.float32, device=dev),
+         "normals": torch.empty((nv, 3), dtype=torch.float32, device=dev) if normals else None,
+         "vi2vox": torch.empty((nv, 3), dtype=torch.int32, device=dev) if vi2vox else None,
+         "vertex_edge": torch.empty((nv,), dtype=torch.int64, device=dev) if vertex_edge else None,
+         "triangles": torch.empty((nt, 3), dtype=torch.int32, device=dev),
+         "tri_cube": torch.empty((nt,), dtype=torch.int64, device=dev) if tri_cube else None}
+    io = _indexed_out(o, nv, nt)
+    ctx.check(_lib.mcg_mc_generate_indexed(ctx.handle, ctypes.byref(cv), ctypes.byref(io), s),
+              "mcg_mc_generate_indexed")
+    return IndexedMesh(o["positions"], o["normals"], o["vi2vox"], o["vertex_edge"], o["triangles"], o["tri_cube"], c)
+
+
+def extract_indexed_into(volume, cell, outputs: dict, capacity_vertices, capacity_triangles, ctx=None, stream=None):
+    """Asynchronous indexed extraction into preallocated buffers (keys as
+    IndexedMesh's attributes); counts(ctx) afterwards gives the sizes."""
+    ctx = ctx or default_context(volume.device.index)
+    cv = _cvol(volume, cell)
+    io = _indexed_out(outputs, capacity_vertices, capacity_triangles)
+    ctx.check(_lib.mcg_mc_extract_indexed(ctx.handle, ctypes.byref(cv), ctypes.byref(io), _stream(stream)),
+              "mcg_mc_extract_indexed")
+    return ctx
+
+
 def extract_into(volume, cell, outputs: dict, capacity, ctx=None, stream=None):
     """Asynchronous extraction into preallocated buffers (no host sync).
 

@@ -26,6 +26,12 @@ class MeshOut(ctypes.Structure):
                 ("ver_voxel", c_void_p), ("tri_cube", c_void_p), ("capacity_vertices", c_int64)]
 
 
+class IndexedOut(ctypes.Structure):
+    _fields_ = [("positions", c_void_p), ("normals", c_void_p), ("vi2vox", c_void_p), ("vertex_edge", c_void_p),
+                ("triangles", c_void_p), ("tri_cube", c_void_p), ("capacity_vertices", c_int64),
+                ("capacity_triangles", c_int64)]
+
+
 class MeshCounts(ctypes.Structure):
     _fields_ = [("occupied", c_int64), ("triangles", c_int64), ("vertices", c_int64),
                 ("active_bricks", c_int64), ("status", c_int32), ("reserved", c_int32)]
@@ -51,6 +57,9 @@ SIGNATURES = {
     "mcg_mc_classify": (c_int, [c_void_p, ctypes.POINTER(Volume), c_void_p]),
     "mcg_mc_counts": (c_int, [c_void_p, ctypes.POINTER(MeshCounts)]),
     "mcg_mc_generate": (c_int, [c_void_p, ctypes.POINTER(Volume), ctypes.POINTER(MeshOut), c_void_p]),
+    "mcg_mc_classify_indexed": (c_int, [c_void_p, ctypes.POINTER(Volume), c_void_p]),
+    "mcg_mc_generate_indexed": (c_int, [c_void_p, ctypes.POINTER(Volume), ctypes.POINTER(IndexedOut), c_void_p]),
+    "mcg_mc_extract_indexed": (c_int, [c_void_p, ctypes.POINTER(Volume), ctypes.POINTER(IndexedOut), c_void_p]),
     "mcg_mc_extract": (c_int, [c_void_p, ctypes.POINTER(Volume), ctypes.POINTER(MeshOut), c_void_p]),
     "mcg_mc_classify_batched": (c_int, [c_void_p, ctypes.POINTER(Volume), c_int32, c_void_p]),
     "mcg_mc_counts_batched": (c_int, [c_void_p, ctypes.POINTER(MeshCounts), c_int32]),

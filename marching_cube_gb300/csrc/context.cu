@@ -65,6 +65,9 @@ mcg_status mcg_destroy(mcg_context *ctx) {
     cudaFree(ctx->brick_occ);
     cudaFree(ctx->brick_vofs);
     cudaFree(ctx->active);
+    cudaFree(ctx->brick_uniq);
+    cudaFree(ctx->brick_uofs);
+    cudaFree(ctx->edge_map);
     cudaFree(ctx->d_totals);
     if (ctx->h_totals) cudaFreeHost(ctx->h_totals);
     if (ctx->counts_ready) cudaEventDestroy(ctx->counts_ready);

@@ -44,21 +44,15 @@
 #include <stdlib.h>
 #include <string.h>
 
-#include "mc_tables.h"
-#include "mcg_internal.h"
-#include "tma.cuh"
-#include "unpack.h"
+#include "mc_common.cuh"
 
 namespace mcg {
 namespace {
 
-constexpr int BX = 32, BY = 8, BZ = 8;
-constexpr int BRICK_CUBES = BX * BY * BZ;  // 2048
 constexpr int THREADS = 256;
 constexpr int WARPS = THREADS / 32;
 constexpr int ROWS = (BY + 1) * (BZ + 1);  // voxel rows feeding one brick: 81
 constexpr int CUBE_ROWS = BY * BZ;         // 64
-constexpr int CHUNK = 256;                 // bricks per scan chunk
 
 // classify tile: voxels [x0, x0+36) x [y0, y0+9) x [z0, z0+9)
 constexpr int CTX = 36, CTY = BY + 1, CTZ = BZ + 1;
@@ -70,82 +64,6 @@ constexpr int TXO = 0, TYO = 0, TZO = 0;
 constexpr int TX = BX + 4, TY = BY + 2, TZ = BZ + 2;
 constexpr int GTILE = TX * TY * TZ;
 constexpr int GSTAGES = 2;
-
-__host__ __device__ constexpr int pad128(int bytes) { return (bytes + 127) / 128 * 128; }
-
-// corner c: x = {0,1,1,0,0,1,1,0}, y = {0,0,1,1,0,0,1,1}, z = {0,0,0,0,1,1,1,1}
-// (corner order of cu_marching_cubes_v1.cu:74-81)
-__device__ __forceinline__ int c_cx(int c) { return (c ^ (c >> 1)) & 1; }
-__device__ __forceinline__ int c_cy(int c) { return (c >> 1) & 1; }
-__device__ __forceinline__ int c_cz(int c) { return c >> 2; }
-// edge e: first corner {0..7,0,1,2,3}, second {1,2,3,0,5,6,7,4,4,5,6,7}
-// (vertex_interp argument order, :304-315)
-__device__ __forceinline__ int c_ea(int e) { return e < 8 ? e : e - 8; }
-__device__ __forceinline__ int c_eb(int e) { return e < 8 ? (e & 4) | ((e + 1) & 3) : e - 4; }
-__constant__ signed char c_tri[256][16];
-__constant__ unsigned char c_nverts[256];
-
-// ---- voxel traits -----------------------------------------------------------
-template <int VT>
-struct Vox;
-
-template <>
-struct Vox<MCG_VOXEL_SHORT2> {
-    using T = short2;  // {tsdf, w}: w is a ushort, only ==0 is tested
-    static constexpr int bytes = 4;
-    static __device__ __forceinline__ T fill() { return make_short2(0, 0); }
-    static __device__ __forceinline__ bool neg(T v) { return v.x < 0; }
-    static __device__ __forceinline__ bool w0(T v) { return v.y == 0; }
-    // d_unpack_tsdf (cu_kinect_fusion_v1.h:253-256), division-free and exact
-    static __device__ __forceinline__ float f(T v) { return mcg_unpack_tsdf(v.x); }
-    static __device__ __forceinline__ bool sentinel(T v) { return v.x == kMaxTsdf || v.x == -kMaxTsdf; }
-    static __device__ __forceinline__ short tsdf(T v) { return v.x; }
-    static __device__ __forceinline__ short wt(T v) { return v.y; }
-};
-
-template <>
-struct Vox<MCG_VOXEL_FLOAT2> {
-    using T = float2;
-    static constexpr int bytes = 8;
-    static __device__ __forceinline__ T fill() { return make_float2(0.f, 0.f); }
-    static __device__ __forceinline__ bool neg(T v) { return v.x < 0.f; }
-    static __device__ __forceinline__ bool w0(T v) { return v.y == 0.f; }
-    static __device__ __forceinline__ float f(T v) { return v.x; }
-    static __device__ __forceinline__ bool sentinel(T) { return false; }
-    static __device__ __forceinline__ short tsdf(T) { return 0; }
-    static __device__ __forceinline__ short wt(T) { return 0; }
-};
-
-__device__ __forceinline__ long long lin3(int nx, int ny, int x, int y, int z) {
-    return ((long long)z * ny + y) * nx + x;
-}
-
-struct BrickPos {
-    int x0, y0, z0;
-};
-
-__device__ __forceinline__ BrickPos brick_pos(long long b, int nbx, int nby) {
-    BrickPos p;
-    const long long r = b / nbx;
-    p.x0 = (int)(b % nbx) * BX;
-    p.y0 = (int)(r % nby) * BY;
-    p.z0 = (int)(r / nby) * BZ;
-    return p;
-}
-
-// Plain-load fill of a (DX, DY, DZ) tile whose origin is (ox, oy, oz);
-// outside the volume reads as the zero voxel, like the TMA fill.
-template <int VT, int DX, int DY, int DZ>
-__device__ __forceinline__ void fill_tile(typename Vox<VT>::T *tile, const typename Vox<VT>::T *__restrict__ vol,
-                                          int nx, int ny, int nz, int ox, int oy, int oz) {
-    for (int i = threadIdx.x; i < DX * DY * DZ; i += blockDim.x) {
-        const int lx = i % DX, t = i / DX, ly = t % DY, lz = t / DY;
-        const int gx = ox + lx, gy = oy + ly, gz = oz + lz;
-        typename Vox<VT>::T v = Vox<VT>::fill();
-        if (gx >= 0 && gy >= 0 && gz >= 0 && gx < nx && gy < ny && gz < nz) v = vol[lin3(nx, ny, gx, gy, gz)];
-        tile[i] = v;
-    }
-}
 
 // Row masks: bit k of neg / dead = voxel (x0 + k) of a 33-voxel row is
 // negative / has weight 0, k = 0..32.  One thread builds one row from 16-byte
@@ -200,10 +118,6 @@ struct RowMask<MCG_VOXEL_FLOAT2> {
 // Occupied-cube mask of cube row (cy, cz) of a brick: bit x set iff cube x
 // has a sign change and no weight-0 corner (cu_marching_cubes_v1.cu:74-91,
 // :136 -- every case other than 0 and 255 emits triangles).
-struct CubeRow {
-    unsigned long long a, b, c, d;  // neg masks of rows (y,z), (y+1,z), (y,z+1), (y+1,z+1)
-    unsigned int occ;
-};
 
 __device__ __forceinline__ CubeRow cube_row(const unsigned long long *neg, const unsigned long long *dead, int cy,
                                             int cz, unsigned int valid) {
@@ -424,78 +338,6 @@ __global__ void __launch_bounds__(CHUNK)
         brick_vofs[b] = 3ull * (base_v + wt + it - t);
         if (t) active[base_a + wa + ia - f] = (uint32_t)b;
     }
-}
-
-// ---- normals (cu_kinect_fusion_v1.cu:3146-3225) -----------------------------------
-// cu_math_functions.h:99-103
-__device__ __forceinline__ float bilinear(float v0, float v1, float v2, float v3, float x, float y) {
-    const float a = 1.0f - x, b = 1.0f - y;
-    return v0 * a * b + v1 * x * b + v2 * a * y + v3 * x * y;
-}
-
-// s[] in the reference's sdfs[] slot order; t = fractional position
-__device__ __forceinline__ float3 normal_from_samples(const float s[8], float tx, float ty, float tz) {
-    float3 n;
-    float s1 = bilinear(s[0], s[2], s[3], s[5], ty, tz);
-    float s2 = bilinear(s[1], s[6], s[4], s[7], ty, tz);
-    n.x = s2 - s1;
-    s1 = bilinear(s[0], s[1], s[3], s[4], tx, tz);
-    s2 = bilinear(s[2], s[6], s[5], s[7], tx, tz);
-    n.y = s2 - s1;
-    s1 = bilinear(s[0], s[1], s[2], s[6], tx, ty);
-    s2 = bilinear(s[3], s[4], s[5], s[7], tx, ty);
-    n.z = s2 - s1;
-    // float3_unit (cu_vector_functions.h:258-264)
-    const float norm = sqrtf(n.x * n.x + n.y * n.y + n.z * n.z);
-    if (norm > 1.192092896e-07f || norm < -1.192092896e-07f) {
-        n.x = n.x / norm;
-        n.y = n.y / norm;
-        n.z = n.z / norm;
-    }
-    return n;
-}
-
-// Sample order V000, V100, V110, V010, V001, V101, V111, V011 -> sdfs slot
-// (0, 1, 6, 2, 3, 4, 7, 5); compile-time so the samples stay in registers
-template <int K>
-struct NSlot {
-    static constexpr int v = K == 0 ? 0 : K == 1 ? 1 : K == 2 ? 6 : K == 3 ? 2 : K == 4 ? 3 : K == 5 ? 4 : K == 6 ? 7 : 5;
-};
-__device__ __forceinline__ void put_slot(float s[8], int k, float v) {
-    switch (k) {
-        case 0: s[NSlot<0>::v] = v; break;
-        case 1: s[NSlot<1>::v] = v; break;
-        case 2: s[NSlot<2>::v] = v; break;
-        case 3: s[NSlot<3>::v] = v; break;
-        case 4: s[NSlot<4>::v] = v; break;
-        case 5: s[NSlot<5>::v] = v; break;
-        case 6: s[NSlot<6>::v] = v; break;
-        default: s[NSlot<7>::v] = v; break;
-    }
-}
-
-// Normal at p through global memory, with the reference's linear addressing
-// from the start of slice p_i.z; any sample outside [0, N) (the reference
-// reads outside its allocation there) gives the zero normal.
-template <int VT>
-__device__ float3 normal_global(const typename Vox<VT>::T *__restrict__ vol, int nx, int ny, int nz,
-                                float cell, float px, float py, float pz) {
-    using V = Vox<VT>;
-    const float fx = px / cell, fy = py / cell, fz = pz / cell;
-    const int ix = (int)fx, iy = (int)fy, iz = (int)fz;
-    const long long xy = (long long)nx * ny, N = xy * nz;
-    const long long base = (long long)iz * xy + (long long)iy * nx + ix;
-    const long long off[8] = {0, 1, 1 + (long long)nx, nx, xy, xy + 1, xy + 1 + nx, xy + nx};
-    float s[8];
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-        const long long a = base + off[k];
-        if (a < 0 || a >= N) return make_float3(0.f, 0.f, 0.f);
-        const typename V::T v = vol[a];
-        if (V::sentinel(v)) return make_float3(0.f, 0.f, 0.f);
-        put_slot(s, k, V::f(v));
-    }
-    return normal_from_samples(s, fx - (float)ix, fy - (float)iy, fz - (float)iz);
 }
 
 // ---- pass 2: generate ------------------------------------------------------
@@ -1151,41 +993,6 @@ __global__ void mc_normals_kernel(const typename Vox<VT>::T *__restrict__ vol, i
 }
 
 // ---- host side ----------------------------------------------------------------
-bool g_tables_ready[64] = {false};
-
-cudaError_t upload_tables(int device) {
-    if (device >= 0 && device < 64 && g_tables_ready[device]) return cudaSuccess;
-    cudaError_t e = cudaMemcpyToSymbol(c_tri, mcg_tri_table, sizeof(mcg_tri_table));
-    if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_nverts, mcg_num_verts, sizeof(mcg_num_verts));
-    if (e == cudaSuccess && device >= 0 && device < 64) g_tables_ready[device] = true;
-    return e;
-}
-
-struct Geometry {
-    int nbx, nby, nbz;
-    long long nbricks;
-};
-
-Geometry geometry(int nx, int ny, int nz) {
-    Geometry g;
-    // cubes exist for x < nx-1 etc.
-    g.nbx = (nx - 1 + BX - 1) / BX;
-    g.nby = (ny - 1 + BY - 1) / BY;
-    g.nbz = (nz - 1 + BZ - 1) / BZ;
-    g.nbricks = (long long)g.nbx * g.nby * g.nbz;
-    return g;
-}
-
-bool vol_ok(const mcg_volume *v) {
-    if (!v || !v->data) return false;
-    if (v->nx < 2 || v->ny < 2 || v->nz < 2) return false;
-    if (v->voxel_type != MCG_VOXEL_SHORT2 && v->voxel_type != MCG_VOXEL_FLOAT2) return false;
-    if (!(v->cell > 0.0f)) return false;
-    // brick ids are 32-bit in the active list
-    if (geometry(v->nx, v->ny, v->nz).nbricks >= (1ll << 32)) return false;
-    return true;
-}
-
 struct Scratch {
     uint32_t *tris;
     uint32_t *chunk;  // 3 per chunk of CHUNK bricks: triangles, active bricks, occupied cubes
@@ -1193,17 +1000,6 @@ struct Scratch {
     uint32_t *active;
     MeshTotals *totals;
 };
-
-template <class K>
-int occupancy(K kernel, int threads, size_t smem) {
-    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    int o = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kernel, threads, smem) != cudaSuccess || o < 1) {
-        cudaGetLastError();
-        o = 1;
-    }
-    return o;
-}
 
 template <int VT, bool TMA, int CSTAGES>
 void launch_classify_s(const CUtensorMap &map, const mcg_volume *vol, const Geometry &g, const Scratch &sc, int sms,
@@ -1342,6 +1138,7 @@ mcg_status mcg_mc_classify(mcg_context *ctx, const mcg_volume *vol, mcg_stream_t
     if (e == cudaSuccess) e = mcg_counts_event(ctx, s);
     if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
     ctx->classified = true;
+    ctx->cls_indexed = false;
     ctx->batch_classified = false;
     ctx->cls_data = vol->data;
     ctx->cls_nx = vol->nx;
@@ -1367,6 +1164,8 @@ mcg_status mcg_mc_counts(mcg_context *ctx, mcg_mesh_counts *out) {
     out->status = MCG_OK;
     if (ctx->h_totals->flags & 1u) out->status = MCG_ERR_TIMEOUT;
     else if (ctx->last_capacity >= 0 && out->vertices > ctx->last_capacity) out->status = MCG_ERR_CAPACITY;
+    else if (ctx->cls_indexed && ctx->last_capacity_tris >= 0 && out->triangles > ctx->last_capacity_tris)
+        out->status = MCG_ERR_CAPACITY;
     out->reserved = 0;
     return (mcg_status)out->status;
 }
@@ -1374,7 +1173,7 @@ mcg_status mcg_mc_counts(mcg_context *ctx, mcg_mesh_counts *out) {
 mcg_status mcg_mc_generate(mcg_context *ctx, const mcg_volume *vol, const mcg_mesh_out *out,
                            mcg_stream_t stream) {
     if (!ctx || !vol_ok(vol) || !out || out->capacity_vertices < 0) return MCG_ERR_INVALID_ARG;
-    if (!ctx->classified || ctx->cls_data != vol->data || ctx->cls_nx != vol->nx ||
+    if (!ctx->classified || ctx->cls_indexed || ctx->cls_data != vol->data || ctx->cls_nx != vol->nx ||
         ctx->cls_ny != vol->ny || ctx->cls_nz != vol->nz || ctx->cls_vtype != vol->voxel_type)
         return MCG_ERR_STATE;
     if (out->capacity_vertices > 0 && !out->soup && !out->soup_normals && !out->vi2vox &&
@@ -1425,8 +1224,8 @@ mcg_status mcg_mc_backward(mcg_context *ctx, const mcg_volume *vol, const float 
                            float *grad_f, mcg_stream_t stream) {
     if (!ctx || !vol_ok(vol) || n_vertices < 0 || !grad_f || (n_vertices > 0 && !grad_pos))
         return MCG_ERR_INVALID_ARG;
-    if (!ctx->classified || ctx->cls_data != vol->data || ctx->cls_nx != vol->nx || ctx->cls_ny != vol->ny ||
-        ctx->cls_nz != vol->nz || ctx->cls_vtype != vol->voxel_type)
+    if (!ctx->classified || ctx->cls_indexed || ctx->cls_data != vol->data || ctx->cls_nx != vol->nx ||
+        ctx->cls_ny != vol->ny || ctx->cls_nz != vol->nz || ctx->cls_vtype != vol->voxel_type)
         return MCG_ERR_STATE;
     if (n_vertices == 0) return MCG_OK;
     cudaStream_t s = (cudaStream_t)stream;

@@ -50,6 +50,14 @@ struct mcg_context {
     size_t brick_vofs_cap = 0;
     uint32_t *active = nullptr;
     size_t active_cap = 0;
+    // indexed extraction: owned vertices and their offsets per brick, and
+    // the vertex id of every grid edge (3 per voxel, written sparsely)
+    uint32_t *brick_uniq = nullptr;
+    size_t brick_uniq_cap = 0;
+    unsigned long long *brick_uofs = nullptr;
+    size_t brick_uofs_cap = 0;
+    uint32_t *edge_map = nullptr;
+    size_t edge_map_cap = 0;
     mcg::MeshTotals *d_totals = nullptr;
     mcg::MeshTotals *h_totals = nullptr;  // pinned
     cudaEvent_t counts_ready = nullptr;
@@ -60,6 +68,8 @@ struct mcg_context {
     const void *cls_data = nullptr;
     int cls_nx = 0, cls_ny = 0, cls_nz = 0, cls_vtype = 0;
     int64_t last_capacity = -1;
+    bool cls_indexed = false;        // the last classify was mcg_mc_classify_indexed
+    int64_t last_capacity_tris = -1;  // indexed: triangle capacity of the last generate
 
     // batched extraction: device tables (volume descriptors, classify and
     // generate tensor maps), pinned staging for them, per-volume sums

@@ -61,6 +61,7 @@ def lib():
             "orc_rle_decode_volume": (i32, [vp, i64, vp, i64, vp, vp]),
             "orc_max_threads": (i32, []),
             "orc_mc_edges": (i64, [vp, i32, i32, i32, i32, vp, vp, i64]),
+            "orc_mc_edge_vertices": (None, [vp, i32, i32, i32, i32, f32, vp, i64, vp, vp, vp]),
             "orc_mc_backward_f64": (i64, [vp, i32, i32, i32, i32, f64, vp, i64, vp]),
             "orc_integrate_seq_f64": (None, [vp, i32, i32, i32, f32, f32, f32, vp, i32, vp, i32, i32, vp, vp, i32,
                                              vp, vp, vp, i32]),
@@ -348,3 +349,34 @@ def integrate_seq_backward_f64(shape, min_t, max_t, grid_s, k, poses, depth, gra
                                          _poses(poses), w, h, _p(depth), _p(normals), 1 if is_dynamic else 0,
                                          _p(gf), _p(gw), _p(gd), _p(gF0), _p(gW0), nthreads)
     return gd, gF0, gW0
+
+
+# ---------------------------------------------------------------------------
+# indexed mesh
+# ---------------------------------------------------------------------------
+def edge_keys(va, vb, nx, ny):
+    """Soup vertex edges (va, vb) -> 3 * linear index of the lower voxel + axis."""
+    lo = np.minimum(va, vb)
+    d = np.abs(vb - va)
+    axis = np.where(d == 1, 0, np.where(d == nx, 1, 2))
+    return 3 * lo + axis
+
+
+def mc_indexed(vol):
+    """Indexed topology of the soup: (keys of the unique vertices sorted,
+    triangles (T, 3) as edge keys in canonical soup order)."""
+    v, vt, nx, ny, nz = _vol(vol)
+    va, vb = mc_edges(v)
+    k = edge_keys(va, vb, nx, ny)
+    return np.unique(k), k.reshape(-1, 3)
+
+
+def mc_edge_vertices(vol, cell, keys):
+    vol, vt, nx, ny, nz = _vol(vol)
+    keys = np.ascontiguousarray(keys, np.int64)
+    n = len(keys)
+    pos = np.zeros((n, 3), np.float32)
+    nrm = np.zeros((n, 3), np.float32)
+    v2v = np.zeros((n, 3), np.int32)
+    lib().orc_mc_edge_vertices(_p(vol), vt, nx, ny, nz, float(cell), _p(keys), n, _p(pos), _p(nrm), _p(v2v))
+    return pos, nrm, v2v

@@ -919,3 +919,28 @@ void orc_integrate_seq_backward_f64(const float *vol0, int nx, int ny, int nz, f
     }
     free(ds);
 }
+
+/* ------------------------------------------------------------------------ */
+/* indexed mesh vertices (no counterpart in the reference): the vertex of    */
+/* grid edge `key` = 3 * lin(x, y, z) + axis, interpolated from the lower    */
+/* voxel to the upper one with vertex_interp (:256-264), FP32 mirror.        */
+/* ------------------------------------------------------------------------ */
+void orc_mc_edge_vertices(const void *vol, int vtype, int nx, int ny, int nz, float cell, const int64_t *keys,
+                          int64_t n, float *pos, float *normals, int32_t *vi2vox) {
+    for (int64_t i = 0; i < n; ++i) {
+        int64_t k = keys[i];
+        int axis = (int)(k % 3);
+        int64_t li = k / 3;
+        int x = (int)(li % nx), y = (int)((li / nx) % ny), z = (int)(li / ((int64_t)nx * ny));
+        int dx = axis == 0, dy = axis == 1, dz = axis == 2;
+        float f0 = vox_f(vol, vtype, li);
+        float f1 = vox_f(vol, vtype, lin(nx, ny, x + dx, y + dy, z + dz));
+        float t = (0.0f - f0) / (f1 - f0 + 1e-15f);
+        float P[3] = {interp1(node(x, cell), node(x + dx, cell), t), interp1(node(y, cell), node(y + dy, cell), t),
+                      interp1(node(z, cell), node(z + dz, cell), t)};
+        if (pos) { pos[3 * i] = P[0]; pos[3 * i + 1] = P[1]; pos[3 * i + 2] = P[2]; }
+        if (vi2vox)
+            for (int d = 0; d < 3; ++d) vi2vox[3 * i + d] = (int)floorf(P[d] / cell - 0.5f);
+        if (normals) orc_surface_normal(vol, vtype, nx, ny, nz, cell, P, normals + 3 * i);
+    }
+}

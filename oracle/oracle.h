@@ -119,6 +119,12 @@ void orc_integrate_seq_backward_f64(const float *vol0, int nx, int ny, int nz, f
                                     const double *gW_end, double *g_depth, double *gF0, double *gW0,
                                     int nthreads);
 
+/* ---- indexed mesh (no counterpart in the reference) -------------------- */
+/* position / normal / voxel of the vertex on grid edge keys[i] =
+ * 3 * linear index of the lower voxel + axis, interpolated lower -> upper */
+void orc_mc_edge_vertices(const void *vol, int vtype, int nx, int ny, int nz, float cell, const int64_t *keys,
+                          int64_t n, float *pos, float *normals, int32_t *vi2vox);
+
 int orc_max_threads(void);
 
 #ifdef __cplusplus
