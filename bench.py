@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-graph", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-indexed", action="store_true")
+    ap.add_argument("--no-stress", action="store_true")
     return ap.parse_args()
 
 
@@ -255,6 +257,95 @@ def bench_graph(mcg, synthetic, torch, n=256, frames=20):
     graph_ms = e0.elapsed_time(e1) / frames
     return {"volume": [n, n, n], "frames": frames, "eager_ms_per_frame": eager_ms, "graph_ms_per_frame": graph_ms}
 
+
+
+def bench_indexed(mcg, torch, vol, cell, ctx, reps=10):
+    """Indexed extraction (one vertex per crossed grid edge) of the headline
+    volume into preallocated positions + normals + triangles, asynchronous,
+    CUDA-event timed; beside it the output bytes of soup and indexed."""
+    m = mcg.extract_indexed(vol, cell, normals=True, ctx=ctx)
+    nv, nt = m.num_vertices, m.num_triangles
+    out = {"positions": m.positions, "normals": m.normals, "triangles": m.triangles}
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for _ in range(3):
+        mcg.extract_indexed_into(vol, cell, out, nv, nt, ctx=ctx)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(reps):
+        mcg.extract_indexed_into(vol, cell, out, nv, nt, ctx=ctx)
+    e1.record()
+    torch.cuda.synchronize()
+    c = mcg.counts(ctx)
+    assert c["status"] == 0 and c["vertices"] == nv
+    ms = e0.elapsed_time(e1) / reps
+    vox = vol.shape[0] * vol.shape[1] * vol.shape[2]
+    return {"ms": ms, "gvoxels_per_s": vox / (ms * 1e-3) / 1e9, "vertices": nv, "triangles": nt,
+            "out_bytes": nv * 24 + nt * 12, "soup_out_bytes": 3 * nt * (28 + 12),
+            "outputs": "positions + normals (12 B each per vertex) + triangles (12 B)"}
+
+
+def bench_stress(mcg, synthetic, torch, n=1024, reps=5):
+    """1024^3 stress volume (4 GiB short2; 200 spheres + gradient noise):
+    extraction (soup + normals) throughput, the FP32 volume's forward
+    positions and MC adjoint, and the RLE codec's throughput with a
+    bit-exact round trip (lossless variant) and a tsdf-exact one (reference
+    format)."""
+    vol = synthetic.stress_volume(n, seed=0)
+    cell = 1.0 / n
+    ctx = mcg.Context()
+    m = mcg.extract(vol, cell, normals=True, ctx=ctx)
+    nvert = m.num_vertices
+    out = {"soup": m.soup, "normals": m.normals}
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for _ in range(2):
+        mcg.extract_into(vol, cell, out, nvert, ctx=ctx)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(reps):
+        mcg.extract_into(vol, cell, out, nvert, ctx=ctx)
+    e1.record()
+    torch.cuda.synchronize()
+    ext_ms = e0.elapsed_time(e1) / reps
+    res = {"volume": [n, n, n], "triangles": m.num_triangles, "extract_ms": ext_ms,
+           "extract_gvoxels_per_s": n ** 3 / (ext_ms * 1e-3) / 1e9}
+    del m, out
+    # FP32 volume: forward positions + MC adjoint
+    f32 = torch.empty((n, n, n, 2), dtype=torch.float32, device="cuda")
+    f32[..., 0] = vol[..., 0].to(torch.float32) / 32766.0
+    f32[..., 1] = (vol[..., 1] != 0).to(torch.float32)
+    pos = mcg.mesh_positions(f32, cell)
+    g = torch.Generator(device="cuda")
+    g.manual_seed(0)
+    G = torch.randn(pos.shape, device="cuda", generator=g)
+    torch.cuda.synchronize()
+    e0.record()
+    pos = mcg.mesh_positions(f32, cell)
+    e1.record()
+    torch.cuda.synchronize()
+    res["fp32_forward_ms"] = e0.elapsed_time(e1)
+    e0.record()
+    gf = mcg.mc_backward(f32, cell, G)
+    e1.record()
+    torch.cuda.synchronize()
+    res["fp32_mc_adjoint_ms"] = e0.elapsed_time(e1)
+    del f32, pos, G, gf
+    # RLE codec (device volume <-> file image in host memory)
+    v = mcg.Voxel(vol, 5 * cell, 5 * cell, cell)
+    raw = n ** 3 * 4
+    for lossless in (True, False):
+        t0 = time.perf_counter()
+        img = mcg.rle_encode(v, lossless=lossless, ctx=ctx)
+        t1 = time.perf_counter()
+        back = mcg.rle_decode(img, ctx=ctx)
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        key = "rle_lossless" if lossless else "rle_reference_format"
+        exact = bool(torch.equal(back.data, vol)) if lossless else bool(torch.equal(back.data[..., 0], vol[..., 0]))
+        res[key] = {"bytes": len(img), "encode_mb_per_s": raw / (t1 - t0) / 1e6,
+                    "decode_mb_per_s": raw / (t2 - t1) / 1e6,
+                    "round_trip": "bit-exact" if (lossless and exact) else ("tsdf-exact" if exact else "MISMATCH")}
+        del img, back
+    return res
 
 
 def bench_adjoint(mcg, synthetic, torch, n=256, frames=10, reps=5):
@@ -513,6 +604,21 @@ def main():
         except Exception as ex:  # pragma: no cover
             graph = {"error": str(ex)}
 
+    indexed = None
+    if not args.no_indexed:
+        try:
+            indexed = bench_indexed(mcg, torch, v.data, cell, ctx)
+        except Exception as ex:  # pragma: no cover
+            indexed = {"error": str(ex)}
+
+    stress = None
+    if not args.no_stress:
+        try:
+            stress = bench_stress(mcg, synthetic, torch)
+        except Exception as ex:  # pragma: no cover
+            stress = {"error": str(ex)}
+        torch.cuda.empty_cache()
+
     adjoint = None
     if not args.no_adjoint:
         try:
@@ -544,6 +650,8 @@ def main():
         "batched": batched,
         "graph": graph,
         "adjoint": adjoint,
+        "indexed": indexed,
+        "stress": stress,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -699,64 +699,85 @@ def integrate_frames(depth, poses, shape, min_t, max_t, grid_s, k, vol0=None, no
 # ---------------------------------------------------------------------------
 # RLE volume I/O (kf.cu:1303-1600)
 # ---------------------------------------------------------------------------
-def rle_encode(v: Voxel, lossless=False, ctx=None, stream=None) -> bytes:
+def _image_out(cap, fill):
+    """Runs fill(pointer, capacity, size_ref) into a fresh bytearray of cap
+    bytes and returns the bytearray cut to the written size.  (A bytearray
+    is allocated lazily by the OS and cut without a copy; ctypes.string_at
+    takes a 32-bit length and would truncate images of 2 GiB and more.)"""
+    buf = bytearray(cap)
+    view = (ctypes.c_uint8 * cap).from_buffer(buf)
+    size = ctypes.c_int64(0)
+    try:
+        st = fill(ctypes.c_void_p(ctypes.addressof(view)), cap, ctypes.byref(size))
+    finally:
+        del view
+    del buf[size.value:]
+    return st, buf
+
+
+def _image_in(image):
+    """(pointer, length, keep-alive) of a bytes-like file image."""
+    import numpy as np
+    arr = np.frombuffer(image, dtype=np.uint8)
+    return arr.ctypes.data_as(ctypes.c_void_p), arr.size, arr
+
+
+def rle_encode(v: Voxel, lossless=False, ctx=None, stream=None) -> bytearray:
     """Encode a short2 volume into the reference's RLE file image."""
     if v.data.dtype != torch.int16:
         raise TypeError("RLE volumes are short2 (int16) volumes")
     ctx = ctx or default_context(v.data.device.index)
     nx, ny, nz = v.size
-    cap = _lib.mcg_rle_bound(nx, ny, nz)
-    buf = (ctypes.c_uint8 * cap)()
-    size = ctypes.c_int64(0)
-    ctx.check(_lib.mcg_rle_encode(ctx.handle, _ptr(v.data), nx, ny, nz, v.min_t, v.max_t, v.grid_s,
-                                  1 if lossless else 0, buf, cap, ctypes.byref(size), _stream(stream)),
-              "mcg_rle_encode")
-    return ctypes.string_at(buf, size.value)
+    st, img = _image_out(_lib.mcg_rle_bound(nx, ny, nz), lambda p, cap, size: _lib.mcg_rle_encode(
+        ctx.handle, _ptr(v.data), nx, ny, nz, v.min_t, v.max_t, v.grid_s, 1 if lossless else 0, p, cap, size,
+        _stream(stream)))
+    ctx.check(st, "mcg_rle_encode")
+    return img
 
 
-def rle_header(image: bytes):
+def rle_header(image):
     dims = (ctypes.c_int32 * 3)()
     params = (ctypes.c_float * 3)()
-    st = _lib.mcg_rle_header(image, len(image), dims, params)
+    p, n, _keep = _image_in(image)
+    st = _lib.mcg_rle_header(p, n, dims, params)
     if st != MCG_OK:
         raise MCGError(st, "mcg_rle_header")
     return (dims[0], dims[1], dims[2]), (params[0], params[1], params[2])
 
 
-def rle_decode(image: bytes, device=None, ctx=None, stream=None) -> Voxel:
+def rle_decode(image, device=None, ctx=None, stream=None) -> Voxel:
     (nx, ny, nz), (min_t, max_t, grid_s) = rle_header(image)
     if device is None:
         device = torch.device("cuda", torch.cuda.current_device())
     data = torch.empty((nz, ny, nx, 2), dtype=torch.int16, device=device)
     ctx = ctx or default_context(data.device.index)
-    ctx.check(_lib.mcg_rle_decode(ctx.handle, image, len(image), _ptr(data), nx * ny * nz, _stream(stream)),
-              "mcg_rle_decode")
+    p, n, _keep = _image_in(image)
+    ctx.check(_lib.mcg_rle_decode(ctx.handle, p, n, _ptr(data), nx * ny * nz, _stream(stream)), "mcg_rle_decode")
     return Voxel(data, min_t, max_t, grid_s)
 
 
-def rle_encode_host(vol, min_t, max_t, grid_s, lossless=False) -> bytes:
+def rle_encode_host(vol, min_t, max_t, grid_s, lossless=False) -> bytearray:
     """Encode a host (numpy) short2 volume (nz, ny, nx, 2) int16; no GPU needed."""
     import numpy as np
     vol = np.ascontiguousarray(vol, dtype=np.int16)
     if vol.ndim != 4 or vol.shape[3] != 2:
         raise ValueError("volume must be (nz, ny, nx, 2)")
     nz, ny, nx, _ = vol.shape
-    cap = _lib.mcg_rle_bound(nx, ny, nz)
-    buf = (ctypes.c_uint8 * cap)()
-    size = ctypes.c_int64(0)
-    st = _lib.mcg_rle_encode_host(vol.ctypes.data_as(ctypes.c_void_p), nx, ny, nz, float(min_t), float(max_t),
-                                  float(grid_s), 1 if lossless else 0, buf, cap, ctypes.byref(size))
+    st, img = _image_out(_lib.mcg_rle_bound(nx, ny, nz), lambda p, cap, size: _lib.mcg_rle_encode_host(
+        vol.ctypes.data_as(ctypes.c_void_p), nx, ny, nz, float(min_t), float(max_t), float(grid_s),
+        1 if lossless else 0, p, cap, size))
     if st != MCG_OK:
         raise MCGError(st, "mcg_rle_encode_host")
-    return ctypes.string_at(buf, size.value)
+    return img
 
 
-def rle_decode_host(image: bytes):
+def rle_decode_host(image):
     """Decode a file image into a host numpy volume; returns (vol, (min_t, max_t, grid_s))."""
     import numpy as np
     (nx, ny, nz), params = rle_header(image)
     vol = np.empty((nz, ny, nx, 2), np.int16)
-    st = _lib.mcg_rle_decode_host(image, len(image), vol.ctypes.data_as(ctypes.c_void_p), nx * ny * nz)
+    p, n, _keep = _image_in(image)
+    st = _lib.mcg_rle_decode_host(p, n, vol.ctypes.data_as(ctypes.c_void_p), nx * ny * nz)
     if st != MCG_OK:
         raise MCGError(st, "mcg_rle_decode_host")
     return vol, params

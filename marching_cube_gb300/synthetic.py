@@ -11,6 +11,10 @@ sizes and value ranges of the workloads:
                   1.5 m (pinhole 525/525/319.5/239.5, 640x480), Gaussian
                   noise sigma 2 mm, uint16 millimetres
   random_volume   small random short2 volumes for exhaustive parity cases
+  stress_volume   1024^3 short2: union of 200 spheres (r 2-8 % of the side)
+                  plus 3-octave gradient noise of amplitude 0.2 voxel added
+                  to the signed distance before quantising (trunc 5 voxels,
+                  scale 32767, weights uniform in [1, 128])
   blended_spheres smooth union (quadratic polynomial smooth-min, blend
                   radius k = 0.06 m) of 8 spheres in a 1 m cube, float depth
                   frames sphere-traced from a camera orbiting at 1.2 m
@@ -54,6 +58,80 @@ def random_volume(shape, seed=0, p_zero_weight=0.05, sentinel_frac=0.1):
     w = rng.integers(1, 65536, size=(nz, ny, nx), dtype=np.int64)
     w[rng.random((nz, ny, nx)) < p_zero_weight] = 0
     return np.stack([t.astype(np.int16), w.astype(np.uint16).view(np.int16)], axis=-1)
+
+
+def _mix32(h):
+    """32-bit integer hash (multiply-xorshift) on int64 tensors holding
+    values in [0, 2^32)."""
+    m = 0xFFFFFFFF
+    h = ((h ^ (h >> 16)) * 0x7FEB352D) & m
+    h = ((h ^ (h >> 15)) * 0x846CA68B) & m
+    return h ^ (h >> 16)
+
+
+def gradient_noise(x, y, z, seed=0):
+    """Perlin-style gradient noise (quintic fade 6t^5 - 15t^4 + 10t^3, one
+    hashed unit gradient per lattice point) at float tensors x, y, z; roughly
+    in [-1, 1]."""
+    xi, yi, zi = torch.floor(x), torch.floor(y), torch.floor(z)
+    fx, fy, fz = x - xi, y - yi, z - zi
+    xi, yi, zi = xi.to(torch.int64), yi.to(torch.int64), zi.to(torch.int64)
+
+    def fade(t):
+        return t * t * t * (t * (t * 6.0 - 15.0) + 10.0)
+
+    u, v, w = fade(fx), fade(fy), fade(fz)
+    out = torch.zeros_like(x)
+    for c in range(8):
+        cx, cy, cz = c & 1, (c >> 1) & 1, c >> 2
+        h = _mix32(((xi + cx) * 73856093 ^ (yi + cy) * 19349663 ^ (zi + cz) * 83492791 ^ (seed * 2654435761))
+                   & 0xFFFFFFFF)
+        # gradient from three hashed bytes, normalised
+        gx = ((h & 0xFF).to(x.dtype) / 127.5) - 1.0
+        gy = (((h >> 8) & 0xFF).to(x.dtype) / 127.5) - 1.0
+        gz = (((h >> 16) & 0xFF).to(x.dtype) / 127.5) - 1.0
+        gn = torch.rsqrt(gx * gx + gy * gy + gz * gz + 1e-12)
+        dot = (gx * (fx - cx) + gy * (fy - cy) + gz * (fz - cz)) * gn
+        wgt = (u if cx else 1.0 - u) * (v if cy else 1.0 - v) * (w if cz else 1.0 - w)
+        out += wgt * dot
+    return out
+
+
+def stress_volume(n=1024, seed=0, n_spheres=200, trunc=5.0, noise_amp=0.2, slab=32, device="cuda"):
+    """(n, n, n, 2) int16 volume built slab by slab on `device`: signed
+    distance (voxel units, voxel centres at i + 0.5) to the union of
+    n_spheres spheres, plus 3 octaves of gradient noise (periods 32, 16, 8
+    voxels, weights 4:2:1) scaled to amplitude noise_amp voxel; tsdf =
+    trunc(clamp(sd / trunc, -1, 1) * 32767); w uniform in [1, 128]."""
+    rng = np.random.default_rng(seed)
+    c = rng.uniform(0.05, 0.95, size=(n_spheres, 3)) * n
+    r = rng.uniform(0.02, 0.08, size=n_spheres) * n
+    dev = torch.device(device)
+    out = torch.empty((n, n, n, 2), dtype=torch.int16, device=dev)
+    g = torch.Generator(device=dev)
+    ii = torch.arange(n, device=dev, dtype=torch.float32) + 0.5
+    for z0 in range(0, n, slab):
+        z1 = min(n, z0 + slab)
+        zz = torch.arange(z0, z1, device=dev, dtype=torch.float32)[:, None, None] + 0.5
+        yy = ii[None, :, None]
+        xx = ii[None, None, :]
+        sd = torch.full((z1 - z0, n, n), float(trunc) + 1.0, device=dev)
+        # only spheres that can come within trunc + 1 of the slab matter after clamping
+        near = np.flatnonzero((c[:, 2] + r + trunc + 1 >= z0) & (c[:, 2] - r - trunc - 1 <= z1))
+        for k in near:
+            d = torch.sqrt((xx - float(c[k, 0])) ** 2 + (yy - float(c[k, 1])) ** 2 + (zz - float(c[k, 2])) ** 2)
+            torch.minimum(sd, d - float(r[k]), out=sd)
+        noise = torch.zeros_like(sd)
+        X, Y, Z = xx.expand_as(sd), yy.expand_as(sd), zz.expand_as(sd)
+        for o, (period, wgt) in enumerate(((32.0, 4.0), (16.0, 2.0), (8.0, 1.0))):
+            noise += wgt * gradient_noise(X / period, Y / period, Z / period, seed=seed * 7 + o)
+        sd += noise * (noise_amp / 7.0)
+        t = torch.trunc(torch.clamp(sd / trunc, -1.0, 1.0) * 32767.0).to(torch.int16)
+        g.manual_seed(seed * 100003 + z0)
+        w = torch.randint(1, 129, t.shape, generator=g, device=dev, dtype=torch.int32).to(torch.int16)
+        out[z0:z1, ..., 0] = t
+        out[z0:z1, ..., 1] = w
+    return out
 
 
 def batch_volumes(n=64, seed=0, lo=32, hi=256, device="cpu", trunc=5.0):

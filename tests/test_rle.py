@@ -85,3 +85,19 @@ def test_malformed_images_rejected(mcg):
     bad[44:46] = (0 | (1 << 14)).to_bytes(2, "little")  # zero-length run in slice 0
     with pytest.raises(mcg.MCGError):
         mcg.rle_decode_host(bytes(bad))
+
+
+def test_image_larger_than_2gib_round_trips(mcg):
+    """A file image past 2^31 bytes (every voxel a 6-byte literal) encodes and
+    decodes whole."""
+    import numpy as np
+    nz = (2 ** 31) // (6 * 1024 * 1024) + 2
+    rng = np.random.default_rng(0)
+    vol = np.empty((nz, 1024, 1024, 2), np.int16)
+    vol[..., 0] = rng.integers(-32767, 32768, size=(nz, 1024, 1024), dtype=np.int16)
+    vol[..., 1] = 1
+    vol[:, :, 1::2, 0] = vol[:, :, 0::2, 0] ^ 1  # no two neighbours share a tsdf
+    img = mcg.rle_encode_host(vol, 0.01, 0.01, 0.002, lossless=True)
+    assert len(img) > 2 ** 31
+    back, _ = mcg.rle_decode_host(img)
+    assert np.array_equal(back, vol)
