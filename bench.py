@@ -41,8 +41,8 @@ UNIT = "Gvoxels/s"
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
-    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=N_VOX, help="volume edge (default 512)")
     ap.add_argument("--frames", type=int, default=N_FRAMES)
@@ -77,24 +77,37 @@ class Clocks:
         self._t = None
 
     def _run(self):
-        while not self._stop.is_set():
-            try:
-                out = subprocess.run(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
-                                      "--format=csv,noheader,nounits"], capture_output=True, text=True,
-                                     timeout=5).stdout.strip()
-                if out:
-                    self.rows.append([x.strip() for x in out.split(",")])
-            except Exception:
-                pass
-            self._stop.wait(0.2)
+        # one nvidia-smi in loop mode (-lms) rather than a process per sample
+        try:
+            self._p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                        "--format=csv,noheader,nounits", "-lms", "50"],
+                                       stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self._p = None
+            return
+        for line in self._p.stdout:
+            if self._stop.is_set():
+                break
+            line = line.strip()
+            if line:
+                self.rows.append([x.strip() for x in line.split(",")])
 
     def __enter__(self):
+        self._p = None
         self._t = threading.Thread(target=self._run, daemon=True)
         self._t.start()
+        time.sleep(0.3)  # the sampler is running before the timed region starts
         return self
 
     def __exit__(self, *a):
         self._stop.set()
+        p = self._p
+        if p is not None and p.poll() is None:
+            p.terminate()  # this sampler's own process, by handle
+            try:
+                p.wait(timeout=5)
+            except Exception:
+                p.kill()
         if self._t:
             self._t.join(timeout=10)
 

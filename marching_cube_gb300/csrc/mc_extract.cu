@@ -8,26 +8,28 @@
 //
 // Work is organised in bricks of 32x8x8 cubes.
 //
-// Pass 1 (classify) streams the whole volume once: each persistent CTA keeps
-// a 4-stage pipeline of brick tiles (brick + 1-voxel halo, 36x9x9 voxels)
-// loaded by TMA (cp.async.bulk.tensor.3d, completion on an mbarrier that one
-// thread polls with a time bound).  Each of 81 threads turns one 33-voxel row
-// of the tile into two bit masks (tsdf < 0, weight == 0) from 16-byte
-// shared-memory loads; a cube row of 32 cubes is then classified with a
+// Pass 1 (classify) streams the whole volume once.  Persistent CTAs take work
+// items (groups of 2 bricks adjacent in x) from a counter; each item's voxels
+// (68x9x9: the bricks plus a 1-voxel halo, x padded to 16 bytes) arrive by
+// TMA (cp.async.bulk.tensor.3d, completion on an mbarrier that one thread
+// polls with a time bound) into a 2-stage ring.  A tile whose voxels all have
+// one sign is settled by one OR/AND pass; otherwise threads turn its rows
+// into two bit masks per 33 voxels (tsdf < 0, weight == 0) from 16-byte
+// shared-memory loads, and a cube row of 32 cubes is classified with a
 // handful of 64-bit AND/OR operations on four row masks and __popc, so only
 // occupied cubes (a few per mille of a fusion volume) ever look up a table.
-// Output: triangle and occupied-cube counts per brick.
+// Output: triangle counts per brick and per-chunk sums.
 //
-// A single-CTA scan turns brick counts into 64-bit soup offsets and a list of
-// active bricks in brick order.
+// A multi-CTA scan (one CTA per chunk of 256 bricks) turns brick counts into
+// 64-bit soup offsets and a list of active bricks in brick order.
 //
-// Pass 2 (generate) visits only active bricks, with a 2-stage TMA prefetch of
-// the brick + halo (-4/-1/-1 .. +4/+2/+2 voxels, 40x11x11, x rounded down to a
-// 16-byte boundary).  The same masks give a compact list of occupied cubes
-// with their vertex offsets; each thread then emits one soup vertex (owning
-// cube by binary search over the list), computes the fused normal from the
-// tile, and the 28-byte records go out through a per-warp shared-memory stage
-// as full coalesced lines.
+// Pass 2 (generate) visits only active bricks (taken from a counter), with a
+// 2-stage TMA prefetch of the brick + halo (36x10x10 voxels).  The same masks
+// give a compact list of occupied cubes with their vertex offsets; each
+// thread then emits one soup vertex (owning cube through a vertex -> cube map
+// or a binary search over the list), computes the fused normal from the tile,
+// and the 28-byte records go out through a per-warp shared-memory stage as
+// full coalesced lines.
 //
 // When TMA cannot describe the volume (x row not a multiple of 16 bytes or an
 // unaligned base) the same kernels fill the tiles with plain loads.
@@ -150,16 +152,38 @@ __device__ __forceinline__ unsigned int valid_mask(int x0, int nx) {
 // ---- pass 1: classify ------------------------------------------------------
 constexpr int CTHREADS = 128;
 
-template <int VT, int CSTAGES>
-struct ClsSmem {
-    static constexpr int STAGE_BYTES = pad128(CTILE * Vox<VT>::bytes);
-    unsigned char tiles[CSTAGES][STAGE_BYTES];
-    unsigned long long neg[ROWS], dead[ROWS];
-    uint64_t bars[CSTAGES];
-    unsigned int red[2][2];
-    unsigned char ntri[256];
-    int abort;
-};
+// True when the tile holds both negative and non-negative voxels.  Most
+// bricks of a fusion volume lie wholly on one side of the surface (or in
+// unobserved space, all -32766), and no cube of such a brick changes sign, so
+// one OR / AND pass over the tile's sign bits settles them before any mask
+// work.  Called by every thread; contains a barrier.
+template <int VT, int NVOX = CTILE, class Smem>
+__device__ __forceinline__ bool tile_mixed(Smem &S, const typename Vox<VT>::T *tile) {
+    static_assert(NVOX * Vox<VT>::bytes % 16 == 0, "tile is a whole number of 16-byte words");
+    constexpr int NQ = NVOX * Vox<VT>::bytes / 16;
+    const uint4 *q = reinterpret_cast<const uint4 *>(tile);
+    unsigned int neg_any = 0, pos_any = 0;
+    for (int i = threadIdx.x; i < NQ; i += blockDim.x) {
+        const uint4 v = q[i];
+        if (VT == MCG_VOXEL_SHORT2) {
+            // bit 15 of each word is the tsdf sign
+            neg_any |= v.x | v.y | v.z | v.w;
+            pos_any |= ~(v.x & v.y & v.z & v.w);
+        } else {
+            // x and z are the tsdf of two voxels; -0.0f is not negative
+            const bool n0 = __uint_as_float(v.x) < 0.f, n1 = __uint_as_float(v.z) < 0.f;
+            neg_any |= (unsigned int)(n0 | n1) << 15;
+            pos_any |= (unsigned int)(!n0 | !n1) << 15;
+        }
+    }
+    neg_any = __reduce_or_sync(0xffffffffu, neg_any & 0x8000u);
+    pos_any = __reduce_or_sync(0xffffffffu, pos_any & 0x8000u);
+    if ((threadIdx.x & 31) == 0) S.mix[threadIdx.x >> 5] = (neg_any ? 1u : 0u) | (pos_any ? 2u : 0u);
+    __syncthreads();
+    unsigned int m = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m |= S.mix[w];
+    return m == 3u;
+}
 
 // Pass-1 work on one brick tile: row masks, cube rows, per-warp sums into
 // S.red (read after the caller's next __syncthreads).  Called by every
@@ -192,58 +216,156 @@ __device__ __forceinline__ void classify_brick(Smem &S, const typename Vox<VT>::
         }
 }
 
-template <int VT, bool TMA, int CSTAGES>
-__global__ void __launch_bounds__(CTHREADS)
+// next brick of the launch for this CTA (dynamic: CTAs take bricks in order
+// from a counter, so a CTA that drew cheap bricks takes more), -1 when done
+__device__ __forceinline__ long long next_brick(unsigned int *ticket, long long n) {
+    const unsigned int t = atomicAdd(ticket, 1u);
+    return (long long)t < n ? (long long)t : -1ll;
+}
+
+// Single-volume classify: one work item is a group of G bricks adjacent in x
+// whose tiles share one TMA box of (32 G + 4) x 9 x 9 voxels -- wider boxes
+// keep more of each DRAM row per request (a 36-voxel box streams the volume
+// at about 5.7 TB/s, a 132-voxel box at about 7 TB/s on GB300).
+constexpr int CLS_THREADS = 256;
+
+template <int G>
+struct ClsGeom {
+    static constexpr int TXW = BX * G + 4;  // tile width in voxels
+    static constexpr int TILE = TXW * CTY * CTZ;
+};
+
+template <int VT, int G, int CSTAGES>
+struct ClsSmemG {
+    static constexpr int STAGE_BYTES = pad128(ClsGeom<G>::TILE * Vox<VT>::bytes);
+    unsigned char tiles[CSTAGES][STAGE_BYTES];
+    unsigned long long neg[G * ROWS], dead[G * ROWS];  // [brick h of the group][row]
+    uint64_t bars[CSTAGES];
+    long long sitem[CSTAGES];  // work item of each stage's tile, -1 when none
+    unsigned int red[CLS_THREADS / 32][2];
+    unsigned int mix[CLS_THREADS / 32];
+    unsigned char ntri[256];
+    int abort;
+};
+
+template <int VT, bool TMA, int G, int CSTAGES>
+__global__ void __launch_bounds__(CLS_THREADS)
     mc_classify_kernel(const __grid_constant__ CUtensorMap map, const typename Vox<VT>::T *__restrict__ vol,
-                       int nx, int ny, int nz, int nbx, int nby, long long nbricks,
+                       int nx, int ny, int nz, int nbx, int nby, long long nitems, int ngx,
                        uint32_t *__restrict__ brick_tris, uint32_t *__restrict__ chunk,
-                       unsigned int *__restrict__ flags) {
+                       unsigned int *__restrict__ flags, unsigned int *__restrict__ ticket) {
     using V = Vox<VT>;
     using T = typename V::T;
+    using Geo = ClsGeom<G>;
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    ClsSmem<VT, CSTAGES> &S = *reinterpret_cast<ClsSmem<VT, CSTAGES> *>(smem_raw);
-    const int tid = threadIdx.x;
-    const long long stride = gridDim.x;
-    for (int c = tid; c < 256; c += CTHREADS) S.ntri[c] = (c == 0 || c == 255) ? 0 : c_nverts[c] / 3;
+    ClsSmemG<VT, G, CSTAGES> &S = *reinterpret_cast<ClsSmemG<VT, G, CSTAGES> *>(smem_raw);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int c = tid; c < 256; c += CLS_THREADS) S.ntri[c] = (c == 0 || c == 255) ? 0 : c_nverts[c] / 3;
+    auto origin = [&](long long item, int &bx0, int &y0, int &z0) {
+        const long long r = item / ngx;
+        bx0 = (int)(item % ngx) * G;
+        y0 = (int)(r % nby) * BY;
+        z0 = (int)(r / nby) * BZ;
+    };
+    // thread 0 draws the item of the next refill one iteration ahead, so the
+    // counter's round trip overlaps the current item
+    long long pend = -1;
     if (tid == 0) {
         S.abort = 0;
         if (TMA) {
             for (int s = 0; s < CSTAGES; ++s) mbar_init(&S.bars[s], 1);
             fence_barrier_init();
+            bool more = true;
             for (int s = 0; s < CSTAGES; ++s) {
-                const long long b = blockIdx.x + s * stride;
-                if (b >= nbricks) break;
-                const BrickPos bp = brick_pos(b, nbx, nby);
-                mbar_arrive_expect_tx(&S.bars[s], CTILE * V::bytes);
-                tma_load_3d(S.tiles[s], &map, &S.bars[s], bp.x0, bp.y0, bp.z0);
+                const long long it = more ? next_brick(ticket, nitems) : -1ll;
+                more = it >= 0;
+                S.sitem[s] = it;
+                if (!more) continue;
+                int bx0, y0, z0;
+                origin(it, bx0, y0, z0);
+                mbar_arrive_expect_tx(&S.bars[s], Geo::TILE * V::bytes);
+                tma_load_3d(S.tiles[s], &map, &S.bars[s], bx0 * BX, y0, z0);
             }
+            if (more) pend = next_brick(ticket, nitems);
         }
     }
     __syncthreads();
     for (int i = 0;; ++i) {
-        const long long b = blockIdx.x + (long long)i * stride;
-        if (b >= nbricks) break;
         const int s = TMA ? i % CSTAGES : 0;
-        const BrickPos bp = brick_pos(b, nbx, nby);
+        if (!TMA) {
+            if (tid == 0) S.sitem[0] = next_brick(ticket, nitems);
+            __syncthreads();
+        }
+        const long long item = S.sitem[s];
+        if (item < 0) break;  // uniform: every thread reads the same entry
+        int bx0, y0, z0;
+        origin(item, bx0, y0, z0);
+        const int x0 = bx0 * BX;
         T *tile = reinterpret_cast<T *>(S.tiles[s]);
         if (TMA) {
             // one thread polls the barrier; the others wait at __syncthreads
             if (tid == 0 && !mbar_wait(&S.bars[s], (uint32_t)((i / CSTAGES) & 1))) S.abort = 1;
         } else {
-            for (int k = tid; k < CTILE; k += CTHREADS) {
-                const int lx = k % CTX, t = k / CTX, ly = t % CTY, lz = t / CTY;
-                const int gx = bp.x0 + lx, gy = bp.y0 + ly, gz = bp.z0 + lz;
-                T v = V::fill();
-                if (gx < nx && gy < ny && gz < nz) v = vol[lin3(nx, ny, gx, gy, gz)];
-                tile[k] = v;
-            }
+            fill_tile<VT, Geo::TXW, CTY, CTZ>(tile, vol, nx, ny, nz, x0, y0, z0);
         }
         __syncthreads();
         if (S.abort) break;
-        classify_brick<VT>(S, tile, nx, ny, nz, bp);
-        __syncthreads();  // tile s consumed, red[] complete
-        if (tid == 0) {
-            const unsigned int t = S.red[0][0] + S.red[1][0], o = S.red[0][1] + S.red[1][1];
+        const bool mixed = tile_mixed<VT, Geo::TILE>(S, tile);
+        if (mixed) {
+            // row masks: 33 bits of row r starting at voxel x0 + 32 h (16-byte aligned)
+            for (int m = tid; m < G * ROWS; m += CLS_THREADS) {
+                const int h = m / ROWS, r = m - h * ROWS;
+                RowMask<VT>::build(tile + r * Geo::TXW + h * BX, S.neg[m], S.dead[m]);
+            }
+            __syncthreads();
+        }
+        // the tile has been read for the last time: refill its stage now, so the
+        // load overlaps the cube rows below
+        if (TMA && tid == 0) {
+            const long long nit = pend;
+            S.sitem[s] = nit;
+            if (nit >= 0) {
+                int nbx0, ny0, nz0;
+                origin(nit, nbx0, ny0, nz0);
+                mbar_arrive_expect_tx(&S.bars[s], Geo::TILE * V::bytes);
+                tma_load_3d(S.tiles[s], &map, &S.bars[s], nbx0 * BX, ny0, nz0);
+                pend = next_brick(ticket, nitems);
+            }
+        }
+        if (mixed) {
+            if (tid < G * CUBE_ROWS) {
+                // 64 cube rows per brick = two whole warps per brick
+                const int h = tid / CUBE_ROWS, c = tid - h * CUBE_ROWS;
+                const int cy = c & (BY - 1), cz = c / BY;
+                unsigned int tri = 0, occ = 0;
+                if (bx0 + h < nbx && y0 + cy < ny - 1 && z0 + cz < nz - 1) {
+                    const CubeRow cr = cube_row(S.neg + h * ROWS, S.dead + h * ROWS, cy, cz,
+                                                valid_mask(x0 + h * BX, nx));
+                    occ = __popc(cr.occ);
+                    unsigned int mm = cr.occ;
+                    while (mm) {
+                        const int x = __ffs(mm) - 1;
+                        mm &= mm - 1;
+                        tri += S.ntri[cube_index(cr, x)];
+                    }
+                }
+                tri = __reduce_add_sync(0xffffffffu, tri);
+                occ = __reduce_add_sync(0xffffffffu, occ);
+                if (lane == 0) {
+                    S.red[warp][0] = tri;
+                    S.red[warp][1] = occ;
+                }
+            }
+            __syncthreads();  // tile s consumed, red[] complete
+        }
+        if (tid < G && bx0 + tid < nbx) {
+            const int h = tid;
+            unsigned int t = 0, o = 0;
+            if (mixed) {
+                t = S.red[2 * h][0] + S.red[2 * h + 1][0];
+                o = S.red[2 * h][1] + S.red[2 * h + 1][1];
+            }
+            const long long b = ((long long)(z0 / BZ) * nby + y0 / BY) * nbx + bx0 + h;
             brick_tris[b] = t;
             // per-chunk (CHUNK consecutive bricks) sums feed the scan
             if (t) {
@@ -251,15 +373,8 @@ __global__ void __launch_bounds__(CTHREADS)
                 atomicAdd(&chunk[(b / CHUNK) * 3 + 1], 1u);
                 atomicAdd(&chunk[(b / CHUNK) * 3 + 2], o);
             }
-            if (TMA) {
-                const long long nb = b + CSTAGES * stride;
-                if (nb < nbricks) {
-                    const BrickPos np = brick_pos(nb, nbx, nby);
-                    mbar_arrive_expect_tx(&S.bars[s], CTILE * V::bytes);
-                    tma_load_3d(S.tiles[s], &map, &S.bars[s], np.x0, np.y0, np.z0);
-                }
-            }
         }
+        if (!TMA) __syncthreads();  // S.sitem[0] is rewritten at the top
     }
     if (S.abort && tid == 0) {
         atomicOr(flags, 1u);
@@ -702,33 +817,45 @@ __global__ void __launch_bounds__(THREADS, 4) mc_generate_kernel(const __grid_co
         }
     }
     __syncthreads();
-    const unsigned int nactive = p.totals->active_bricks;
+    const long long nactive = p.totals->active_bricks;
+    unsigned int *ticket = &p.totals->gen_ticket;
+    long long pend = -1;  // thread 0: list entry of the next refill, drawn one iteration ahead
     if (TMA && tid == 0) {
+        bool more = true;
         for (int s = 0; s < GSTAGES; ++s) {
-            const unsigned int w = blockIdx.x + s * gridDim.x;
-            if (w >= nactive) break;
-            const long long b = p.active[w];
-            S.sbrick[s] = b;
+            const long long w = more ? next_brick(ticket, nactive) : -1ll;
+            more = w >= 0;
+            S.sbrick[s] = more ? (long long)p.active[w] : -1ll;
+            if (!more) continue;
+            const long long b = S.sbrick[s];
             S.svbase[s] = p.brick_vofs[b];
             const BrickPos bp = brick_pos(b, p.nbx, p.nby);
             mbar_arrive_expect_tx(&S.bars[s], GTILE * V::bytes);
             tma_load_3d(S.tiles[s], &map, &S.bars[s], bp.x0 - TXO, bp.y0 - TYO, bp.z0 - TZO);
         }
+        if (more) pend = next_brick(ticket, nactive);
     }
-    int it = 0;
-    for (unsigned int w = blockIdx.x; w < nactive; w += gridDim.x, ++it) {
+    if (TMA) __syncthreads();
+    for (int it = 0;; ++it) {
         const int s = TMA ? it % GSTAGES : 0;
         const T *tile = reinterpret_cast<const T *>(S.tiles[s]);
         long long b;
         unsigned long long vbase;
         if (TMA) {
+            b = S.sbrick[s];
+            if (b < 0) break;  // uniform
             if (tid == 0 && !mbar_wait(&S.bars[s], (uint32_t)((it / GSTAGES) & 1))) S.abort = 1;
             __syncthreads();
             if (S.abort) break;
-            b = S.sbrick[s];
             vbase = S.svbase[s];
         } else {
-            b = p.active[w];
+            if (tid == 0) {
+                const long long w = next_brick(ticket, nactive);
+                S.sbrick[0] = w >= 0 ? (long long)p.active[w] : -1ll;
+            }
+            __syncthreads();
+            b = S.sbrick[0];
+            if (b < 0) break;
             vbase = p.brick_vofs[b];
             const BrickPos fp = brick_pos(b, p.nbx, p.nby);
             fill_tile<VT, TX, TY, TZ>(reinterpret_cast<T *>(S.tiles[s]), vol, nx, ny, nz, fp.x0 - TXO,
@@ -751,16 +878,19 @@ __global__ void __launch_bounds__(THREADS, 4) mc_generate_kernel(const __grid_co
         }
         __syncthreads();  // tile s, the list and the stage are free again
         if (TMA && tid == 0) {
-            const unsigned int wn = w + GSTAGES * gridDim.x;
-            if (wn < nactive) {
-                const long long nb2 = p.active[wn];
-                S.sbrick[s] = nb2;
+            const long long wn = pend;
+            S.sbrick[s] = wn >= 0 ? (long long)p.active[wn] : -1ll;
+            if (wn >= 0) {
+                pend = next_brick(ticket, nactive);
+                const long long nb2 = S.sbrick[s];
                 S.svbase[s] = p.brick_vofs[nb2];
                 const BrickPos np = brick_pos(nb2, p.nbx, p.nby);
                 mbar_arrive_expect_tx(&S.bars[s], GTILE * V::bytes);
                 tma_load_3d(S.tiles[s], &map, &S.bars[s], np.x0 - TXO, np.y0 - TYO, np.z0 - TZO);
             }
         }
+        // S.sbrick[s] is next read at the top of iteration it + GSTAGES, after the
+        // barriers of iteration it + 1
     }
     if (S.abort && tid == 0) {
         atomicOr(&p.totals->flags, 1u);
@@ -809,6 +939,7 @@ struct ClsSmemMulti {
     unsigned long long neg[ROWS], dead[ROWS];
     uint64_t bars[2];
     unsigned int red[2][2];
+    unsigned int mix[CTHREADS / 32];
     unsigned char ntri[256];
     int svol[2];
     int stma[2];
@@ -869,10 +1000,17 @@ __global__ void __launch_bounds__(CTHREADS)
         }
         __syncthreads();
         if (S.abort) break;
-        classify_brick<VT>(S, tile, d.nx, d.ny, d.nz, bp);
-        __syncthreads();  // tile s consumed, red[] complete
+        const bool mixed = tile_mixed<VT>(S, tile);
+        if (mixed) {
+            classify_brick<VT>(S, tile, d.nx, d.ny, d.nz, bp);
+            __syncthreads();  // tile s consumed, red[] complete
+        }
         if (tid == 0) {
-            const unsigned int t = S.red[0][0] + S.red[1][0], o = S.red[0][1] + S.red[1][1];
+            unsigned int t = 0, o = 0;
+            if (mixed) {
+                t = S.red[0][0] + S.red[1][0];
+                o = S.red[0][1] + S.red[1][1];
+            }
             brick_tris[b] = t;
             if (t) {
                 atomicAdd(&chunk[(b / CHUNK) * 3 + 0], t);
@@ -1001,17 +1139,19 @@ struct Scratch {
     MeshTotals *totals;
 };
 
-template <int VT, bool TMA, int CSTAGES>
+template <int VT, bool TMA, int G, int CSTAGES>
 void launch_classify_s(const CUtensorMap &map, const mcg_volume *vol, const Geometry &g, const Scratch &sc, int sms,
                        cudaStream_t s) {
-    const size_t smem = sizeof(ClsSmem<VT, CSTAGES>);
+    const size_t smem = sizeof(ClsSmemG<VT, G, CSTAGES>);
     static int occ = 0;  // per instantiation; all devices of a run are the same part
-    if (!occ) occ = occupancy(mc_classify_kernel<VT, TMA, CSTAGES>, CTHREADS, smem);
+    if (!occ) occ = occupancy(mc_classify_kernel<VT, TMA, G, CSTAGES>, CLS_THREADS, smem);
+    const int ngx = (g.nbx + G - 1) / G;
+    const long long nitems = (long long)ngx * g.nby * g.nbz;
     long long grid = (long long)sms * occ;
-    if (grid > g.nbricks) grid = g.nbricks;
-    mc_classify_kernel<VT, TMA, CSTAGES><<<(int)grid, CTHREADS, smem, s>>>(
-        map, static_cast<const typename Vox<VT>::T *>(vol->data), vol->nx, vol->ny, vol->nz, g.nbx, g.nby,
-        g.nbricks, sc.tris, sc.chunk, &sc.totals->flags);
+    if (grid > nitems) grid = nitems;
+    mc_classify_kernel<VT, TMA, G, CSTAGES><<<(int)grid, CLS_THREADS, smem, s>>>(
+        map, static_cast<const typename Vox<VT>::T *>(vol->data), vol->nx, vol->ny, vol->nz, g.nbx, g.nby, nitems,
+        ngx, sc.tris, sc.chunk, &sc.totals->flags, &sc.totals->cls_ticket);
 }
 
 // pipeline depth of the classify pass (tile stages per CTA); MCG_CLS_STAGES
@@ -1022,20 +1162,35 @@ int classify_stages() {
         st = 2;
         if (const char *e = getenv("MCG_CLS_STAGES")) {
             const int v = atoi(e);
-            if (v == 2 || v == 3 || v == 4) st = v;
+            if (v == 2 || v == 3) st = v;
         }
     }
     return st;
 }
 
-template <int VT, bool TMA>
-void launch_classify_t(const CUtensorMap &map, const mcg_volume *vol, const Geometry &g, const Scratch &sc, int sms,
+// bricks per classify work item: 2 (a 68-voxel box; measured fastest at 512^3
+// against 1 and 4) when the volume is wide enough for that box, else 1;
+// MCG_CLS_GROUP (1, 2 or 4) overrides it for tuning
+int classify_group(int nx) {
+    static int pref = 0;
+    if (!pref) {
+        pref = 2;
+        if (const char *e = getenv("MCG_CLS_GROUP")) {
+            const int v = atoi(e);
+            if (v == 1 || v == 2 || v == 4) pref = v;
+        }
+    }
+    if (pref == 4 && nx >= ClsGeom<4>::TXW) return 4;
+    if (pref >= 2 && nx >= ClsGeom<2>::TXW) return 2;
+    return 1;
+}
+
+template <int VT, bool TMA, int G>
+void launch_classify_g(const CUtensorMap &map, const mcg_volume *vol, const Geometry &g, const Scratch &sc, int sms,
                        cudaStream_t s) {
     // without TMA only one stage is ever used
-    const int st = TMA ? classify_stages() : 2;
-    if (st == 4) launch_classify_s<VT, TMA, 4>(map, vol, g, sc, sms, s);
-    else if (st == 3) launch_classify_s<VT, TMA, 3>(map, vol, g, sc, sms, s);
-    else launch_classify_s<VT, TMA, 2>(map, vol, g, sc, sms, s);
+    if (TMA && classify_stages() == 3) launch_classify_s<VT, TMA, G, 3>(map, vol, g, sc, sms, s);
+    else launch_classify_s<VT, TMA, G, 2>(map, vol, g, sc, sms, s);
 }
 
 template <int VT, bool TMA, int MODE = 0>
@@ -1052,19 +1207,37 @@ void launch_generate_t(const CUtensorMap &map, const GenParams &p, const Geometr
 long long num_chunks(long long nbricks) { return (nbricks + CHUNK - 1) / CHUNK; }
 
 cudaError_t launch_count_phase(const mcg_volume *vol, const Geometry &g, const Scratch &sc, int sms, cudaStream_t s) {
-    cudaError_t e = cudaMemsetAsync(&sc.totals->flags, 0, sizeof(unsigned int), s);
+    // flags and both work counters
+    cudaError_t e = cudaMemsetAsync(&sc.totals->flags, 0, 3 * sizeof(unsigned int), s);
     if (e == cudaSuccess) e = cudaMemsetAsync(sc.chunk, 0, sizeof(uint32_t) * 3 * num_chunks(g.nbricks), s);
     if (e != cudaSuccess) return e;
     CUtensorMap map;
     const int eb = vol->voxel_type == MCG_VOXEL_SHORT2 ? 4 : 8;
-    const bool tma = encode_volume_map(&map, vol->data, vol->nx, vol->ny, vol->nz, eb, CTX, CTY, CTZ);
+    const int G = classify_group(vol->nx);
+    const bool tma = encode_volume_map(&map, vol->data, vol->nx, vol->ny, vol->nz, eb, G * BX + 4, CTY, CTZ);
     if (!tma) memset(&map, 0, sizeof(map));
     if (vol->voxel_type == MCG_VOXEL_SHORT2) {
-        if (tma) launch_classify_t<MCG_VOXEL_SHORT2, true>(map, vol, g, sc, sms, s);
-        else launch_classify_t<MCG_VOXEL_SHORT2, false>(map, vol, g, sc, sms, s);
+        if (G == 4) {
+            if (tma) launch_classify_g<MCG_VOXEL_SHORT2, true, 4>(map, vol, g, sc, sms, s);
+            else launch_classify_g<MCG_VOXEL_SHORT2, false, 4>(map, vol, g, sc, sms, s);
+        } else if (G == 2) {
+            if (tma) launch_classify_g<MCG_VOXEL_SHORT2, true, 2>(map, vol, g, sc, sms, s);
+            else launch_classify_g<MCG_VOXEL_SHORT2, false, 2>(map, vol, g, sc, sms, s);
+        } else {
+            if (tma) launch_classify_g<MCG_VOXEL_SHORT2, true, 1>(map, vol, g, sc, sms, s);
+            else launch_classify_g<MCG_VOXEL_SHORT2, false, 1>(map, vol, g, sc, sms, s);
+        }
     } else {
-        if (tma) launch_classify_t<MCG_VOXEL_FLOAT2, true>(map, vol, g, sc, sms, s);
-        else launch_classify_t<MCG_VOXEL_FLOAT2, false>(map, vol, g, sc, sms, s);
+        if (G == 4) {
+            if (tma) launch_classify_g<MCG_VOXEL_FLOAT2, true, 4>(map, vol, g, sc, sms, s);
+            else launch_classify_g<MCG_VOXEL_FLOAT2, false, 4>(map, vol, g, sc, sms, s);
+        } else if (G == 2) {
+            if (tma) launch_classify_g<MCG_VOXEL_FLOAT2, true, 2>(map, vol, g, sc, sms, s);
+            else launch_classify_g<MCG_VOXEL_FLOAT2, false, 2>(map, vol, g, sc, sms, s);
+        } else {
+            if (tma) launch_classify_g<MCG_VOXEL_FLOAT2, true, 1>(map, vol, g, sc, sms, s);
+            else launch_classify_g<MCG_VOXEL_FLOAT2, false, 1>(map, vol, g, sc, sms, s);
+        }
     }
     mc_scan_kernel<<<(unsigned int)num_chunks(g.nbricks), CHUNK, 0, s>>>(sc.tris, sc.chunk, g.nbricks, sc.vofs,
                                                                         sc.active, sc.totals);
@@ -1075,6 +1248,10 @@ cudaError_t launch_generate_phase(const mcg_volume *vol, const Geometry &g, cons
                                   const mcg_mesh_out *out, int sms, cudaStream_t s) {
     if (out->ver_voxel) {
         cudaError_t e = cudaMemsetAsync(out->ver_voxel, 0, sizeof(int16_t) * (size_t)vol->nx * vol->ny * vol->nz, s);
+        if (e != cudaSuccess) return e;
+    }
+    {
+        const cudaError_t e = cudaMemsetAsync(&sc.totals->gen_ticket, 0, sizeof(unsigned int), s);
         if (e != cudaSuccess) return e;
     }
     GenParams p;
@@ -1232,6 +1409,8 @@ mcg_status mcg_mc_backward(mcg_context *ctx, const mcg_volume *vol, const float 
     cudaError_t e = cudaSetDevice(ctx->device);
     if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
     const Geometry g = geometry(vol->nx, vol->ny, vol->nz);
+    e = cudaMemsetAsync(&ctx->d_totals->gen_ticket, 0, sizeof(unsigned int), s);
+    if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
     GenParams p;
     memset(&p, 0, sizeof(p));
     p.vol = vol->data;

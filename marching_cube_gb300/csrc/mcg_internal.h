@@ -18,8 +18,11 @@ struct MeshTotals {
     unsigned long long triangles;
     unsigned long long vertices;
     unsigned int active_bricks;
-    unsigned int flags;  // bit 0: a bounded device wait expired (set by the kernels, cleared by the host)
+    unsigned int flags;       // bit 0: a bounded device wait expired (set by the kernels, cleared by the host)
+    unsigned int cls_ticket;  // work counters of the classify and generate launches (zeroed before each)
+    unsigned int gen_ticket;
 };
+static_assert(sizeof(MeshTotals) <= 256, "MeshTotals fits the totals region of the fixed scratch");
 
 // Grows a device allocation; returns false on cudaMalloc failure.
 template <class T>
