@@ -250,10 +250,16 @@ mcg_status mcg_integrate_backward(mcg_context *ctx, const void *vol0, int32_t nx
 /* upper bound of the encoded file image size */
 int64_t mcg_rle_bound(int32_t nx, int32_t ny, int32_t nz);
 /* Encode a device short2 volume into a host file image (header + per-slice
- * dumps, the reference's file layout).  lossless = 0 writes the reference
+ * dumps, the reference's file layout), on the GPU (kf.cu:1367-1417 encodes
+ * one slice at a time on the host).  lossless = 0 writes the reference
  * format (runs compare tsdf only; weights inside a run are not kept);
  * lossless = 1 writes the same layout with tag "VOLUME_TSDF_W32" and runs
- * that compare whole voxels.  Synchronous. */
+ * that compare whole voxels.  The image is assembled in device memory kept
+ * by ctx and copied out once.  image = NULL with capacity = 0 returns the
+ * exact image size in *size; a smaller capacity gives MCG_ERR_CAPACITY with
+ * the size in *size.  MCG_ERR_TOO_LARGE when a slice could exceed the
+ * format's 32-bit slice byte count (more than 715 827 882 voxels per
+ * slice).  Synchronous. */
 mcg_status mcg_rle_encode(mcg_context *ctx, const void *vol, int32_t nx, int32_t ny, int32_t nz,
                           float min_t, float max_t, float grid_s, int32_t lossless,
                           uint8_t *image, int64_t capacity, int64_t *size, mcg_stream_t stream);

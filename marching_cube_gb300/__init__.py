@@ -701,9 +701,9 @@ def integrate_frames(depth, poses, shape, min_t, max_t, grid_s, k, vol0=None, no
 # ---------------------------------------------------------------------------
 def _image_out(cap, fill):
     """Runs fill(pointer, capacity, size_ref) into a fresh bytearray of cap
-    bytes and returns the bytearray cut to the written size.  (A bytearray
-    is allocated lazily by the OS and cut without a copy; ctypes.string_at
-    takes a 32-bit length and would truncate images of 2 GiB and more.)"""
+    bytes and returns the bytearray cut to the written size (in place, no
+    copy; ctypes.string_at would take a 32-bit length and truncate images of
+    2 GiB and more)."""
     buf = bytearray(cap)
     view = (ctypes.c_uint8 * cap).from_buffer(buf)
     size = ctypes.c_int64(0)
@@ -722,17 +722,31 @@ def _image_in(image):
     return arr.ctypes.data_as(ctypes.c_void_p), arr.size, arr
 
 
-def rle_encode(v: Voxel, lossless=False, ctx=None, stream=None) -> bytearray:
-    """Encode a short2 volume into the reference's RLE file image."""
+def rle_encode(v: Voxel, lossless=False, out=None, ctx=None, stream=None) -> memoryview:
+    """Encode a short2 volume into the reference's RLE file image (on the
+    GPU).  out: optional writable buffer reused across calls; the result is a
+    memoryview of the written bytes (of `out`, or of a new buffer sized
+    exactly)."""
+    import numpy as np
     if v.data.dtype != torch.int16:
         raise TypeError("RLE volumes are short2 (int16) volumes")
     ctx = ctx or default_context(v.data.device.index)
     nx, ny, nz = v.size
-    st, img = _image_out(_lib.mcg_rle_bound(nx, ny, nz), lambda p, cap, size: _lib.mcg_rle_encode(
-        ctx.handle, _ptr(v.data), nx, ny, nz, v.min_t, v.max_t, v.grid_s, 1 if lossless else 0, p, cap, size,
-        _stream(stream)))
-    ctx.check(st, "mcg_rle_encode")
-    return img
+    size = ctypes.c_int64(0)
+
+    def call(ptr, cap):
+        return _lib.mcg_rle_encode(ctx.handle, _ptr(v.data), nx, ny, nz, v.min_t, v.max_t, v.grid_s,
+                                   1 if lossless else 0, ptr, cap, ctypes.byref(size), _stream(stream))
+
+    if out is None:
+        ctx.check(call(None, 0), "mcg_rle_encode")  # exact size first
+        buf = np.empty(size.value, np.uint8)
+    else:
+        buf = np.frombuffer(out, dtype=np.uint8)
+        if buf.flags.writeable is False:
+            raise ValueError("out must be writable")
+    ctx.check(call(buf.ctypes.data_as(ctypes.c_void_p), buf.size), "mcg_rle_encode")
+    return memoryview(buf)[: size.value]
 
 
 def rle_header(image):

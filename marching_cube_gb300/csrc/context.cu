@@ -78,6 +78,8 @@ mcg_status mcg_destroy(mcg_context *ctx) {
     cudaFree(ctx->d_vol_sums);
     if (ctx->h_vol_sums) cudaFreeHost(ctx->h_vol_sums);
     delete[] ctx->batch_caps;
+    cudaFree(ctx->rle_slices);
+    cudaFree(ctx->rle_image);
     cudaFree(ctx->depth_scaled);
     cudaFree(ctx->ray_x);
     if (ctx->h_ray_x) cudaFreeHost(ctx->h_ray_x);

@@ -94,6 +94,12 @@ struct mcg_context {
     int64_t *batch_caps = nullptr;  // host, last generate's capacities
     size_t batch_caps_cap = 0;
 
+    // GPU run-length encoder: per-slice byte counts / offsets and the image
+    unsigned long long *rle_slices = nullptr;
+    size_t rle_slices_cap = 0;
+    uint8_t *rle_image = nullptr;
+    size_t rle_image_cap = 0;
+
     // integrate scratch
     float *depth_scaled = nullptr;
     size_t depth_scaled_cap = 0;

@@ -13,8 +13,10 @@
 // for w == 0.
 //
 // The reference codes slices one after another on one host thread and copies
-// every slice separately; here slabs of slices are copied with one
-// cudaMemcpyAsync each and the slices of a slab are coded by all host threads.
+// every slice separately.  Here a device volume is encoded by the GPU
+// (rle_gpu.cu); host volumes are encoded, and images decoded, slice-parallel
+// on all host threads, decoded slabs moving to the device in one
+// cudaMemcpyAsync each.
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string.h>
@@ -212,53 +214,6 @@ mcg_status mcg_rle_decode_host(const uint8_t *image, int64_t size, void *vol, in
         if (!decode_slice(image + off[z], len[z], v + (int64_t)z * xy, xy)) bad = true;
     });
     return bad ? MCG_ERR_FORMAT : MCG_OK;
-}
-
-mcg_status mcg_rle_encode(mcg_context *ctx, const void *vol, int32_t nx, int32_t ny, int32_t nz,
-                          float min_t, float max_t, float grid_s, int32_t lossless, uint8_t *image,
-                          int64_t capacity, int64_t *size, mcg_stream_t stream) {
-    if (!ctx || !vol || !image || !size || nx <= 0 || ny <= 0 || nz <= 0) return MCG_ERR_INVALID_ARG;
-    *size = 0;
-    if (capacity < 40) return MCG_ERR_CAPACITY;
-    cudaError_t e = cudaSetDevice(ctx->device);
-    if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
-    cudaStream_t s = (cudaStream_t)stream;
-    memcpy(image, lossless ? kTagLossless : kTagRef, 16);
-    const int32_t dims[3] = {nx, ny, nz};
-    memcpy(image + 16, dims, 12);
-    memcpy(image + 28, &min_t, 4);
-    memcpy(image + 32, &max_t, 4);
-    memcpy(image + 36, &grid_s, 4);
-    int64_t o = 40;
-    const int64_t xy = (int64_t)nx * ny;
-    const int slab = std::min(nz, slab_slices(xy));
-    HVox *host = nullptr;
-    if (cudaMallocHost((void **)&host, sizeof(HVox) * xy * slab) != cudaSuccess)
-        return mcg_cuda_fail(ctx, cudaErrorMemoryAllocation);
-    std::vector<std::vector<uint8_t>> enc(slab);
-    mcg_status st = MCG_OK;
-    for (int z0 = 0; z0 < nz && st == MCG_OK; z0 += slab) {
-        const int ns = std::min(slab, nz - z0);
-        e = cudaMemcpyAsync(host, (const HVox *)vol + (int64_t)z0 * xy, sizeof(HVox) * xy * ns,
-                            cudaMemcpyDeviceToHost, s);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-        if (e != cudaSuccess) { st = mcg_cuda_fail(ctx, e); break; }
-        std::vector<int64_t> sz(ns);
-        parallel_for(ns, [&](int i) {
-            enc[i].resize((size_t)(6 * xy + 16));
-            sz[i] = encode_slice(host + (int64_t)i * xy, xy, lossless != 0, enc[i].data());
-        });
-        for (int i = 0; i < ns; ++i) {
-            if (o + 4 + sz[i] > capacity) { st = MCG_ERR_CAPACITY; break; }
-            const uint32_t s32 = (uint32_t)sz[i];
-            memcpy(image + o, &s32, 4);
-            memcpy(image + o + 4, enc[i].data(), (size_t)sz[i]);
-            o += 4 + sz[i];
-        }
-    }
-    cudaFreeHost(host);
-    if (st == MCG_OK) *size = o;
-    return st;
 }
 
 mcg_status mcg_rle_decode(mcg_context *ctx, const uint8_t *image, int64_t size, void *vol,
