@@ -52,6 +52,7 @@ def parse():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-indexed", action="store_true")
     ap.add_argument("--no-stress", action="store_true")
+    ap.add_argument("--stress-n", type=int, default=1024, help="stress volume edge (default 1024)")
     return ap.parse_args()
 
 
@@ -630,7 +631,7 @@ def main():
     stress = None
     if not args.no_stress:
         try:
-            stress = bench_stress(mcg, synthetic, torch)
+            stress = bench_stress(mcg, synthetic, torch, n=args.stress_n)
         except Exception as ex:  # pragma: no cover
             stress = {"error": str(ex)}
         torch.cuda.empty_cache()
