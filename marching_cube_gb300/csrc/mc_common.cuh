@@ -22,6 +22,11 @@ namespace {
 constexpr int BX = 32, BY = 8, BZ = 8;
 constexpr int BRICK_CUBES = BX * BY * BZ;  // 2048
 constexpr int CHUNK = 256;                 // bricks per scan chunk
+// per-chunk sums written by the count pass: triangles, active bricks,
+// occupied cubes, heavy bricks (more than HEAVY_TRIS triangles: more than one
+// pass of a 256-thread CTA over their soup vertices)
+constexpr int CHUNK_FIELDS = 4;
+constexpr unsigned int HEAVY_TRIS = 85;
 
 __host__ __device__ constexpr int pad128(int bytes) { return (bytes + 127) / 128 * 128; }
 

@@ -369,9 +369,11 @@ __global__ void __launch_bounds__(CLS_THREADS)
             brick_tris[b] = t;
             // per-chunk (CHUNK consecutive bricks) sums feed the scan
             if (t) {
-                atomicAdd(&chunk[(b / CHUNK) * 3 + 0], t);
-                atomicAdd(&chunk[(b / CHUNK) * 3 + 1], 1u);
-                atomicAdd(&chunk[(b / CHUNK) * 3 + 2], o);
+                uint32_t *c = chunk + (b / CHUNK) * CHUNK_FIELDS;
+                atomicAdd(c + 0, t);
+                atomicAdd(c + 1, 1u);
+                atomicAdd(c + 2, o);
+                if (t > HEAVY_TRIS) atomicAdd(c + 3, 1u);
             }
         }
         if (!TMA) __syncthreads();  // S.sitem[0] is rewritten at the top
@@ -393,65 +395,89 @@ __global__ void __launch_bounds__(CHUNK)
     mc_scan_kernel(const uint32_t *__restrict__ brick_tris, const uint32_t *__restrict__ chunk, long long nb,
                    unsigned long long *__restrict__ brick_vofs, uint32_t *__restrict__ active,
                    MeshTotals *__restrict__ totals) {
-    __shared__ unsigned long long s_part[5][CHUNK / 32];
+    __shared__ unsigned long long s_part[7][CHUNK / 32];
     __shared__ unsigned long long s_base_v;
-    __shared__ unsigned int s_base_a;
+    __shared__ unsigned int s_base_h, s_base_l, s_heavy;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const long long j = blockIdx.x;
     const long long nchunks = (nb + CHUNK - 1) / CHUNK;
-    // base offsets: sums over the chunks before this one; CTA 0 also sums all
-    // chunks for the totals
-    const long long upto = j == 0 ? nchunks : j;
-    unsigned long long acc[5] = {0, 0, 0, 0, 0};  // base tris, base active, all tris, all active, all occupied
-    for (long long i = tid; i < upto; i += CHUNK) {
-        const unsigned long long cv = chunk[i * 3 + 0], ca = chunk[i * 3 + 1];
-        if (i < j) { acc[0] += cv; acc[1] += ca; }
-        acc[2] += cv;
-        acc[3] += ca;
-        acc[4] += chunk[i * 3 + 2];
+    // base offsets: sums over the chunks before this one; every CTA also sums
+    // all chunks' heavy bricks (the light ones follow them in the list), CTA 0
+    // the totals.
+    // acc: base tris, base active, base heavy, all tris, all active, all occupied, all heavy
+    unsigned long long acc[7] = {0, 0, 0, 0, 0, 0, 0};
+    for (long long i = tid; i < nchunks; i += CHUNK) {
+        const uint32_t *c = chunk + i * CHUNK_FIELDS;
+        const unsigned long long cv = c[0], ca = c[1], ch = c[3];
+        if (i < j) {
+            acc[0] += cv;
+            acc[1] += ca;
+            acc[2] += ch;
+        }
+        acc[3] += cv;
+        acc[4] += ca;
+        acc[5] += c[2];
+        acc[6] += ch;
     }
 #pragma unroll
-    for (int k = 0; k < 5; ++k) {
+    for (int k = 0; k < 7; ++k) {
 #pragma unroll
         for (int o = 16; o; o >>= 1) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], o);
         if (lane == 0) s_part[k][warp] = acc[k];
     }
     __syncthreads();
     if (tid == 0) {
-        unsigned long long r[5] = {0, 0, 0, 0, 0};
-        for (int k = 0; k < 5; ++k)
+        unsigned long long r[7] = {0, 0, 0, 0, 0, 0, 0};
+        for (int k = 0; k < 7; ++k)
             for (int w = 0; w < CHUNK / 32; ++w) r[k] += s_part[k][w];
         s_base_v = r[0];
-        s_base_a = (unsigned int)r[1];
+        s_base_h = (unsigned int)r[2];
+        s_base_l = (unsigned int)(r[1] - r[2]);
+        s_heavy = (unsigned int)r[6];
         if (j == 0) {
-            totals->occupied = r[4];
-            totals->triangles = r[2];
-            totals->vertices = 3ull * r[2];
-            totals->active_bricks = (unsigned int)r[3];
+            totals->occupied = r[5];
+            totals->triangles = r[3];
+            totals->vertices = 3ull * r[3];
+            totals->active_bricks = (unsigned int)r[4];
         }
     }
     __syncthreads();
     const unsigned long long base_v = s_base_v;
-    const unsigned int base_a = s_base_a;
-    // scan of this chunk's bricks
+    // scan of this chunk's bricks; the active list holds the heavy bricks
+    // (more than HEAVY_TRIS triangles) first, then the light ones, each in
+    // brick order, so the longest bricks start first and the tail is short
     const long long b = j * CHUNK + tid;
     const unsigned int t = b < nb ? brick_tris[b] : 0u;
-    const unsigned int f = t != 0;
-    unsigned int it = t, ia = f;
+    const unsigned int fh = t > HEAVY_TRIS, fl = t != 0 && !fh;
+    unsigned int it = t, ih = fh, il = fl;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
         const unsigned int x = __shfl_up_sync(0xffffffffu, it, o);
-        const unsigned int y = __shfl_up_sync(0xffffffffu, ia, o);
-        if (lane >= o) { it += x; ia += y; }
+        const unsigned int y = __shfl_up_sync(0xffffffffu, ih, o);
+        const unsigned int z = __shfl_up_sync(0xffffffffu, il, o);
+        if (lane >= o) {
+            it += x;
+            ih += y;
+            il += z;
+        }
     }
-    __shared__ unsigned int s_wt[CHUNK / 32], s_wa[CHUNK / 32];
-    if (lane == 31) { s_wt[warp] = it; s_wa[warp] = ia; }
+    __shared__ unsigned int s_w[3][CHUNK / 32];
+    if (lane == 31) {
+        s_w[0][warp] = it;
+        s_w[1][warp] = ih;
+        s_w[2][warp] = il;
+    }
     __syncthreads();
-    unsigned int wt = 0, wa = 0;
-    for (int w = 0; w < warp; ++w) { wt += s_wt[w]; wa += s_wa[w]; }
+    unsigned int wt = 0, wh = 0, wl = 0;
+    for (int w = 0; w < warp; ++w) {
+        wt += s_w[0][w];
+        wh += s_w[1][w];
+        wl += s_w[2][w];
+    }
     if (b < nb) {
         brick_vofs[b] = 3ull * (base_v + wt + it - t);
-        if (t) active[base_a + wa + ia - f] = (uint32_t)b;
+        if (fh) active[s_base_h + wh + ih - fh] = (uint32_t)b;
+        if (fl) active[s_heavy + s_base_l + wl + il - fl] = (uint32_t)b;
     }
 }
 
@@ -1013,9 +1039,11 @@ __global__ void __launch_bounds__(CTHREADS)
             }
             brick_tris[b] = t;
             if (t) {
-                atomicAdd(&chunk[(b / CHUNK) * 3 + 0], t);
-                atomicAdd(&chunk[(b / CHUNK) * 3 + 1], 1u);
-                atomicAdd(&chunk[(b / CHUNK) * 3 + 2], o);
+                uint32_t *c = chunk + (b / CHUNK) * CHUNK_FIELDS;
+                atomicAdd(c + 0, t);
+                atomicAdd(c + 1, 1u);
+                atomicAdd(c + 2, o);
+                if (t > HEAVY_TRIS) atomicAdd(c + 3, 1u);
                 atomicAdd(&vol_sums[2 * v + 0], (unsigned long long)t);
                 atomicAdd(&vol_sums[2 * v + 1], (unsigned long long)o);
             }
@@ -1133,7 +1161,7 @@ __global__ void mc_normals_kernel(const typename Vox<VT>::T *__restrict__ vol, i
 // ---- host side ----------------------------------------------------------------
 struct Scratch {
     uint32_t *tris;
-    uint32_t *chunk;  // 3 per chunk of CHUNK bricks: triangles, active bricks, occupied cubes
+    uint32_t *chunk;  // CHUNK_FIELDS per chunk of CHUNK bricks
     unsigned long long *vofs;
     uint32_t *active;
     MeshTotals *totals;
@@ -1209,7 +1237,7 @@ long long num_chunks(long long nbricks) { return (nbricks + CHUNK - 1) / CHUNK; 
 cudaError_t launch_count_phase(const mcg_volume *vol, const Geometry &g, const Scratch &sc, int sms, cudaStream_t s) {
     // flags and both work counters
     cudaError_t e = cudaMemsetAsync(&sc.totals->flags, 0, 3 * sizeof(unsigned int), s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(sc.chunk, 0, sizeof(uint32_t) * 3 * num_chunks(g.nbricks), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(sc.chunk, 0, sizeof(uint32_t) * CHUNK_FIELDS * num_chunks(g.nbricks), s);
     if (e != cudaSuccess) return e;
     CUtensorMap map;
     const int eb = vol->voxel_type == MCG_VOXEL_SHORT2 ? 4 : 8;
@@ -1305,7 +1333,7 @@ mcg_status mcg_mc_classify(mcg_context *ctx, const mcg_volume *vol, mcg_stream_t
     if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
     const Geometry g = geometry(vol->nx, vol->ny, vol->nz);
     if (!ensure(&ctx->brick_tris, &ctx->brick_tris_cap, (size_t)g.nbricks) ||
-        !ensure(&ctx->brick_occ, &ctx->brick_occ_cap, (size_t)(3 * num_chunks(g.nbricks))) ||
+        !ensure(&ctx->brick_occ, &ctx->brick_occ_cap, (size_t)(CHUNK_FIELDS * num_chunks(g.nbricks))) ||
         !ensure(&ctx->brick_vofs, &ctx->brick_vofs_cap, (size_t)g.nbricks) ||
         !ensure(&ctx->active, &ctx->active_cap, (size_t)g.nbricks))
         return mcg_cuda_fail(ctx, cudaErrorMemoryAllocation);
@@ -1571,7 +1599,7 @@ mcg_status mcg_mc_classify_batched(mcg_context *ctx, const mcg_volume *vols, int
     for (int v = 0; v < nvol; ++v) nbricks += geometry(vols[v].nx, vols[v].ny, vols[v].nz).nbricks;
     if (nbricks >= (1ll << 32)) return MCG_ERR_INVALID_ARG;
     if (!ensure(&ctx->brick_tris, &ctx->brick_tris_cap, (size_t)nbricks) ||
-        !ensure(&ctx->brick_occ, &ctx->brick_occ_cap, (size_t)(3 * num_chunks(nbricks))) ||
+        !ensure(&ctx->brick_occ, &ctx->brick_occ_cap, (size_t)(CHUNK_FIELDS * num_chunks(nbricks))) ||
         !ensure(&ctx->brick_vofs, &ctx->brick_vofs_cap, (size_t)nbricks) ||
         !ensure(&ctx->active, &ctx->active_cap, (size_t)nbricks) ||
         !ensure(&ctx->d_vol_sums, &ctx->d_vol_sums_cap, (size_t)(2 * nvol)))
@@ -1589,7 +1617,7 @@ mcg_status mcg_mc_classify_batched(mcg_context *ctx, const mcg_volume *vols, int
     mcg_status st = upload_btab(ctx, vols, nullptr, nvol, true, s, &total);
     if (st != MCG_OK) return st;
     e = cudaMemsetAsync(&ctx->d_totals->flags, 0, sizeof(unsigned int), s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(ctx->brick_occ, 0, sizeof(uint32_t) * 3 * num_chunks(nbricks), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(ctx->brick_occ, 0, sizeof(uint32_t) * CHUNK_FIELDS * num_chunks(nbricks), s);
     if (e == cudaSuccess) e = cudaMemsetAsync(ctx->d_vol_sums, 0, sizeof(unsigned long long) * 2 * nvol, s);
     if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
     if (vols[0].voxel_type == MCG_VOXEL_SHORT2) launch_classify_multi<MCG_VOXEL_SHORT2>(ctx, nvol, nbricks, s);
@@ -1692,7 +1720,7 @@ namespace {
 constexpr long long kNoAllocBricks = MCG_NOALLOC_MAX_BRICKS;
 constexpr size_t kNoAllocTrisOff = 0;
 constexpr size_t kNoAllocOccOff = kNoAllocTrisOff + sizeof(uint32_t) * kNoAllocBricks;
-static_assert(3 * ((kNoAllocBricks + CHUNK - 1) / CHUNK) <= kNoAllocBricks, "chunk sums fit their region");
+static_assert(CHUNK_FIELDS * ((kNoAllocBricks + CHUNK - 1) / CHUNK) <= kNoAllocBricks, "chunk sums fit their region");
 constexpr size_t kNoAllocVofsOff = kNoAllocOccOff + sizeof(uint32_t) * kNoAllocBricks;
 constexpr size_t kNoAllocActiveOff = kNoAllocVofsOff + sizeof(unsigned long long) * kNoAllocBricks;
 constexpr size_t kNoAllocTotalsOff = kNoAllocActiveOff + sizeof(uint32_t) * kNoAllocBricks;
@@ -1731,7 +1759,7 @@ extern "C" mcg_status mcg_mc_extract_noalloc(const mcg_volume *vol, const mcg_me
     unsigned char *base = g_noalloc_addr[dev];
     Scratch sc;
     sc.tris = reinterpret_cast<uint32_t *>(base + kNoAllocTrisOff);
-    sc.chunk = reinterpret_cast<uint32_t *>(base + kNoAllocOccOff);  // 3 * 256 chunk sums at most
+    sc.chunk = reinterpret_cast<uint32_t *>(base + kNoAllocOccOff);  // CHUNK_FIELDS * 256 chunk sums at most
     sc.vofs = reinterpret_cast<unsigned long long *>(base + kNoAllocVofsOff);
     sc.active = reinterpret_cast<uint32_t *>(base + kNoAllocActiveOff);
     sc.totals = reinterpret_cast<MeshTotals *>(base + kNoAllocTotalsOff);

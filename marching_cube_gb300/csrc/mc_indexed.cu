@@ -235,46 +235,58 @@ __device__ __forceinline__ unsigned int block_scan(IdxSmem<VT> &S, unsigned int 
     return base + x - v;
 }
 
-// Streams the bricks of a persistent CTA through the TMA ring (or plain
-// loads) and calls body(tile, b, bp) for each; `list` (may be null) maps the
-// CTA's work item to a brick id.  Returns false when a bounded wait expired.
+// Streams bricks through the CTA's TMA ring (or plain loads) and calls
+// body(tile, b, bp) for each.  Work items come from the device counter
+// `ticket` (thread 0 draws the next refill one item ahead, so the counter's
+// round trip overlaps the current brick); `list` (may be null) maps an item
+// to a brick id.  Returns false when a bounded wait expired.
 template <int VT, bool TMA, class Body>
 __device__ __forceinline__ bool for_each_brick(IdxSmem<VT> &S, const CUtensorMap *map,
                                                const typename Vox<VT>::T *__restrict__ vol, int nx, int ny, int nz,
-                                               int nbx, int nby, long long nitems, const uint32_t *list, Body body) {
+                                               int nbx, int nby, long long nitems, const uint32_t *list,
+                                               unsigned int *ticket, Body body) {
     using V = Vox<VT>;
     using T = typename V::T;
     const int tid = threadIdx.x;
-    const long long stride = gridDim.x;
+    auto draw = [&]() -> long long {
+        const unsigned int t = atomicAdd(ticket, 1u);
+        if ((long long)t >= nitems) return -1ll;
+        return list ? (long long)list[t] : (long long)t;
+    };
+    long long pend = -1;
     if (tid == 0) {
         S.abort = 0;
         if (TMA) {
             for (int s = 0; s < ISTAGES; ++s) mbar_init(&S.bars[s], 1);
             fence_barrier_init();
+            bool more = true;
             for (int s = 0; s < ISTAGES; ++s) {
-                const long long w = blockIdx.x + s * stride;
-                if (w >= nitems) break;
-                const long long b = list ? (long long)list[w] : w;
+                const long long b = more ? draw() : -1ll;
+                more = b >= 0;
                 S.sbrick[s] = b;
+                if (!more) continue;
                 const BrickPos bp = brick_pos(b, nbx, nby);
                 mbar_arrive_expect_tx(&S.bars[s], ITILE * V::bytes);
                 tma_load_3d(S.tiles[s], map, &S.bars[s], bp.x0 - 4, bp.y0 - 1, bp.z0 - 1);
             }
+            if (more) pend = draw();
         }
     }
     __syncthreads();
-    int it = 0;
-    for (long long w = blockIdx.x; w < nitems; w += stride, ++it) {
+    for (int it = 0;; ++it) {
         const int s = TMA ? it % ISTAGES : 0;
         T *tile = reinterpret_cast<T *>(S.tiles[s]);
-        long long b;
+        if (!TMA) {
+            if (tid == 0) S.sbrick[0] = draw();
+            __syncthreads();
+        }
+        const long long b = S.sbrick[s];
+        if (b < 0) break;  // uniform
         if (TMA) {
             if (tid == 0 && !mbar_wait(&S.bars[s], (uint32_t)((it / ISTAGES) & 1))) S.abort = 1;
             __syncthreads();
             if (S.abort) break;
-            b = S.sbrick[s];
         } else {
-            b = list ? (long long)list[w] : w;
             const BrickPos fp = brick_pos(b, nbx, nby);
             fill_tile<VT, IX, IY, IZ>(tile, vol, nx, ny, nz, fp.x0 - 4, fp.y0 - 1, fp.z0 - 1);
             __syncthreads();
@@ -282,15 +294,18 @@ __device__ __forceinline__ bool for_each_brick(IdxSmem<VT> &S, const CUtensorMap
         body(tile, b, brick_pos(b, nbx, nby));
         __syncthreads();  // tile s and the shared scratch are free again
         if (TMA && tid == 0) {
-            const long long wn = w + ISTAGES * stride;
-            if (wn < nitems) {
-                const long long nb2 = list ? (long long)list[wn] : wn;
-                S.sbrick[s] = nb2;
+            const long long nb2 = pend;
+            S.sbrick[s] = nb2;
+            if (nb2 >= 0) {
                 const BrickPos np = brick_pos(nb2, nbx, nby);
                 mbar_arrive_expect_tx(&S.bars[s], ITILE * V::bytes);
                 tma_load_3d(S.tiles[s], map, &S.bars[s], np.x0 - 4, np.y0 - 1, np.z0 - 1);
+                pend = draw();
             }
         }
+        // S.sbrick[s] is next read at the top of iteration it + ISTAGES, after
+        // the barriers of iteration it + 1; the plain path rewrites sbrick[0]
+        // only after the barrier above
     }
     if (TMA && S.abort) {
         if (tid == 0)
@@ -298,6 +313,34 @@ __device__ __forceinline__ bool for_each_brick(IdxSmem<VT> &S, const CUtensorMap
         return false;
     }
     return true;
+}
+
+// True when the tile holds both negative and non-negative voxels; a tile of
+// one sign has no crossed edge and no emitting cube.  Every thread; one barrier.
+template <int VT>
+__device__ __forceinline__ bool idx_tile_mixed(IdxSmem<VT> &S, const typename Vox<VT>::T *tile) {
+    constexpr int NQ = ITILE * Vox<VT>::bytes / 16;
+    const uint4 *q = reinterpret_cast<const uint4 *>(tile);
+    unsigned int neg_any = 0, pos_any = 0;
+    for (int i = threadIdx.x; i < NQ; i += ITHREADS) {
+        const uint4 v = q[i];
+        if (VT == MCG_VOXEL_SHORT2) {
+            neg_any |= v.x | v.y | v.z | v.w;  // bit 15 of each word: tsdf sign
+            pos_any |= ~(v.x & v.y & v.z & v.w);
+        } else {
+            const bool n0 = __uint_as_float(v.x) < 0.f, n1 = __uint_as_float(v.z) < 0.f;
+            neg_any |= (unsigned int)(n0 | n1) << 15;
+            pos_any |= (unsigned int)(!n0 | !n1) << 15;
+        }
+    }
+    neg_any = __reduce_or_sync(0xffffffffu, neg_any & 0x8000u);
+    pos_any = __reduce_or_sync(0xffffffffu, pos_any & 0x8000u);
+    if ((threadIdx.x & 31) == 0) S.wsum[threadIdx.x >> 5][3] = (neg_any ? 1u : 0u) | (pos_any ? 2u : 0u);
+    __syncthreads();
+    unsigned int m = 0;
+#pragma unroll
+    for (int w = 0; w < IWARPS; ++w) m |= S.wsum[w][3];
+    return m == 3u;
 }
 
 struct IdxParams {
@@ -332,7 +375,14 @@ __global__ void __launch_bounds__(ITHREADS) mc_idx_count_kernel(const __grid_con
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const bool ok = for_each_brick<VT, TMA>(
         S, &map, static_cast<const typename Vox<VT>::T *>(p.vol), p.nx, p.ny, p.nz, p.nbx, p.nby, p.nbricks, nullptr,
-        [&](const typename Vox<VT>::T *tile, long long b, BrickPos bp) {
+        &p.totals->cls_ticket, [&](const typename Vox<VT>::T *tile, long long b, BrickPos bp) {
+            if (!idx_tile_mixed<VT>(S, tile)) {
+                if (tid == 0) {
+                    p.brick_tris[b] = 0;
+                    p.brick_uniq[b] = 0;
+                }
+                return;  // uniform across the CTA
+            }
             idx_prepare<VT>(S, tile, bp, p.nx, p.ny, p.nz);
             unsigned int t = 0, o = 0, u = 0;
             if (tid < BY * BZ) {
@@ -485,7 +535,7 @@ __global__ void __launch_bounds__(ITHREADS) mc_idx_vertex_kernel(const __grid_co
     const long long capv = p.out.capacity_vertices;
     const bool ok = for_each_brick<VT, TMA>(
         S, &map, vol, p.nx, p.ny, p.nz, p.nbx, p.nby, (long long)p.totals->active_bricks, p.active,
-        [&](const T *tile, long long b, BrickPos bp) {
+        &p.totals->gen_ticket, [&](const T *tile, long long b, BrickPos bp) {
             idx_prepare<VT>(S, tile, bp, p.nx, p.ny, p.nz);
             unsigned long long m = 0;
             int oy = 0, oz = 0, axis = 0;
@@ -568,7 +618,7 @@ __global__ void __launch_bounds__(ITHREADS)
     const long long capt = p.out.capacity_triangles;
     const bool ok = for_each_brick<VT, TMA>(
         S, &map, static_cast<const T *>(p.vol), p.nx, p.ny, p.nz, p.nbx, p.nby, (long long)p.totals->active_bricks,
-        p.active, [&](const T *tile, long long b, BrickPos bp) {
+        p.active, &p.totals->idx_ticket, [&](const T *tile, long long b, BrickPos bp) {
             if (p.brick_tris[b] == 0) return;  // uniform across the CTA
             idx_prepare<VT>(S, tile, bp, p.nx, p.ny, p.nz);
             // four adjacent threads per cube row (64 rows = 256 threads); thread q of a row
@@ -704,7 +754,8 @@ mcg_status mcg_mc_classify_indexed(mcg_context *ctx, const mcg_volume *vol, mcg_
         !ensure(&ctx->brick_uofs, &ctx->brick_uofs_cap, (size_t)g.nbricks) ||
         !ensure(&ctx->active, &ctx->active_cap, (size_t)g.nbricks))
         return mcg_cuda_fail(ctx, cudaErrorMemoryAllocation);
-    e = cudaMemsetAsync(&ctx->d_totals->flags, 0, sizeof(unsigned int), s);
+    // flags and the three work counters
+    e = cudaMemsetAsync(&ctx->d_totals->flags, 0, 4 * sizeof(unsigned int), s);
     if (e == cudaSuccess) e = cudaMemsetAsync(ctx->brick_occ, 0, sizeof(uint32_t) * 4 * nch, s);
     if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
     const IdxParams p = idx_params(ctx, vol, g);
@@ -746,6 +797,8 @@ mcg_status mcg_mc_generate_indexed(mcg_context *ctx, const mcg_volume *vol, cons
     if (!ensure(&ctx->edge_map, &ctx->edge_map_cap, nedges)) return mcg_cuda_fail(ctx, cudaErrorMemoryAllocation);
     IdxParams p = idx_params(ctx, vol, g);
     p.out = *out;
+    e = cudaMemsetAsync(&ctx->d_totals->gen_ticket, 0, 2 * sizeof(unsigned int), s);
+    if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
     launch_idx_pass(1, vol, p, ctx->num_sms, g.nbricks, s);
     launch_idx_pass(2, vol, p, ctx->num_sms, g.nbricks, s);
     e = cudaGetLastError();

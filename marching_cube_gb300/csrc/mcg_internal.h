@@ -19,8 +19,9 @@ struct MeshTotals {
     unsigned long long vertices;
     unsigned int active_bricks;
     unsigned int flags;       // bit 0: a bounded device wait expired (set by the kernels, cleared by the host)
-    unsigned int cls_ticket;  // work counters of the classify and generate launches (zeroed before each)
-    unsigned int gen_ticket;
+    unsigned int cls_ticket;  // work counters of the count, generate and (indexed) triangle launches,
+    unsigned int gen_ticket;  // zeroed before each
+    unsigned int idx_ticket;
 };
 static_assert(sizeof(MeshTotals) <= 256, "MeshTotals fits the totals region of the fixed scratch");
 
@@ -47,7 +48,7 @@ struct mcg_context {
     // marching-cubes scratch (one entry per brick)
     uint32_t *brick_tris = nullptr;
     size_t brick_tris_cap = 0;
-    uint32_t *brick_occ = nullptr;  // per-chunk sums (triangles, active bricks, occupied cubes)
+    uint32_t *brick_occ = nullptr;  // per-chunk sums of the count pass (CHUNK_FIELDS per chunk)
     size_t brick_occ_cap = 0;
     unsigned long long *brick_vofs = nullptr;
     size_t brick_vofs_cap = 0;

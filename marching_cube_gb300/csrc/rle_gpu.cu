@@ -50,7 +50,7 @@ struct RleSmem {
     uint32_t vox[RCHUNK];   // their first voxels
     uint32_t boff[RCHUNK];  // their byte offsets from the chunk's first record
     uint32_t wn[RT / 32], wb[RT / 32];
-    unsigned long long wr[RT / 32];
+    int wr[RT / 32];
 };
 
 // block-wide exclusive sums of two values; totals returned through refs
@@ -89,20 +89,20 @@ __device__ __forceinline__ void scan2(RleSmem &S, uint32_t a, uint32_t b, uint32
 }
 
 // block-wide inclusive max-scan of a signed value (run starts, -1 = none)
-__device__ __forceinline__ long long scan_max(RleSmem &S, long long v, long long carry) {
+__device__ __forceinline__ int scan_max(RleSmem &S, int v, int carry) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    long long x = v;
+    int x = v;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-        const long long p = __shfl_up_sync(0xffffffffu, x, o);
+        const int p = __shfl_up_sync(0xffffffffu, x, o);
         if (lane >= o && p > x) x = p;
     }
-    if (lane == 31) S.wr[warp] = (unsigned long long)x;
+    if (lane == 31) S.wr[warp] = x;
     __syncthreads();
-    long long m = carry;
+    int m = carry;
 #pragma unroll
     for (int w = 0; w < RT / 32; ++w)
-        if (w < warp && (long long)S.wr[w] > m) m = (long long)S.wr[w];
+        if (w < warp && S.wr[w] > m) m = S.wr[w];
     __syncthreads();
     return x > m ? x : m;
 }
@@ -125,7 +125,7 @@ __device__ __forceinline__ void emit(uint8_t *img, unsigned long long off, uint3
 // WRITE = false: slice_bytes[z] = record bytes of slice z.  WRITE = true:
 // slice z goes to img + slice_off[z]: its byte count (uint32) then records.
 template <bool WRITE>
-__global__ void __launch_bounds__(RT) rle_encode_kernel(const uint32_t *__restrict__ vol, long long xy, int lossless_i,
+__global__ void __launch_bounds__(RT) rle_encode_kernel(const uint32_t *__restrict__ vol, int xy, int lossless_i,
                                                         unsigned long long *__restrict__ slice_bytes,
                                                         const unsigned long long *__restrict__ slice_off,
                                                         uint8_t *__restrict__ img) {
@@ -137,28 +137,30 @@ __global__ void __launch_bounds__(RT) rle_encode_kernel(const uint32_t *__restri
     const int tid = threadIdx.x;
     uint8_t *out = WRITE ? img + slice_off[z] + 4 : nullptr;
     uint32_t prev = 0;            // voxel before the chunk
-    long long rs_carry = -1;      // run start in force at the chunk's start
+    int rs_carry = -1;            // run start in force at the chunk's start
     unsigned long long bytes = 0; // bytes of the records started before the chunk
-    long long pend = -1;          // record open at the chunk's start (WRITE)
+    int pend = -1;                // record open at the chunk's start (WRITE)
     uint32_t pend_v = 0;
     unsigned long long pend_off = 0;
-    for (long long c0 = 0; c0 < xy; c0 += RCHUNK) {
-        const long long i0 = c0 + (long long)tid * RV;
+    // slice indices fit 32 bits: the host rejects slices whose image could
+    // pass the format's 32-bit byte count
+    for (int c0 = 0; c0 < xy; c0 += RCHUNK) {
+        const int i0 = c0 + tid * RV;
         uint32_t v[RV];
 #pragma unroll
-        for (int j = 0; j < RV; ++j) v[j] = i0 + j < xy ? sl[i0 + j] : 0u;
+        for (int j = 0; j < RV; ++j) v[j] = i0 + j < xy ? __ldg(sl + i0 + j) : 0u;
         // previous voxel of each thread's first voxel
         uint32_t left = __shfl_up_sync(0xffffffffu, v[RV - 1], 1);
         if ((tid & 31) == 0) {
             if (tid == 0) left = prev;
-            else left = i0 - 1 < xy ? sl[i0 - 1] : 0u;
+            else left = i0 - 1 < xy ? __ldg(sl + i0 - 1) : 0u;
         }
         // run starts (local inclusive max), then the block max-scan
-        long long rs_loc = -1;
+        int rs_loc = -1;
         uint32_t chg = 0;
 #pragma unroll
         for (int j = 0; j < RV; ++j) {
-            const long long i = i0 + j;
+            const int i = i0 + j;
             const uint32_t pv = j == 0 ? left : v[j - 1];
             const bool c = i < xy && (i == 0 || !same_voxel(v[j], pv, lossless));
             if (c) {
@@ -166,27 +168,29 @@ __global__ void __launch_bounds__(RT) rle_encode_kernel(const uint32_t *__restri
                 rs_loc = i;
             }
         }
-        const long long rs_incl = scan_max(S, rs_loc, rs_carry);
-        // run start in force at this thread's first voxel: the exclusive value
-        long long rs = __shfl_up_sync(0xffffffffu, rs_incl, 1);
+        const int rs_incl = scan_max(S, rs_loc, rs_carry);
+        // run start in force before this thread's first voxel: the exclusive value
+        int rs = __shfl_up_sync(0xffffffffu, rs_incl, 1);
         if ((tid & 31) == 0) {
             // exclusive across warps: the block max of everything before this warp
             rs = rs_carry;
             for (int w = 0; w < (tid >> 5); ++w)
-                if ((long long)S.wr[w] > rs) rs = (long long)S.wr[w];
+                if (S.wr[w] > rs) rs = S.wr[w];
         }
-        // record starts and their bytes
+        // record starts and their bytes; d = voxels since the run start, mod 16383
         uint32_t rec = 0, nrec = 0, nb = 0;
+        unsigned d = (unsigned)(i0 - rs) % kMaxRun;
 #pragma unroll
         for (int j = 0; j < RV; ++j) {
-            const long long i = i0 + j;
+            const int i = i0 + j;
             if (i >= xy) break;
-            if (chg & (1u << j)) rs = i;
-            if ((chg & (1u << j)) || ((i - rs) % kMaxRun == 0)) {
+            if (chg & (1u << j)) d = 0;
+            if (d == 0) {
                 rec |= 1u << j;
                 ++nrec;
                 nb += record_kind(v[j], lossless) == 3u ? 6u : 2u;
             }
+            d = d + 1 == kMaxRun ? 0u : d + 1;
         }
         uint32_t er, eb, tr, tb;
         scan2(S, nrec, nb, er, eb, tr, tb);
@@ -203,10 +207,10 @@ __global__ void __launch_bounds__(RT) rle_encode_kernel(const uint32_t *__restri
             }
             __syncthreads();
             if (tr > 0) {
-                if (tid == 0 && pend >= 0) emit(out, pend_off, pend_v, (unsigned)((long long)S.pos[0] - pend), lossless);
+                if (tid == 0 && pend >= 0) emit(out, pend_off, pend_v, (unsigned)((int)S.pos[0] - pend), lossless);
                 for (uint32_t q = tid; q + 1 < tr; q += RT)
                     emit(out, bytes + S.boff[q], S.vox[q], S.pos[q + 1] - S.pos[q], lossless);
-                pend = S.pos[tr - 1];
+                pend = (int)S.pos[tr - 1];
                 pend_v = S.vox[tr - 1];
                 pend_off = bytes + S.boff[tr - 1];
             }
@@ -215,11 +219,11 @@ __global__ void __launch_bounds__(RT) rle_encode_kernel(const uint32_t *__restri
         bytes += tb;
         // carries: the run start in force and the voxel at the chunk's end
         if (tid == RT - 1) {
-            S.wr[0] = (unsigned long long)rs_incl;
+            S.wr[0] = rs_incl;
             S.wn[0] = v[RV - 1];
         }
         __syncthreads();
-        rs_carry = (long long)S.wr[0];
+        rs_carry = S.wr[0];
         prev = S.wn[0];
         __syncthreads();
     }
@@ -263,7 +267,7 @@ extern "C" mcg_status mcg_rle_encode(mcg_context *ctx, const void *vol, int32_t 
     const size_t smem = sizeof(RleSmem);
     cudaFuncSetAttribute(rle_encode_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     cudaFuncSetAttribute(rle_encode_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    rle_encode_kernel<false><<<nz, RT, smem, s>>>(static_cast<const uint32_t *>(vol), xy, lossless ? 1 : 0, d_bytes,
+    rle_encode_kernel<false><<<nz, RT, smem, s>>>(static_cast<const uint32_t *>(vol), (int)xy, lossless ? 1 : 0, d_bytes,
                                                   nullptr, nullptr);
     e = cudaGetLastError();
     if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
@@ -283,7 +287,7 @@ extern "C" mcg_status mcg_rle_encode(mcg_context *ctx, const void *vol, int32_t 
     if (!ensure(&ctx->rle_image, &ctx->rle_image_cap, (size_t)o)) return mcg_cuda_fail(ctx, cudaErrorMemoryAllocation);
     e = cudaMemcpyAsync(d_off, off.data(), sizeof(unsigned long long) * nz, cudaMemcpyHostToDevice, s);
     if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
-    rle_encode_kernel<true><<<nz, RT, smem, s>>>(static_cast<const uint32_t *>(vol), xy, lossless ? 1 : 0, nullptr,
+    rle_encode_kernel<true><<<nz, RT, smem, s>>>(static_cast<const uint32_t *>(vol), (int)xy, lossless ? 1 : 0, nullptr,
                                                  d_off, ctx->rle_image);
     e = cudaGetLastError();
     if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
