@@ -147,6 +147,19 @@ mcg_status mcg_mc_generate_indexed(mcg_context *ctx, const mcg_volume *vol, cons
                                    mcg_stream_t stream);
 mcg_status mcg_mc_extract_indexed(mcg_context *ctx, const mcg_volume *vol, const mcg_indexed_out *out,
                                   mcg_stream_t stream);
+/* Slabs (no counterpart in the reference): the count phase, and with it the
+ * next mcg_mc_generate, over the cubes with z0 <= z < z1 only, z0 a multiple
+ * of 8 (the brick depth), 0 <= z0 < z1 <= nz - 1.  Soup offsets start at 0
+ * in each slab; positions, voxels, tri_cube and normals are those of the
+ * whole volume, and the slabs' soups of consecutive ranges concatenate to
+ * the whole volume's soup.  This is the unit a multi-GPU split hands to
+ * each device; the per-slab vertex totals are the only exchange.  ver_voxel
+ * is not available for a slab short of the whole volume (MCG_ERR_INVALID_ARG:
+ * it is cleared whole before the scatter). */
+mcg_status mcg_mc_classify_slab(mcg_context *ctx, const mcg_volume *vol, int32_t z0, int32_t z1,
+                                mcg_stream_t stream);
+mcg_status mcg_mc_extract_slab(mcg_context *ctx, const mcg_volume *vol, int32_t z0, int32_t z1,
+                               const mcg_mesh_out *out, mcg_stream_t stream);
 /* Batched extraction: nvol volumes of any sizes (same voxel type) in one
  * launch per pass (replaces a loop of MarchingCubes::run calls).  Outputs
  * of volume v go to outs[v], in the same order and bit-identical to a

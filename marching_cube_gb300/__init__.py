@@ -343,6 +343,24 @@ def extract_indexed_into(volume, cell, outputs: dict, capacity_vertices, capacit
     return ctx
 
 
+def extract_slab(volume, cell, z0, z1, *, soup=True, normals=True, vi2vox=False, tri_cube=False, ctx=None,
+                 stream=None) -> Mesh:
+    """Marching cubes over the cubes with z0 <= z < z1 (z0 a multiple of 8):
+    the part of extract(volume) those cubes emit, in the same order, so the
+    slabs of consecutive ranges concatenate to the whole soup."""
+    ctx = ctx or default_context(volume.device.index)
+    cv = _cvol(volume, cell)
+    s = _stream(stream)
+    ctx.check(_lib.mcg_mc_classify_slab(ctx.handle, ctypes.byref(cv), int(z0), int(z1), s), "mcg_mc_classify_slab")
+    c = counts(ctx)
+    n = c["vertices"]
+    nz, ny, nx, _ = volume.shape
+    o = _alloc_outputs(n, nx * ny * nz, volume.device, soup, normals, vi2vox, False, tri_cube)
+    mo = _mesh_out(o, n)
+    ctx.check(_lib.mcg_mc_generate(ctx.handle, ctypes.byref(cv), ctypes.byref(mo), s), "mcg_mc_generate")
+    return Mesh(o["soup"], o["normals"], o["vi2vox"], None, o["tri_cube"], c)
+
+
 def extract_into(volume, cell, outputs: dict, capacity, ctx=None, stream=None):
     """Asynchronous extraction into preallocated buffers (no host sync).
 

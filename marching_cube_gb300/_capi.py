@@ -60,6 +60,9 @@ SIGNATURES = {
     "mcg_mc_classify_indexed": (c_int, [c_void_p, ctypes.POINTER(Volume), c_void_p]),
     "mcg_mc_generate_indexed": (c_int, [c_void_p, ctypes.POINTER(Volume), ctypes.POINTER(IndexedOut), c_void_p]),
     "mcg_mc_extract_indexed": (c_int, [c_void_p, ctypes.POINTER(Volume), ctypes.POINTER(IndexedOut), c_void_p]),
+    "mcg_mc_classify_slab": (c_int, [c_void_p, ctypes.POINTER(Volume), c_int32, c_int32, c_void_p]),
+    "mcg_mc_extract_slab": (c_int, [c_void_p, ctypes.POINTER(Volume), c_int32, c_int32, ctypes.POINTER(MeshOut),
+                                    c_void_p]),
     "mcg_mc_extract": (c_int, [c_void_p, ctypes.POINTER(Volume), ctypes.POINTER(MeshOut), c_void_p]),
     "mcg_mc_classify_batched": (c_int, [c_void_p, ctypes.POINTER(Volume), c_int32, c_void_p]),
     "mcg_mc_counts_batched": (c_int, [c_void_p, ctypes.POINTER(MeshCounts), c_int32]),

@@ -90,6 +90,13 @@ __device__ __forceinline__ BrickPos brick_pos(long long b, int nbx, int nby) {
     return p;
 }
 
+// brick b of a slab whose first brick layer starts at voxel z = zbase
+__device__ __forceinline__ BrickPos slab_pos(long long b, int nbx, int nby, int zbase) {
+    BrickPos p = brick_pos(b, nbx, nby);
+    p.z0 += zbase;
+    return p;
+}
+
 // Plain-load fill of a (DX, DY, DZ) tile whose origin is (ox, oy, oz);
 // outside the volume reads as the zero voxel, like the TMA fill.
 template <int VT, int DX, int DY, int DZ>
@@ -197,6 +204,7 @@ cudaError_t upload_tables(int device) {
 struct Geometry {
     int nbx, nby, nbz;
     long long nbricks;
+    int zbase, zlim;  // brick layer 0 starts at voxel z = zbase; cubes exist for z < zlim
 };
 
 Geometry geometry(int nx, int ny, int nz) {
@@ -206,6 +214,20 @@ Geometry geometry(int nx, int ny, int nz) {
     g.nby = (ny - 1 + BY - 1) / BY;
     g.nbz = (nz - 1 + BZ - 1) / BZ;
     g.nbricks = (long long)g.nbx * g.nby * g.nbz;
+    g.zbase = 0;
+    g.zlim = nz - 1;
+    return g;
+}
+
+// the cubes with z0 <= z < z1 (z0 a multiple of the brick depth)
+Geometry geometry_slab(int nx, int ny, int z0, int z1) {
+    Geometry g;
+    g.nbx = (nx - 1 + BX - 1) / BX;
+    g.nby = (ny - 1 + BY - 1) / BY;
+    g.nbz = (z1 - z0 + BZ - 1) / BZ;
+    g.nbricks = (long long)g.nbx * g.nby * g.nbz;
+    g.zbase = z0;
+    g.zlim = z1;
     return g;
 }
 

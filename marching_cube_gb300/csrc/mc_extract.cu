@@ -251,7 +251,7 @@ struct ClsSmemG {
 template <int VT, bool TMA, int G, int CSTAGES>
 __global__ void __launch_bounds__(CLS_THREADS)
     mc_classify_kernel(const __grid_constant__ CUtensorMap map, const typename Vox<VT>::T *__restrict__ vol,
-                       int nx, int ny, int nz, int nbx, int nby, long long nitems, int ngx,
+                       int nx, int ny, int nz, int nbx, int nby, long long nitems, int ngx, int zbase, int zlim,
                        uint32_t *__restrict__ brick_tris, uint32_t *__restrict__ chunk,
                        unsigned int *__restrict__ flags, unsigned int *__restrict__ ticket) {
     using V = Vox<VT>;
@@ -265,7 +265,7 @@ __global__ void __launch_bounds__(CLS_THREADS)
         const long long r = item / ngx;
         bx0 = (int)(item % ngx) * G;
         y0 = (int)(r % nby) * BY;
-        z0 = (int)(r / nby) * BZ;
+        z0 = (int)(r / nby) * BZ + zbase;
     };
     // thread 0 draws the item of the next refill one iteration ahead, so the
     // counter's round trip overlaps the current item
@@ -338,7 +338,7 @@ __global__ void __launch_bounds__(CLS_THREADS)
                 const int h = tid / CUBE_ROWS, c = tid - h * CUBE_ROWS;
                 const int cy = c & (BY - 1), cz = c / BY;
                 unsigned int tri = 0, occ = 0;
-                if (bx0 + h < nbx && y0 + cy < ny - 1 && z0 + cz < nz - 1) {
+                if (bx0 + h < nbx && y0 + cy < ny - 1 && z0 + cz < zlim) {
                     const CubeRow cr = cube_row(S.neg + h * ROWS, S.dead + h * ROWS, cy, cz,
                                                 valid_mask(x0 + h * BX, nx));
                     occ = __popc(cr.occ);
@@ -365,7 +365,7 @@ __global__ void __launch_bounds__(CLS_THREADS)
                 t = S.red[2 * h][0] + S.red[2 * h + 1][0];
                 o = S.red[2 * h][1] + S.red[2 * h + 1][1];
             }
-            const long long b = ((long long)(z0 / BZ) * nby + y0 / BY) * nbx + bx0 + h;
+            const long long b = ((long long)((z0 - zbase) / BZ) * nby + y0 / BY) * nbx + bx0 + h;
             brick_tris[b] = t;
             // per-chunk (CHUNK consecutive bricks) sums feed the scan
             if (t) {
@@ -487,6 +487,7 @@ struct GenParams {
     int nx, ny, nz;
     float cell;
     int nbx, nby;
+    int zbase, zlim;  // z of brick layer 0; cubes exist for z < zlim
     const uint32_t *active;
     const unsigned long long *brick_vofs;
     MeshTotals *totals;
@@ -532,6 +533,7 @@ struct GenOut {
     int16_t *ver_voxel;
     int64_t *tri_cube;
     long long cap;
+    int zlim;  // cubes exist for z < zlim (nz - 1, or the end of a slab)
 };
 
 // All per-brick work of pass 2 once the brick's tile is in shared memory:
@@ -542,7 +544,7 @@ struct GenOut {
 // vertices, and S.vmap when the brick has at most 2048 of them.  Called by
 // every thread (contains __syncthreads); the list is valid after return.
 template <int VT>
-__device__ __forceinline__ void occupied_list(GenSmem<VT> &S, const typename Vox<VT>::T *tile, int nx, int ny, int nz,
+__device__ __forceinline__ void occupied_list(GenSmem<VT> &S, const typename Vox<VT>::T *tile, int nx, int ny, int zlim,
                                               int x0, int y0, int z0) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
         // occupied cubes of the brick, from row masks (voxel rows y0..y0+8, z0..z0+8)
@@ -556,7 +558,7 @@ __device__ __forceinline__ void occupied_list(GenSmem<VT> &S, const typename Vox
         unsigned int cnt = 0, vsum = 0;
         if (tid < CUBE_ROWS) {
             const int cy = tid & (BY - 1), cz = tid / BY;
-            if (y0 + cy < ny - 1 && z0 + cz < nz - 1) cr = cube_row(S.neg, S.dead, cy, cz, valid_mask(x0, nx));
+            if (y0 + cy < ny - 1 && z0 + cz < zlim) cr = cube_row(S.neg, S.dead, cy, cz, valid_mask(x0, nx));
             cnt = __popc(cr.occ);
             unsigned int m = cr.occ;
             while (m) {
@@ -613,7 +615,7 @@ __device__ __forceinline__ void generate_brick(GenSmem<VT> &S, const typename Vo
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const long long N = (long long)nx * ny * nz;
 
-        occupied_list<VT>(S, tile, nx, ny, nz, x0, y0, z0);
+        occupied_list<VT>(S, tile, nx, ny, o.zlim, x0, y0, z0);
         const unsigned int nocc = S.nocc, T_brick = S.total;
         const bool use_map = T_brick <= BRICK_CUBES;
 
@@ -775,12 +777,13 @@ __device__ __forceinline__ void generate_brick(GenSmem<VT> &S, const typename Vo
 // Called by every thread (contains __syncthreads).
 template <int VT>
 __device__ __forceinline__ void backward_brick(GenSmem<VT> &S, const typename Vox<VT>::T *tile, int nx, int ny,
-                                               int nz, float cell, int x0, int y0, int z0, unsigned long long vbase,
+                                               int nz, int zlim, float cell, int x0, int y0, int z0,
+                                               unsigned long long vbase,
                                                const float *__restrict__ grad_pos, float *__restrict__ grad_f,
                                                long long n_grad) {
     using V = Vox<VT>;
     const int tid = threadIdx.x;
-    occupied_list<VT>(S, tile, nx, ny, nz, x0, y0, z0);
+    occupied_list<VT>(S, tile, nx, ny, zlim, x0, y0, z0);
     const unsigned int nocc = S.nocc, T_brick = S.total;
     const bool use_map = T_brick <= BRICK_CUBES;
     for (unsigned int v = tid; v < T_brick; v += THREADS) {
@@ -855,7 +858,7 @@ __global__ void __launch_bounds__(THREADS, 4) mc_generate_kernel(const __grid_co
             if (!more) continue;
             const long long b = S.sbrick[s];
             S.svbase[s] = p.brick_vofs[b];
-            const BrickPos bp = brick_pos(b, p.nbx, p.nby);
+            const BrickPos bp = slab_pos(b, p.nbx, p.nby, p.zbase);
             mbar_arrive_expect_tx(&S.bars[s], GTILE * V::bytes);
             tma_load_3d(S.tiles[s], &map, &S.bars[s], bp.x0 - TXO, bp.y0 - TYO, bp.z0 - TZO);
         }
@@ -883,12 +886,12 @@ __global__ void __launch_bounds__(THREADS, 4) mc_generate_kernel(const __grid_co
             b = S.sbrick[0];
             if (b < 0) break;
             vbase = p.brick_vofs[b];
-            const BrickPos fp = brick_pos(b, p.nbx, p.nby);
+            const BrickPos fp = slab_pos(b, p.nbx, p.nby, p.zbase);
             fill_tile<VT, TX, TY, TZ>(reinterpret_cast<T *>(S.tiles[s]), vol, nx, ny, nz, fp.x0 - TXO,
                                       fp.y0 - TYO, fp.z0 - TZO);
             __syncthreads();
         }
-        const BrickPos bp = brick_pos(b, p.nbx, p.nby);
+        const BrickPos bp = slab_pos(b, p.nbx, p.nby, p.zbase);
         if (MODE == 0) {
             GenOut o;
             o.soup = p.soup;
@@ -897,10 +900,11 @@ __global__ void __launch_bounds__(THREADS, 4) mc_generate_kernel(const __grid_co
             o.ver_voxel = p.ver_voxel;
             o.tri_cube = p.tri_cube;
             o.cap = p.cap;
+            o.zlim = p.zlim;
             generate_brick<VT>(S, tile, vol, nx, ny, nz, cell, bp.x0, bp.y0, bp.z0, vbase, o);
         } else {
-            backward_brick<VT>(S, tile, nx, ny, nz, cell, bp.x0, bp.y0, bp.z0, vbase, p.grad_pos, p.grad_f,
-                               p.n_grad);
+            backward_brick<VT>(S, tile, nx, ny, nz, p.zlim, cell, bp.x0, bp.y0, bp.z0, vbase, p.grad_pos,
+                               p.grad_f, p.n_grad);
         }
         __syncthreads();  // tile s, the list and the stage are free again
         if (TMA && tid == 0) {
@@ -910,7 +914,7 @@ __global__ void __launch_bounds__(THREADS, 4) mc_generate_kernel(const __grid_co
                 pend = next_brick(ticket, nactive);
                 const long long nb2 = S.sbrick[s];
                 S.svbase[s] = p.brick_vofs[nb2];
-                const BrickPos np = brick_pos(nb2, p.nbx, p.nby);
+                const BrickPos np = slab_pos(nb2, p.nbx, p.nby, p.zbase);
                 mbar_arrive_expect_tx(&S.bars[s], GTILE * V::bytes);
                 tma_load_3d(S.tiles[s], &map, &S.bars[s], np.x0 - TXO, np.y0 - TYO, np.z0 - TZO);
             }
@@ -1130,6 +1134,7 @@ __global__ void __launch_bounds__(THREADS, 4)
         o.ver_voxel = d.ver_voxel;
         o.tri_cube = d.tri_cube;
         o.cap = d.cap;
+        o.zlim = d.nz - 1;
         generate_brick<VT>(S, tile, static_cast<const T *>(d.data), d.nx, d.ny, d.nz, d.cell, bp.x0, bp.y0, bp.z0,
                            vbase, o);
         __syncthreads();  // tile s, the list and the stage are free again
@@ -1179,7 +1184,7 @@ void launch_classify_s(const CUtensorMap &map, const mcg_volume *vol, const Geom
     if (grid > nitems) grid = nitems;
     mc_classify_kernel<VT, TMA, G, CSTAGES><<<(int)grid, CLS_THREADS, smem, s>>>(
         map, static_cast<const typename Vox<VT>::T *>(vol->data), vol->nx, vol->ny, vol->nz, g.nbx, g.nby, nitems,
-        ngx, sc.tris, sc.chunk, &sc.totals->flags, &sc.totals->cls_ticket);
+        ngx, g.zbase, g.zlim, sc.tris, sc.chunk, &sc.totals->flags, &sc.totals->cls_ticket);
 }
 
 // pipeline depth of the classify pass (tile stages per CTA); MCG_CLS_STAGES
@@ -1290,6 +1295,8 @@ cudaError_t launch_generate_phase(const mcg_volume *vol, const Geometry &g, cons
     p.cell = vol->cell;
     p.nbx = g.nbx;
     p.nby = g.nby;
+    p.zbase = g.zbase;
+    p.zlim = g.zlim;
     p.active = sc.active;
     p.brick_vofs = sc.vofs;
     p.totals = sc.totals;
@@ -1325,13 +1332,14 @@ Scratch ctx_scratch(mcg_context *ctx) {
 
 using namespace mcg;
 
-mcg_status mcg_mc_classify(mcg_context *ctx, const mcg_volume *vol, mcg_stream_t stream) {
-    if (!ctx || !vol_ok(vol)) return MCG_ERR_INVALID_ARG;
+// count phase over the cubes with z0 <= z < z1
+static mcg_status classify_impl(mcg_context *ctx, const mcg_volume *vol, int32_t z0, int32_t z1,
+                                mcg_stream_t stream) {
     cudaStream_t s = (cudaStream_t)stream;
     cudaError_t e = cudaSetDevice(ctx->device);
     if (e == cudaSuccess) e = upload_tables(ctx->device);
     if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
-    const Geometry g = geometry(vol->nx, vol->ny, vol->nz);
+    const Geometry g = geometry_slab(vol->nx, vol->ny, z0, z1);
     if (!ensure(&ctx->brick_tris, &ctx->brick_tris_cap, (size_t)g.nbricks) ||
         !ensure(&ctx->brick_occ, &ctx->brick_occ_cap, (size_t)(CHUNK_FIELDS * num_chunks(g.nbricks))) ||
         !ensure(&ctx->brick_vofs, &ctx->brick_vofs_cap, (size_t)g.nbricks) ||
@@ -1350,8 +1358,22 @@ mcg_status mcg_mc_classify(mcg_context *ctx, const mcg_volume *vol, mcg_stream_t
     ctx->cls_ny = vol->ny;
     ctx->cls_nz = vol->nz;
     ctx->cls_vtype = vol->voxel_type;
+    ctx->cls_z0 = z0;
+    ctx->cls_z1 = z1;
     ctx->last_capacity = -1;
     return MCG_OK;
+}
+
+mcg_status mcg_mc_classify(mcg_context *ctx, const mcg_volume *vol, mcg_stream_t stream) {
+    if (!ctx || !vol_ok(vol)) return MCG_ERR_INVALID_ARG;
+    return classify_impl(ctx, vol, 0, vol->nz - 1, stream);
+}
+
+mcg_status mcg_mc_classify_slab(mcg_context *ctx, const mcg_volume *vol, int32_t z0, int32_t z1,
+                                mcg_stream_t stream) {
+    if (!ctx || !vol_ok(vol)) return MCG_ERR_INVALID_ARG;
+    if (z0 < 0 || z1 <= z0 || z1 > vol->nz - 1 || z0 % BZ != 0) return MCG_ERR_INVALID_ARG;
+    return classify_impl(ctx, vol, z0, z1, stream);
 }
 
 mcg_status mcg_mc_counts(mcg_context *ctx, mcg_mesh_counts *out) {
@@ -1384,10 +1406,14 @@ mcg_status mcg_mc_generate(mcg_context *ctx, const mcg_volume *vol, const mcg_me
     if (out->capacity_vertices > 0 && !out->soup && !out->soup_normals && !out->vi2vox &&
         !out->ver_voxel && !out->tri_cube)
         return MCG_ERR_INVALID_ARG;
+    // ver_voxel is cleared whole before it is scattered: a slab would clear the
+    // other slabs' entries
+    const bool slab = ctx->cls_z0 != 0 || ctx->cls_z1 != vol->nz - 1;
+    if (slab && out->ver_voxel) return MCG_ERR_INVALID_ARG;
     cudaStream_t s = (cudaStream_t)stream;
     cudaError_t e = cudaSetDevice(ctx->device);
     if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
-    const Geometry g = geometry(vol->nx, vol->ny, vol->nz);
+    const Geometry g = geometry_slab(vol->nx, vol->ny, ctx->cls_z0, ctx->cls_z1);
     e = launch_generate_phase(vol, g, ctx_scratch(ctx), out, ctx->num_sms, s);
     // the totals are re-read so a timeout flagged by generate is reported
     if (e == cudaSuccess)
@@ -1401,6 +1427,13 @@ mcg_status mcg_mc_generate(mcg_context *ctx, const mcg_volume *vol, const mcg_me
 mcg_status mcg_mc_extract(mcg_context *ctx, const mcg_volume *vol, const mcg_mesh_out *out,
                           mcg_stream_t stream) {
     mcg_status st = mcg_mc_classify(ctx, vol, stream);
+    if (st != MCG_OK) return st;
+    return mcg_mc_generate(ctx, vol, out, stream);
+}
+
+mcg_status mcg_mc_extract_slab(mcg_context *ctx, const mcg_volume *vol, int32_t z0, int32_t z1,
+                               const mcg_mesh_out *out, mcg_stream_t stream) {
+    mcg_status st = mcg_mc_classify_slab(ctx, vol, z0, z1, stream);
     if (st != MCG_OK) return st;
     return mcg_mc_generate(ctx, vol, out, stream);
 }
@@ -1436,7 +1469,7 @@ mcg_status mcg_mc_backward(mcg_context *ctx, const mcg_volume *vol, const float 
     cudaStream_t s = (cudaStream_t)stream;
     cudaError_t e = cudaSetDevice(ctx->device);
     if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
-    const Geometry g = geometry(vol->nx, vol->ny, vol->nz);
+    const Geometry g = geometry_slab(vol->nx, vol->ny, ctx->cls_z0, ctx->cls_z1);
     e = cudaMemsetAsync(&ctx->d_totals->gen_ticket, 0, sizeof(unsigned int), s);
     if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
     GenParams p;
@@ -1448,6 +1481,8 @@ mcg_status mcg_mc_backward(mcg_context *ctx, const mcg_volume *vol, const float 
     p.cell = vol->cell;
     p.nbx = g.nbx;
     p.nby = g.nby;
+    p.zbase = g.zbase;
+    p.zlim = g.zlim;
     p.active = ctx->active;
     p.brick_vofs = ctx->brick_vofs;
     p.totals = ctx->d_totals;

@@ -776,6 +776,8 @@ mcg_status mcg_mc_classify_indexed(mcg_context *ctx, const mcg_volume *vol, mcg_
     ctx->cls_ny = vol->ny;
     ctx->cls_nz = vol->nz;
     ctx->cls_vtype = vol->voxel_type;
+    ctx->cls_z0 = 0;
+    ctx->cls_z1 = vol->nz - 1;
     ctx->last_capacity = -1;
     ctx->last_capacity_tris = -1;
     return MCG_OK;

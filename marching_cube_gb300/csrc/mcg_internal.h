@@ -71,6 +71,7 @@ struct mcg_context {
     bool classified = false;
     const void *cls_data = nullptr;
     int cls_nx = 0, cls_ny = 0, cls_nz = 0, cls_vtype = 0;
+    int cls_z0 = 0, cls_z1 = 0;  // cube layers z0 <= z < z1 of the last count phase
     int64_t last_capacity = -1;
     bool cls_indexed = false;        // the last classify was mcg_mc_classify_indexed
     int64_t last_capacity_tris = -1;  // indexed: triangle capacity of the last generate
