@@ -52,6 +52,7 @@ def parse():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-indexed", action="store_true")
     ap.add_argument("--no-stress", action="store_true")
+    ap.add_argument("--no-raycast", action="store_true")
     ap.add_argument("--stress-n", type=int, default=1024, help="stress volume edge (default 1024)")
     return ap.parse_args()
 
@@ -271,6 +272,28 @@ def bench_graph(mcg, synthetic, torch, n=256, frames=20):
     graph_ms = e0.elapsed_time(e1) / frames
     return {"volume": [n, n, n], "frames": frames, "eager_ms_per_frame": eager_ms, "graph_ms_per_frame": graph_ms}
 
+
+
+def bench_raycast(mcg, synthetic, torch, v, reps=20):
+    """Ray casting the headline volume into 640x480 depth + normal maps from
+    poses of the orbit that built it (the fusion loop's model prediction)."""
+    scene = synthetic.FusionScene(seed=0, extent=EXTENT)
+    k = mcg.intrinsic(FX, FY, CX, CY)
+    poses = [mcg.extrinsic(*scene.pose(i, reps)) for i in range(reps)]
+    d = torch.empty((H, W), dtype=torch.float32, device="cuda")
+    n = torch.empty((H, W, 3), dtype=torch.float32, device="cuda")
+    for e in poses[:3]:
+        mcg.raycast(v, k, e, W, H, out_depth=d, out_normal=n)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    for e in poses:
+        mcg.raycast(v, k, e, W, H, out_depth=d, out_normal=n)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    return {"image": [W, H], "ms_per_frame": ms, "rays_per_s": W * H / (ms * 1e-3),
+            "hit_fraction": float((d > 0).float().mean())}
 
 
 def bench_indexed(mcg, torch, vol, cell, ctx, reps=10):
@@ -621,6 +644,13 @@ def main():
         except Exception as ex:  # pragma: no cover
             graph = {"error": str(ex)}
 
+    raycast = None
+    if not args.no_raycast:
+        try:
+            raycast = bench_raycast(mcg, synthetic, torch, v)
+        except Exception as ex:  # pragma: no cover
+            raycast = {"error": str(ex)}
+
     indexed = None
     if not args.no_indexed:
         try:
@@ -668,6 +698,7 @@ def main():
         "graph": graph,
         "adjoint": adjoint,
         "indexed": indexed,
+        "raycast": raycast,
         "stress": stress,
     }
     if rank == 0:

@@ -51,6 +51,13 @@ void _cu_voxel_volumetric_integration(cu_voxel v, float_camera_intrinsic ci, flo
                                       int2 size, float *d_depth_ptr, float3 *d_normal_ptr, uchar3 *d_color_ptr,
                                       bool is_dynamic);
 
+/* ---- ray casting (cu_kinect_fusion_v1.cu:965-986) ---- */
+/* depth (metres) and camera-frame normal maps of size.x x size.y pixels
+ * (device pointers; n_ptr may be NULL); c_ptr (may be NULL) is filled with
+ * white, the reference's default, since the voxel carries no colour */
+void _cu_voxel_extract_depth_and_normal_map(cu_voxel v, float_camera_intrinsic ci, float_camera_extrinsic ce,
+                                            int2 size, float *d_ptr, float3 *n_ptr, uchar3 *c_ptr);
+
 /* ---- depth maps (cu_kinect_fusion_v1.cu:99-151, :275-295) ---- */
 /* host buffers in and out, as the reference's host wrappers */
 void cu_meter_to_vertex(float_camera_intrinsic k, int2 size, float *h_meter, float3 *h_vertex);

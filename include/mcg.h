@@ -259,6 +259,18 @@ mcg_status mcg_integrate_backward(mcg_context *ctx, const void *vol0, int32_t nx
                                   const float *grad_w, float *grad_depth, float *grad_f0, float *grad_w0,
                                   mcg_stream_t stream);
 
+/* ---- ray casting: kf.cu:786-986 (_cu_voxel_extract_depth_and_normal_map) */
+/* Depth (metres, z-depth; 0 where the ray finds no zero crossing) and, if
+ * normal is not NULL, camera-frame normals (float3, (0,0,0) where none) of a
+ * w x h image seen by (k, e) (camera -> global) in a short2 volume of cell
+ * size grid_s.  The march, the trilinear sampler (kf.cu:551-657) and the
+ * surface normal (kf.cu:3146-3233) are the reference's; colour is not part
+ * of the voxel and is not produced.  When K R^T is singular nothing is
+ * written, as the reference then launches nothing. */
+mcg_status mcg_raycast(mcg_context *ctx, const void *vol, int32_t nx, int32_t ny, int32_t nz, float grid_s,
+                       const mcg_intrinsic *k, const mcg_extrinsic *e, int32_t w, int32_t h, float *depth,
+                       float *normal, mcg_stream_t stream);
+
 /* ---- RLE volume codec: kf.cu:1303-1600 ----------------------------------- */
 /* upper bound of the encoded file image size */
 int64_t mcg_rle_bound(int32_t nx, int32_t ny, int32_t nz);

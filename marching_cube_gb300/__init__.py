@@ -541,6 +541,24 @@ def volumetric_integration(v: Voxel, k, e, depth_m, normals=None, is_dynamic=Fal
               "mcg_integrate")
 
 
+def raycast(v: Voxel, k, e, w, h, normals=True, out_depth=None, out_normal=None, ctx=None, stream=None):
+    """_cu_voxel_extract_depth_and_normal_map (kf.cu:786-986): depth (h, w)
+    metres and camera-frame normals (h, w, 3) of a short2 volume seen by
+    camera (k, e).  out_* may supply preallocated outputs."""
+    if v.data.dtype != torch.int16:
+        raise TypeError("ray casting reads short2 (int16) volumes")
+    _check_volume(v.data)
+    ctx = ctx or default_context(v.data.device.index)
+    nx, ny, nz = v.size
+    dev = v.data.device
+    d = out_depth if out_depth is not None else torch.empty((h, w), dtype=torch.float32, device=dev)
+    n = out_normal if out_normal is not None else (
+        torch.empty((h, w, 3), dtype=torch.float32, device=dev) if normals else None)
+    ctx.check(_lib.mcg_raycast(ctx.handle, _ptr(v.data), nx, ny, nz, v.grid_s, ctypes.byref(k), ctypes.byref(e), w, h,
+                               _ptr(d), _ptr(n), _stream(stream)), "mcg_raycast")
+    return d, n
+
+
 def extrinsic_tensor(R, t, device=None):
     """Pose as a 12-float device tensor (rotation column-major, then t) for
     volumetric_integration_device_pose."""

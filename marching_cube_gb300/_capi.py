@@ -82,6 +82,8 @@ SIGNATURES = {
     "mcg_integrate": (c_int, [c_void_p, c_void_p, c_int32, c_int32, c_int32, c_int32, c_float, c_float,
                               c_float, ctypes.POINTER(Intrinsic), ctypes.POINTER(Extrinsic), c_int32,
                               c_int32, c_void_p, c_void_p, c_int32, c_void_p]),
+    "mcg_raycast": (c_int, [c_void_p, c_void_p, c_int32, c_int32, c_int32, c_float, ctypes.POINTER(Intrinsic),
+                            ctypes.POINTER(Extrinsic), c_int32, c_int32, c_void_p, c_void_p, c_void_p]),
     "mcg_integrate_backward": (c_int, [c_void_p, c_void_p, c_int32, c_int32, c_int32, c_float, c_float, c_float,
                                        ctypes.POINTER(Intrinsic), c_int32, c_void_p, c_int32, c_int32, c_void_p,
                                        c_void_p, c_int32, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,

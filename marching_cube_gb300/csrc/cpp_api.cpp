@@ -384,6 +384,19 @@ void _cu_voxel_volumetric_integration(cu_voxel v, float_camera_intrinsic ci, flo
     check(cudaDeviceSynchronize(), "_cu_voxel_volumetric_integration");
 }
 
+void _cu_voxel_extract_depth_and_normal_map(cu_voxel v, float_camera_intrinsic ci, float_camera_extrinsic ce,
+                                            int2 size, float *d_ptr, float3 *n_ptr, uchar3 *c_ptr) {
+    mcg_context *ctx = thread_ctx();
+    const mcg_intrinsic k = to_intrinsic(ci);
+    const mcg_extrinsic e = to_extrinsic(ce);
+    // the voxel carries no colour: the colour map keeps the reference's default, white
+    if (c_ptr) check(cudaMemset(c_ptr, 0xff, sizeof(uchar3) * (size_t)size.x * size.y), "cudaMemset");
+    check_status(mcg_raycast(ctx, v.data, v.size.x, v.size.y, v.size.z, v.grid_s, &k, &e, size.x, size.y, d_ptr,
+                             (float *)n_ptr, nullptr),
+                 ctx, "mcg_raycast");
+    check(cudaDeviceSynchronize(), "_cu_voxel_extract_depth_and_normal_map");
+}
+
 void cu_kinect_depth_to_maps(float_camera_intrinsic k, int2 size, const unsigned short *d_depth_mm, float *d_meter,
                              float3 *d_vertex, float3 *d_normal) {
     mcg_context *ctx = thread_ctx();

@@ -61,6 +61,7 @@ def lib():
             "orc_rle_decode_volume": (i32, [vp, i64, vp, i64, vp, vp]),
             "orc_max_threads": (i32, []),
             "orc_mc_edges": (i64, [vp, i32, i32, i32, i32, vp, vp, i64]),
+            "orc_raycast": (i32, [vp, i32, i32, i32, f32, vp, vp, i32, i32, vp, vp, i32]),
             "orc_mc_edge_vertices": (None, [vp, i32, i32, i32, i32, f32, vp, i64, vp, vp, vp]),
             "orc_mc_backward_f64": (i64, [vp, i32, i32, i32, i32, f64, vp, i64, vp]),
             "orc_integrate_seq_f64": (None, [vp, i32, i32, i32, f32, f32, f32, vp, i32, vp, i32, i32, vp, vp, i32,
@@ -380,3 +381,20 @@ def mc_edge_vertices(vol, cell, keys):
     v2v = np.zeros((n, 3), np.int32)
     lib().orc_mc_edge_vertices(_p(vol), vt, nx, ny, nz, float(cell), _p(keys), n, _p(pos), _p(nrm), _p(v2v))
     return pos, nrm, v2v
+
+
+# ---------------------------------------------------------------------------
+# ray casting (kf.cu:551-659, 786-986)
+# ---------------------------------------------------------------------------
+def raycast(vol, grid_s, k, e, w, h, normals=True, nthreads=0):
+    """(depth (h, w) metres, normal (h, w, 3) or None) of a short2 volume seen
+    by camera (k, e); None if the camera matrix is singular."""
+    vol = np.ascontiguousarray(vol)
+    if vol.dtype != np.int16:
+        raise TypeError("ray casting reads short2 volumes")
+    nz, ny, nx, _ = vol.shape
+    depth = np.zeros((h, w), np.float32)
+    nrm = np.zeros((h, w, 3), np.float32) if normals else None
+    ok = lib().orc_raycast(_p(vol), nx, ny, nz, float(grid_s), ctypes.byref(k), ctypes.byref(e), w, h, _p(depth),
+                           _p(nrm), nthreads)
+    return (depth, nrm) if ok else None

@@ -944,3 +944,149 @@ void orc_mc_edge_vertices(const void *vol, int vtype, int nx, int ny, int nz, fl
         if (normals) orc_surface_normal(vol, vtype, nx, ny, nz, cell, P, normals + 3 * i);
     }
 }
+
+/* ------------------------------------------------------------------------ */
+/* ray casting (cu_kinect_fusion_v1.cu:551-659, 786-986), short2 volumes,    */
+/* FP32 mirror.  Colour is not part of the voxel, so it is not produced.     */
+/* ------------------------------------------------------------------------ */
+
+/* d_voxel_extract_trilinear_interpolated_sdf (:551-657): the samples in the
+ * order V000, V100, V010, V001, V101, V011, V110, V111; the first +-32766 met
+ * returns +-1; float_interpolation_trilinear (cu_math_functions.h:107-111) */
+static float trilinear_sdf(const orc_voxel *vol, int nx, int ny, const float p[3]) {
+    int pi[3] = {(int)p[0], (int)p[1], (int)p[2]};
+    float t[3] = {p[0] - (float)pi[0], p[1] - (float)pi[1], p[2] - (float)pi[2]};
+    static const int O[8][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {1, 0, 1}, {0, 1, 1}, {1, 1, 0}, {1, 1, 1}};
+    float s[8];
+    for (int k = 0; k < 8; ++k) {
+        int16_t v = vol[lin(nx, ny, pi[0] + O[k][0], pi[1] + O[k][1], pi[2] + O[k][2])].tsdf;
+        if (v == ORC_MAX_TSDF) return 1.0f;
+        if (v == -ORC_MAX_TSDF) return -1.0f;
+        s[k] = unpack_tsdf(v);
+    }
+    float a = 1.0f - t[0], b = 1.0f - t[1], c = 1.0f - t[2];
+    float x = t[0], y = t[1], z = t[2];
+    return s[0] * a * b * c + s[1] * x * b * c + s[2] * a * y * c + s[3] * a * b * z + s[4] * x * b * z +
+           s[5] * a * y * z + s[6] * x * y * c + s[7] * x * y * z;
+}
+
+/* camera set-up of _cu_voxel_extract_depth_and_normal_map (:965-986):
+ * K (cu_geometry_functions.h:248-255), M = K R^T (matrix33_mt), IM = M^-1
+ * (float33_inv, cu_vector_functions.h:555-575), camera centre t / grid_s.
+ * Matrices are three column vectors m[j][i] (column j, component i).
+ * Returns 0 when M is singular (the reference then launches nothing). */
+int orc_raycast_setup(const orc_intrinsic *k, const orc_extrinsic *e, float grid_s, float IM[3][3], float cc[3]) {
+    float K[3][3] = {{k->fx, 0.0f, 0.0f}, {0.0f, k->fy, 0.0f}, {k->cx, k->cy, 1.0f}};
+    float R[3][3];
+    for (int j = 0; j < 3; ++j)
+        for (int i = 0; i < 3; ++i) R[j][i] = e->r[3 * j + i];
+    float M[3][3];
+    for (int j = 0; j < 3; ++j)
+        for (int i = 0; i < 3; ++i) M[j][i] = K[0][i] * R[0][j] + K[1][i] * R[1][j] + K[2][i] * R[2][j];
+    float A = M[2][2] * M[1][1] - M[2][1] * M[1][2];
+    float B = M[0][2] * M[2][1] - M[0][1] * M[2][2];
+    float C = M[0][1] * M[1][2] - M[0][2] * M[1][1];
+    float det = M[0][0] * A + M[1][0] * B + M[2][0] * C;
+    if (det > -FLT_EPSILON && det < FLT_EPSILON) return 0;
+    IM[0][0] = A;
+    IM[0][1] = B;
+    IM[0][2] = C;
+    IM[1][0] = M[1][2] * M[2][0] - M[1][0] * M[2][2];
+    IM[1][1] = M[0][0] * M[2][2] - M[0][2] * M[2][0];
+    IM[1][2] = M[0][2] * M[1][0] - M[0][0] * M[1][2];
+    IM[2][0] = M[1][0] * M[2][1] - M[1][1] * M[2][0];
+    IM[2][1] = M[0][1] * M[2][0] - M[0][0] * M[2][1];
+    IM[2][2] = M[0][0] * M[1][1] - M[0][1] * M[1][0];
+    for (int j = 0; j < 3; ++j)
+        for (int i = 0; i < 3; ++i) IM[j][i] = IM[j][i] / det;
+    for (int i = 0; i < 3; ++i) cc[i] = e->t[i] / grid_s;
+    return 1;
+}
+
+/* d_voxel_extract_depth_and_normal_map (:786-963) for every pixel.  depth:
+ * w*h metres (0 where nothing is hit); normal: w*h*3 (may be NULL),
+ * (0,0,0) where nothing is hit.  Returns 0 (and writes nothing) when the
+ * camera matrix is singular. */
+int orc_raycast(const orc_voxel *vol, int nx, int ny, int nz, float grid_s, const orc_intrinsic *k,
+                const orc_extrinsic *e, int w, int h, float *depth, float *normal, int nthreads) {
+    float IM[3][3], cc[3];
+    if (!orc_raycast_setup(k, e, grid_s, IM, cc)) return 0;
+    nthreads = nthreads_or_default(nthreads);
+#pragma omp parallel for schedule(dynamic, 4) num_threads(nthreads)
+    for (int y = 0; y < h; ++y)
+        for (int x = 0; x < w; ++x) {
+            int64_t idx = (int64_t)y * w + x;
+            depth[idx] = 0.0f;
+            if (normal) normal[3 * idx] = normal[3 * idx + 1] = normal[3 * idx + 2] = 0.0f;
+            const float margin = 1.0f;
+            float x_max = (float)nx - margin, y_max = (float)ny - margin, z_max = (float)nz - margin;
+            const float dt_max = 1.0f, dt_min = 0.25f;
+            float dt = dt_max;
+            int dt_status = 0;
+            float fx = (float)x, fy = (float)y;
+            /* float33_mv_2 (cu_vector_functions.h:623-626, matrix33_mv_2) */
+            float rd[3] = {IM[0][0] * fx + IM[1][0] * fy + IM[2][0], IM[0][1] * fx + IM[1][1] * fy + IM[2][1],
+                           IM[0][2] * fx + IM[1][2] * fy + IM[2][2]};
+            unit3(rd);
+            for (int i = 0; i < 3; ++i)
+                if (rd[i] == 0.0f) rd[i] = (float)1e-15;
+            float t_min = FLT_MAX, t_max = 0.0f, t, t1 = 0.0f, t2, sdf, sdf1 = 1.0f;
+            const float lo[3] = {margin, margin, margin}, hi[3] = {x_max, y_max, z_max};
+            /* entry / exit over the six faces x = margin, x_max, y = ..., z = ... */
+            for (int ax = 0; ax < 3; ++ax) {
+                int a1 = ax == 0 ? 1 : 0, a2 = ax == 2 ? 1 : 2;
+                for (int side = 0; side < 2; ++side) {
+                    float plane = side == 0 ? margin : hi[ax];
+                    t = (plane - cc[ax]) / rd[ax];
+                    if (t > 0) {
+                        float u1 = rd[a1] * t + cc[a1];
+                        float u2 = rd[a2] * t + cc[a2];
+                        if (u1 > lo[a1] && u1 < hi[a1] && u2 > lo[a2] && u2 < hi[a2]) {
+                            if (t < t_min) t_min = t;
+                            if (t > t_max) t_max = t;
+                        }
+                    }
+                }
+            }
+            if (t_min == FLT_MAX && t_max == 0.0f) continue;
+            if (t_min == t_max) t_min = dt * margin;
+            for (t = t_min; t < t_max; t += dt) {
+                float p[3] = {rd[0] * t + cc[0], rd[1] * t + cc[1], rd[2] * t + cc[2]};
+                if (p[0] < 0.0f || p[1] < 0.0f || p[2] < 0.0f || p[0] >= x_max || p[1] >= y_max || p[2] >= z_max)
+                    continue;
+                sdf = trilinear_sdf(vol, nx, ny, p);
+                if (sdf < 0.0f && sdf > -1.0f && sdf1 >= 0.0f && sdf1 < 1.0f) {
+                    t2 = t1 - dt * sdf1 / (sdf - sdf1); /* eq. (15) */
+                    float np[3] = {rd[0] * t2, rd[1] * t2, rd[2] * t2};
+                    float tp[3] = {np[0] + cc[0], np[1] + cc[1], np[2] + cc[2]};
+                    float p2x = (fx - k->cx) / k->fx, p2y = (fy - k->cy) / k->fy;
+                    float nn = sqrtf(np[0] * np[0] + np[1] * np[1] + np[2] * np[2]);
+                    depth[idx] = nn / sqrtf(p2x * p2x + p2y * p2y + 1.0f) * grid_s;
+                    if (normal) {
+                        float sn[3];
+                        orc_surface_normal(vol, ORC_VOXEL_SHORT2, nx, ny, nz, 1.0f, tp, sn);
+                        /* float33_tv (matrix33_tv): R^T n */
+                        for (int i = 0; i < 3; ++i)
+                            normal[3 * idx + i] = e->r[3 * i] * sn[0] + e->r[3 * i + 1] * sn[1] + e->r[3 * i + 2] * sn[2];
+                    }
+                    break;
+                } else if (sdf1 <= 0.0f && sdf1 > -1.0f && sdf >= 0.0f && sdf < 1.0f) {
+                    break; /* back face */
+                }
+                if (sdf > -1.0f && sdf < 1.0f) {
+                    if (!dt_status) {
+                        t -= dt;
+                        dt_status = 1;
+                        dt = dt_min;
+                        continue;
+                    }
+                } else if (dt_status) {
+                    dt_status = 0;
+                    dt = dt_max;
+                }
+                t1 = t;
+                sdf1 = sdf;
+            }
+        }
+    return 1;
+}

@@ -125,6 +125,15 @@ void orc_integrate_seq_backward_f64(const float *vol0, int nx, int ny, int nz, f
 void orc_mc_edge_vertices(const void *vol, int vtype, int nx, int ny, int nz, float cell, const int64_t *keys,
                           int64_t n, float *pos, float *normals, int32_t *vi2vox);
 
+/* ---- ray casting (kf.cu:551-659, 786-986), short2 volumes --------------- */
+/* camera set-up (:965-986): IM = (K R^T)^-1 as columns IM[j][i], cc = t /
+ * grid_s; 0 if singular */
+int orc_raycast_setup(const orc_intrinsic *k, const orc_extrinsic *e, float grid_s, float IM[3][3], float cc[3]);
+/* depth (metres, 0 = no hit) and normal (may be NULL) maps of w x h pixels;
+ * 0 (nothing written) if the camera matrix is singular */
+int orc_raycast(const orc_voxel *vol, int nx, int ny, int nz, float grid_s, const orc_intrinsic *k,
+                const orc_extrinsic *e, int w, int h, float *depth, float *normal, int nthreads);
+
 int orc_max_threads(void);
 
 #ifdef __cplusplus
