@@ -53,6 +53,7 @@ def parse():
     ap.add_argument("--no-indexed", action="store_true")
     ap.add_argument("--no-stress", action="store_true")
     ap.add_argument("--no-raycast", action="store_true")
+    ap.add_argument("--no-text-load", action="store_true")
     ap.add_argument("--stress-n", type=int, default=1024, help="stress volume edge (default 1024)")
     return ap.parse_args()
 
@@ -294,6 +295,76 @@ def bench_raycast(mcg, synthetic, torch, v, reps=20):
     ms = e0.elapsed_time(e1) / reps
     return {"image": [W, H], "ms_per_frame": ms, "rays_per_s": W * H / (ms * 1e-3),
             "hit_fraction": float((d > 0).float().mean())}
+
+
+def bench_text_load(mcg, synthetic, torch, v, hbm, reps=10, sample_bytes=48 << 20):
+    """Text-record loader (cu_voxel_rlc_to_mesh's volume load): the headline
+    512^3 volume dumped as "x y z sdf weight" records of the window at
+    (512, 512, 0), x outermost, z innermost (~3 GB of text), loaded back
+    (a) from device memory, (b) from pageable host memory through the
+    reader-thread staging, (c) from pinned host memory; beside it the
+    reference loop over libstdc++ streams on a bounded sample, one core."""
+    import numpy as np
+    n = v.data.shape[0]
+    text = synthetic.text_dump(v.data, mcg.TEXT_ORIGIN)
+    L = text.numel()
+    out = torch.empty_like(v.data)
+    stats = {}
+    mcg.load_text_records(text, n, out=out, stats=stats)
+    assert stats["stored"] == n ** 3 and torch.equal(out, v.data)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for _ in range(3):
+        mcg.load_text_records(text, n, out=out)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(reps):
+        mcg.load_text_records(text, n, out=out)
+    e1.record()
+    torch.cuda.synchronize()
+    dev_ms = e0.elapsed_time(e1) / reps
+    host = np.empty(L, np.uint8)
+    host[:] = text.cpu().numpy()
+    pinned = torch.empty(L, dtype=torch.uint8, pin_memory=True)
+    pinned.copy_(text)
+    del text
+    torch.cuda.empty_cache()
+    res = {}
+    for name, src in (("pageable", host), ("pinned", pinned)):
+        for _ in range(2):
+            mcg.load_text_records(src, n, out=out)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(max(3, reps // 2)):
+            mcg.load_text_records(src, n, out=out)
+        torch.cuda.synchronize()
+        res[name] = (time.perf_counter() - t0) / max(3, reps // 2)
+    assert torch.equal(out, v.data)
+    # CPU: the reference loop on the first sample_bytes (cut after a newline)
+    cpu = None
+    try:
+        import oracle as orc
+        cut = int(np.flatnonzero(host[:sample_bytes] == 10)[-1]) + 1
+        sample = host[:cut].tobytes()
+        t0 = time.perf_counter()
+        _, st = orc.text_load(sample, n, mcg.TEXT_ORIGIN)
+        cs = time.perf_counter() - t0
+        cpu = {"value": cut / cs / 1e9, "unit": "GB/s of text", "cores": 1, "kind": "port",
+               "sample": "first %d bytes (%d records) of the same dump" % (cut, st["stored"]),
+               "seconds": cs}
+    except Exception as ex:  # pragma: no cover
+        cpu = {"value": None, "error": str(ex)}
+    del host, pinned
+    alg = L + 4 * n ** 3
+    return {"workload": "text dump of the 512^3 window at (512,512,0), %d records" % n ** 3,
+            "text_bytes": L, "device_ms": dev_ms, "device_gbs": L / (dev_ms * 1e-3) / 1e9,
+            "records_per_s": n ** 3 / (dev_ms * 1e-3),
+            "roofline": {"bound": "hbm", "alg_bytes": alg, "achieved": alg / (dev_ms * 1e-3) / 1e9,
+                         "peak": hbm, "frac": alg / (dev_ms * 1e-3) / 1e9 / hbm,
+                         "note": "text read once + volume written once over the whole six-kernel parse"},
+            "e2e_pageable": {"ms": res["pageable"] * 1e3, "gbs": L / res["pageable"] / 1e9,
+                             "h2d_bytes": L},
+            "e2e_pinned": {"ms": res["pinned"] * 1e3, "gbs": L / res["pinned"] / 1e9, "h2d_bytes": L},
+            "cpu_baseline": cpu}
 
 
 def bench_indexed(mcg, torch, vol, cell, ctx, reps=10):
@@ -651,6 +722,14 @@ def main():
         except Exception as ex:  # pragma: no cover
             raycast = {"error": str(ex)}
 
+    text_load = None
+    if not args.no_text_load:
+        try:
+            text_load = bench_text_load(mcg, synthetic, torch, v, hbm)
+        except Exception as ex:  # pragma: no cover
+            text_load = {"error": str(ex)}
+        torch.cuda.empty_cache()
+
     indexed = None
     if not args.no_indexed:
         try:
@@ -699,6 +778,7 @@ def main():
         "adjoint": adjoint,
         "indexed": indexed,
         "raycast": raycast,
+        "text_load": text_load,
         "stress": stress,
     }
     if rank == 0:

@@ -298,6 +298,46 @@ mcg_status mcg_rle_decode_host(const uint8_t *image, int64_t size, void *vol, in
 mcg_status mcg_rle_decode(mcg_context *ctx, const uint8_t *image, int64_t size, void *vol,
                           int64_t capacity_voxels, mcg_stream_t stream);
 
+/* ---- text-record volume loader: kf.cu:3289-3361 ---------------------------- */
+/* The loop of cu_voxel_rlc_to_mesh: integers read five at a time as
+ * "x y z sdf weight" records with `ifs >> int` (C++ formatted input:
+ * white space skipped, optional sign, decimal digits, int range); records
+ * inside [origin, origin + dim)^3 fill the dim^3 short2 device volume vol in
+ * arrival order, z fastest, then y, then x (v[zi*dim*dim + yi*dim + xi] =
+ * {(short)sdf, (ushort)weight}), until dim^3 are stored.  The reference
+ * passes origin {512, 512, 0}.  The volume is zeroed first (the reference's
+ * host array is uninitialised).  The end of the stream follows the
+ * reference's `while (!ifs.eof())` loop: text ending in white space repeats
+ * the last record; a partial record takes its missing fields from the record
+ * before; a failed field (no digits, or outside int) reads 0 / INT_MAX /
+ * INT_MIN, and unless it ran into end of file that record repeats into every
+ * remaining voxel -- or, when it lies outside the window, the reference
+ * never returns: MCG_ERR_FORMAT here, with the voxels stored before it.
+ * Parsed on the device; synchronous. */
+typedef struct mcg_text_info {
+    int64_t bytes;        /* text bytes parsed */
+    int64_t numbers;      /* integers extracted before the stream ended */
+    int64_t records;      /* complete records, numbers / 5 */
+    int64_t stored;       /* voxels written in arrival order (<= dim^3) */
+    int64_t fail_offset;  /* byte offset of the first failed extraction, -1 if none */
+    int32_t filled_rest;  /* 1: a failed record inside the window filled the remaining voxels */
+    int32_t reserved;
+} mcg_text_info;
+/* text: device bytes (e.g. read by GPUDirect or produced on the device) */
+mcg_status mcg_text_records_parse(mcg_context *ctx, const void *text, int64_t len, int32_t dim,
+                                  const int32_t origin[3], void *vol, mcg_text_info *info, mcg_stream_t stream);
+/* text: host bytes; copied through pinned staging by reader threads */
+mcg_status mcg_text_records_load(mcg_context *ctx, const void *text, int64_t len, int32_t dim,
+                                 const int32_t origin[3], void *vol, mcg_text_info *info, mcg_stream_t stream);
+/* The last tail_bytes of a file, as kf.cu:3316-3317 seeks (tail 11e9): the
+ * line cut by the seek is skipped.  A file no longer than tail_bytes (or
+ * tail_bytes <= 0) is read whole, from offset 0, without skipping a line;
+ * the reference's seek fails there and its loop never ends.  MCG_ERR_IO when
+ * the file cannot be opened or read. */
+mcg_status mcg_text_records_load_file(mcg_context *ctx, const char *path, int64_t tail_bytes, int32_t dim,
+                                      const int32_t origin[3], void *vol, mcg_text_info *info,
+                                      mcg_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -844,3 +844,61 @@ def run_length_decode(file_name, device=None) -> Voxel:
     """cu_voxel_run_length_decode (kf.cu:1533-1563), whole-volume form."""
     with open(file_name, "rb") as f:
         return rle_decode(f.read(), device)
+
+
+# ---------------------------------------------------------------------------
+# text-record volume loader (kf.cu:3289-3361)
+# ---------------------------------------------------------------------------
+TEXT_TAIL_BYTES = 11_000_000_000   # kf.cu:3316 seekg(-11000000000, end)
+TEXT_ORIGIN = (512, 512, 0)        # kf.cu:3314 xs, ys, zs
+TEXT_GRID_S = 0.003                # kf.cu:3271 local_volume.grid_s
+
+
+def load_text_records(source, dim, origin=TEXT_ORIGIN, tail_bytes=TEXT_TAIL_BYTES, out=None, grid_s=TEXT_GRID_S,
+                      stats=None, device=None, ctx=None, stream=None) -> Voxel:
+    """The volume loader of cu_voxel_rlc_to_mesh: "x y z sdf weight" text
+    records inside [origin, origin + dim)^3 fill a dim^3 short2 volume in
+    arrival order (z fastest, then y, then x), parsed on the GPU.
+
+    source: a path (the last tail_bytes of the file, the reference's seek and
+    line skip; tail_bytes=None reads it whole), host bytes (bytes, bytearray,
+    memoryview, numpy uint8, CPU uint8 tensor) or a CUDA uint8 tensor.
+    out: optional (dim, dim, dim, 2) int16 CUDA tensor to fill.  stats: an
+    optional dict receiving the mcg_text_info fields.  Raises MCGError with
+    MCG_ERR_FORMAT where the reference's loop would never end."""
+    import numpy as np
+    dim = int(dim)
+    if out is None:
+        if device is None:
+            device = torch.device("cuda", torch.cuda.current_device())
+        out = torch.empty((dim, dim, dim, 2), dtype=torch.int16, device=device)
+    elif out.dtype != torch.int16 or tuple(out.shape) != (dim, dim, dim, 2) or not out.is_contiguous() \
+            or not out.is_cuda:
+        raise ValueError("out must be a contiguous (dim, dim, dim, 2) int16 CUDA tensor")
+    ctx = ctx or default_context(out.device.index)
+    org = (ctypes.c_int32 * 3)(*(int(o) for o in origin))
+    info = _capi.TextInfo()
+    if isinstance(source, (str, os.PathLike)):
+        tail = 0 if tail_bytes is None else int(tail_bytes)
+        st = _lib.mcg_text_records_load_file(ctx.handle, os.fsencode(source), tail, dim, org, _ptr(out),
+                                             ctypes.byref(info), _stream(stream))
+        what = "mcg_text_records_load_file"
+    elif isinstance(source, torch.Tensor) and source.is_cuda:
+        if source.dtype != torch.uint8 or not source.is_contiguous():
+            raise ValueError("device text must be a contiguous uint8 tensor")
+        st = _lib.mcg_text_records_parse(ctx.handle, _ptr(source), source.numel(), dim, org, _ptr(out),
+                                         ctypes.byref(info), _stream(stream))
+        what = "mcg_text_records_parse"
+    else:
+        if isinstance(source, torch.Tensor):
+            source = source.numpy()
+        arr = np.frombuffer(source, dtype=np.uint8) if not isinstance(source, np.ndarray) else source
+        if arr.dtype != np.uint8 or not arr.flags.c_contiguous:
+            raise ValueError("host text must be contiguous bytes")
+        st = _lib.mcg_text_records_load(ctx.handle, arr.ctypes.data_as(ctypes.c_void_p), arr.size, dim, org,
+                                        _ptr(out), ctypes.byref(info), _stream(stream))
+        what = "mcg_text_records_load"
+    if stats is not None:
+        stats.update({k: getattr(info, k) for k, _ in _capi.TextInfo._fields_ if k != "reserved"})
+    ctx.check(st, what)
+    return Voxel(out, 0.0, 0.0, float(grid_s))

@@ -37,6 +37,11 @@ class MeshCounts(ctypes.Structure):
                 ("active_bricks", c_int64), ("status", c_int32), ("reserved", c_int32)]
 
 
+class TextInfo(ctypes.Structure):
+    _fields_ = [("bytes", c_int64), ("numbers", c_int64), ("records", c_int64), ("stored", c_int64),
+                ("fail_offset", c_int64), ("filled_rest", c_int32), ("reserved", c_int32)]
+
+
 class Intrinsic(ctypes.Structure):
     _fields_ = [("fx", c_float), ("fy", c_float), ("cx", c_float), ("cy", c_float),
                 ("dc", c_float * 5)]
@@ -99,6 +104,12 @@ SIGNATURES = {
     "mcg_rle_decode_host": (c_int, [c_void_p, c_int64, c_void_p, c_int64]),
     "mcg_rle_header": (c_int, [c_void_p, c_int64, ctypes.POINTER(c_int32), ctypes.POINTER(c_float)]),
     "mcg_rle_decode": (c_int, [c_void_p, c_void_p, c_int64, c_void_p, c_int64, c_void_p]),
+    "mcg_text_records_parse": (c_int, [c_void_p, c_void_p, c_int64, c_int32, ctypes.POINTER(c_int32), c_void_p,
+                                       ctypes.POINTER(TextInfo), c_void_p]),
+    "mcg_text_records_load": (c_int, [c_void_p, c_void_p, c_int64, c_int32, ctypes.POINTER(c_int32), c_void_p,
+                                      ctypes.POINTER(TextInfo), c_void_p]),
+    "mcg_text_records_load_file": (c_int, [c_void_p, ctypes.c_char_p, c_int64, c_int32, ctypes.POINTER(c_int32),
+                                           c_void_p, ctypes.POINTER(TextInfo), c_void_p]),
 }
 
 

@@ -83,6 +83,13 @@ mcg_status mcg_destroy(mcg_context *ctx) {
     cudaFree(ctx->depth_scaled);
     cudaFree(ctx->ray_x);
     if (ctx->h_ray_x) cudaFreeHost(ctx->h_ray_x);
+    cudaFree(ctx->tr_text);
+    cudaFree(ctx->tr_tok);
+    cudaFree(ctx->tr_seg);
+    cudaFree(ctx->tr_cta);
+    cudaFree(ctx->tr_scan);
+    if (ctx->h_tr_scan) cudaFreeHost(ctx->h_tr_scan);
+    if (ctx->h_tr_stage) cudaFreeHost(ctx->h_tr_stage);
     delete ctx;
     return MCG_OK;
 }

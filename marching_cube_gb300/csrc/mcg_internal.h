@@ -113,6 +113,21 @@ struct mcg_context {
     size_t h_ray_x_cap = 0;
     int ray_x_n = 0;
     float ray_x_g = 0.0f;
+
+    // text-record loader: the text on the device, its fields, per-segment
+    // and per-CTA counts, the result block and pinned staging
+    uint8_t *tr_text = nullptr;
+    size_t tr_text_cap = 0;
+    int *tr_tok = nullptr;
+    size_t tr_tok_cap = 0;
+    long long *tr_seg = nullptr;
+    size_t tr_seg_cap = 0;
+    long long *tr_cta = nullptr;
+    size_t tr_cta_cap = 0;
+    unsigned char *tr_scan = nullptr;
+    size_t tr_scan_cap = 0;
+    unsigned char *h_tr_scan = nullptr;   // pinned
+    uint8_t *h_tr_stage = nullptr;        // pinned, reader-thread staging
 };
 
 // records a CUDA failure on ctx and returns the matching status

@@ -320,3 +320,62 @@ def mm_to_u16_bits(mm):
     pattern (the depth kernels read the 16 bits as unsigned)."""
     m = mm.to(torch.int32) & 0xFFFF
     return torch.where(m >= 32768, m - 65536, m).to(torch.int16)
+
+
+# ---------------------------------------------------------------------------
+# text dumps of a volume: "x y z sdf weight\n" per voxel, x outermost, z
+# innermost (the record order the loader of cu_voxel_rlc_to_mesh expects,
+# kf.cu:3289-3358), formatted on the device with torch ops
+# ---------------------------------------------------------------------------
+def _format_ints(v, width):
+    """(n, width) uint8 right-aligned decimal text of int64 tensor v; unused
+    leading columns hold 0 (removed by the caller)."""
+    n = v.shape[0]
+    out = torch.zeros((n, width), dtype=torch.uint8, device=v.device)
+    neg = v < 0
+    a = v.abs()
+    nd = torch.ones_like(a)
+    t = a // 10
+    for p in range(1, width):
+        nd = nd + (t > 0).to(nd.dtype)
+        t = t // 10
+    t = a
+    for p in range(width):
+        col = width - 1 - p
+        d = (t % 10).to(torch.uint8) + 48
+        out[:, col] = torch.where(p < nd, d, torch.zeros_like(d))
+        t = t // 10
+    rows = torch.nonzero(neg).squeeze(1)
+    if rows.numel():
+        out[rows, (width - 1 - nd[rows])] = 45
+    return out
+
+
+def text_dump(values, box_origin=(0, 0, 0), records_per_chunk=1 << 24):
+    """uint8 CUDA tensor of the text records of a (nz, ny, nx, 2) int16
+    volume whose voxel (0, 0, 0) sits at box_origin; "%d %d %d %d %d\\n" per
+    voxel, x outermost, z innermost, weights printed unsigned."""
+    nz, ny, nx, _ = values.shape
+    dev = values.device
+    bx, by, bz = (int(o) for o in box_origin)
+    vt = values.permute(2, 1, 0, 3).reshape(-1, 2)  # x, y, z order
+    n = vt.shape[0]
+    wid = [len(str(max(abs(bx), abs(bx + nx)))) + 1, len(str(max(abs(by), abs(by + ny)))) + 1,
+           len(str(max(abs(bz), abs(bz + nz)))) + 1, 6, 5]
+    parts = []
+    for s in range(0, n, records_per_chunk):
+        e = min(n, s + records_per_chunk)
+        i = torch.arange(s, e, device=dev, dtype=torch.int64)
+        z = i % nz + bz
+        y = (i // nz) % ny + by
+        x = i // (nz * ny) + bx
+        sdf = vt[s:e, 0].to(torch.int64)
+        w = vt[s:e, 1].to(torch.int64) & 0xFFFF
+        cols = []
+        for k, f in enumerate((x, y, z, sdf, w)):
+            cols.append(_format_ints(f, wid[k]))
+            sep = torch.full((e - s, 1), 10 if k == 4 else 32, dtype=torch.uint8, device=dev)
+            cols.append(sep)
+        buf = torch.cat(cols, dim=1)
+        parts.append(buf[buf != 0])
+    return torch.cat(parts) if parts else torch.zeros(0, dtype=torch.uint8, device=dev)

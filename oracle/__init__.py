@@ -68,6 +68,8 @@ def lib():
                                              vp, vp, vp, i32]),
             "orc_integrate_seq_backward_f64": (None, [vp, i32, i32, i32, f32, f32, f32, vp, i32, vp, i32, i32, vp, vp,
                                                       i32, vp, vp, vp, vp, vp, i32]),
+            "orc_text_load": (i32, [ctypes.c_char_p, i64, i32, i32, i32, i32, vp, vp]),
+            "orc_text_load_file": (i32, [ctypes.c_char_p, i64, i32, i32, i32, i32, vp, vp]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -398,3 +400,32 @@ def raycast(vol, grid_s, k, e, w, h, normals=True, nthreads=0):
     ok = lib().orc_raycast(_p(vol), nx, ny, nz, float(grid_s), ctypes.byref(k), ctypes.byref(e), w, h, _p(depth),
                            _p(nrm), nthreads)
     return (depth, nrm) if ok else None
+
+
+# ---------------------------------------------------------------------------
+# text-record volume loader (kf.cu:3289-3361), libstdc++ extraction rules
+# ---------------------------------------------------------------------------
+REFERENCE_TAIL_BYTES = 11_000_000_000  # kf.cu:3316 seekg(-11000000000, end)
+
+
+def text_load(text, dim, origin=(512, 512, 0)):
+    """Load records from a text in memory: (volume (dim, dim, dim, 2) int16,
+    {"stored", "iterations", "status"}); status 1 = the reference's loop
+    would not end (a failed extraction outside the window)."""
+    text = bytes(text)
+    vol = np.empty((dim, dim, dim, 2), np.int16)
+    st = np.zeros(3, np.int64)
+    lib().orc_text_load(text, len(text), int(dim), int(origin[0]), int(origin[1]), int(origin[2]), _p(vol), _p(st))
+    return vol, {"stored": int(st[0]), "iterations": int(st[1]), "status": int(st[2])}
+
+
+def text_load_file(path, dim, origin=(512, 512, 0), tail_bytes=REFERENCE_TAIL_BYTES):
+    """Load records from the last tail_bytes of a file (seek, skip the cut
+    line, then the loop of text_load)."""
+    vol = np.empty((dim, dim, dim, 2), np.int16)
+    st = np.zeros(3, np.int64)
+    r = lib().orc_text_load_file(os.fsencode(path), int(tail_bytes), int(dim), int(origin[0]), int(origin[1]),
+                                 int(origin[2]), _p(vol), _p(st))
+    if r != 0:
+        raise OSError("cannot open %s" % path)
+    return vol, {"stored": int(st[0]), "iterations": int(st[1]), "status": int(st[2])}
