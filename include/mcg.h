@@ -326,10 +326,11 @@ typedef struct mcg_text_info {
 /* text: device bytes (e.g. read by GPUDirect or produced on the device) */
 mcg_status mcg_text_records_parse(mcg_context *ctx, const void *text, int64_t len, int32_t dim,
                                   const int32_t origin[3], void *vol, mcg_text_info *info, mcg_stream_t stream);
-/* text: host bytes; copied through pinned staging by reader threads */
+/* text: host bytes (pageable or pinned), copied to the device in one copy */
 mcg_status mcg_text_records_load(mcg_context *ctx, const void *text, int64_t len, int32_t dim,
                                  const int32_t origin[3], void *vol, mcg_text_info *info, mcg_stream_t stream);
-/* The last tail_bytes of a file, as kf.cu:3316-3317 seeks (tail 11e9): the
+/* The last tail_bytes of a file, as kf.cu:3316-3317 seeks (tail 11e9), read
+ * by host threads through pinned staging while earlier pieces copy: the
  * line cut by the seek is skipped.  A file no longer than tail_bytes (or
  * tail_bytes <= 0) is read whole, from offset 0, without skipping a line;
  * the reference's seek fails there and its loop never ends.  MCG_ERR_IO when

@@ -87,6 +87,7 @@ mcg_status mcg_destroy(mcg_context *ctx) {
     cudaFree(ctx->tr_tok);
     cudaFree(ctx->tr_seg);
     cudaFree(ctx->tr_cta);
+    cudaFree(ctx->tr_arr);
     cudaFree(ctx->tr_scan);
     if (ctx->h_tr_scan) cudaFreeHost(ctx->h_tr_scan);
     if (ctx->h_tr_stage) cudaFreeHost(ctx->h_tr_stage);

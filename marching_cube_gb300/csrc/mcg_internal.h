@@ -124,6 +124,8 @@ struct mcg_context {
     size_t tr_seg_cap = 0;
     long long *tr_cta = nullptr;
     size_t tr_cta_cap = 0;
+    uint32_t *tr_arr = nullptr;  // voxels in arrival order
+    size_t tr_arr_cap = 0;
     unsigned char *tr_scan = nullptr;
     size_t tr_scan_cap = 0;
     unsigned char *h_tr_scan = nullptr;   // pinned

@@ -15,21 +15,27 @@
 // digits begins the next extraction).  A start whose field has no digits or
 // leaves int's range is a failure; the stream ends at the first one.
 //
-// Device passes (64-byte slice per thread, 16 KiB segment per CTA):
-//   tr_count   extraction starts per segment, lowest failing start (atomicMin)
-//   tr_scan    exclusive segment offsets (one CTA)
+// Device passes (32-byte slice per thread, 8 KiB segment per CTA), run per
+// 64 MiB chunk of text as the chunks land:
+//   tr_count   extraction starts per segment, lowest failing start (atomicMin);
+//              byte classes as bit masks (SWAR), an exact byte walk only for
+//              slices with ten-digit runs or the first failure
+//   tr_scan    exclusive segment offsets, continuing the running total (one CTA)
 //   tr_fields  the value of every field before the first failure, in order
-//   tr_window  in-window complete records per CTA range
-//   tr_wscan   exclusive CTA offsets, the fields around the end (one CTA)
-//   tr_place   slot s of the s-th in-window record -> voxel (z = s % dim,
-//              y = s / dim % dim, x = s / dim^2)
+//   tr_window  in-window records among those the chunk completes, per CTA
+//   tr_wscan   exclusive CTA offsets, continuing the running count (one CTA)
+//   tr_place   the s-th in-window record -> slot s of an arrival-order array
+// and once at the end:
+//   tr_transpose  slot s -> voxel (z = s % dim, y = s / dim % dim,
+//              x = s / dim^2) through shared-memory tiles; unfilled -> 0
 // How the reference loop ends (a repeated last record, a partial record, a
 // failed field that repeats into every remaining slot) is decided on the
 // host from the fields around the end (text_finish).
 //
-// Host text reaches the device through pinned staging buffers filled by
-// reader threads (memcpy from memory, pread from a file), each with its own
-// stream, so reading and the host-to-device copies overlap.
+// Host text in memory is copied chunk by chunk on a copy stream (the driver
+// moves pageable memory at about the pinned rate on this platform); a file
+// is read chunk by chunk by host threads (pread) into two pinned staging
+// buffers, so file reads, copies and the passes overlap.
 #include <cuda_runtime.h>
 #include <errno.h>
 #include <fcntl.h>
@@ -50,7 +56,8 @@ namespace mcg {
 namespace {
 
 constexpr int TR_THREADS = 256;
-constexpr int TR_SLICE = 64;                       // bytes per thread
+constexpr int TR_SLICE = 32;                       // bytes per thread
+constexpr int TR_WORDS = TR_SLICE / 4;
 constexpr int64_t TR_SEG = TR_THREADS * TR_SLICE;  // bytes per CTA
 constexpr int TR_SCAN_THREADS = 1024;
 constexpr unsigned long long TR_NONE = ~0ull;
@@ -66,6 +73,9 @@ struct TextScan {
     int last_byte;                  // T[L-1], -1 for an empty text
     int tail_n;                     // fields in tail[]
     int tail[12];                   // the last complete record and the fields after it
+    int incomplete;                 // a field ran past the bytes resident at its pass
+    long long rec_done;             // records windowed by the chunks so far
+    long long cur_rb, cur_re;       // the record range of the current chunk
 };
 
 __device__ __forceinline__ bool tr_space(unsigned c) { return c == 32u || (c - 9u) < 5u; }
@@ -100,14 +110,13 @@ __device__ __forceinline__ Field tr_finish(int64_t pos, bool neg, int nd, unsign
     return f;
 }
 
-// the 64 bytes [base, base + 64) as 16 little-endian words; bytes at or past
-// L read as 0 and are never examined
-template <bool ALIGNED>
-__device__ __forceinline__ void tr_load(const uint8_t *__restrict__ T, int64_t L, int64_t base, uint32_t w[16]) {
-    if (ALIGNED && base + TR_SLICE <= L) {
+// nw little-endian words of T from byte base; bytes at or past L read as 0
+template <bool ALIGNED, int NW>
+__device__ __forceinline__ void tr_load(const uint8_t *__restrict__ T, int64_t L, int64_t base, uint32_t *w) {
+    if (ALIGNED && base + 4 * NW <= L) {
         const uint4 *p = reinterpret_cast<const uint4 *>(T + base);
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
+        for (int q = 0; q < NW / 4; ++q) {
             const uint4 v = __ldg(p + q);
             w[4 * q] = v.x;
             w[4 * q + 1] = v.y;
@@ -116,31 +125,21 @@ __device__ __forceinline__ void tr_load(const uint8_t *__restrict__ T, int64_t L
         }
     } else {
 #pragma unroll
-        for (int q = 0; q < 16; ++q) w[q] = 0;
+        for (int q = 0; q < NW; ++q) w[q] = 0;
 #pragma unroll
-        for (int k = 0; k < TR_SLICE; ++k)
+        for (int k = 0; k < 4 * NW; ++k)
             if (base + k < L) w[k >> 2] |= (uint32_t)__ldg(T + base + k) << (8 * (k & 3));
     }
 }
 
-__device__ __forceinline__ unsigned tr_byte(const uint32_t w[16], int k) { return (w[k >> 2] >> (8 * (k & 3))) & 0xffu; }
+__device__ __forceinline__ unsigned tr_byte(const uint32_t *w, int k) { return (w[k >> 2] >> (8 * (k & 3))) & 0xffu; }
 
-__device__ __forceinline__ int tr_starts(const uint32_t w[16], int n, unsigned prev) {
-    int cnt = 0;
-#pragma unroll
-    for (int k = 0; k < TR_SLICE; ++k) {
-        const unsigned c = tr_byte(w, k);
-        if (k < n && tr_start(prev, c)) ++cnt;
-        prev = c;
-    }
-    return cnt;
-}
-
-// Calls f(Field) for every extraction that starts in [base, base + n), in
-// order.  A field still open at the end of the slice continues in T.
+// Exact walk (any field length, failures): calls f(Field) for every
+// extraction that starts in [base, base + n), in order.  A field still open
+// at the end of the slice continues in T, up to the resident bytes [0, La).
 template <class F>
-__device__ __forceinline__ void tr_walk(const uint8_t *__restrict__ T, int64_t L, int64_t base, const uint32_t w[16],
-                                        int n, unsigned prev, F &&f) {
+__device__ __forceinline__ void tr_walk(const uint8_t *__restrict__ T, int64_t L, int64_t La, int64_t base,
+                                        const uint32_t *w, int n, unsigned prev, int *incomplete, F &&f) {
     bool open = false, neg = false;
     int64_t pos = 0;
     int nd = 0;
@@ -177,15 +176,124 @@ __device__ __forceinline__ void tr_walk(const uint8_t *__restrict__ T, int64_t L
     }
     if (open) {
         int64_t j = base + n;
-        while (j < L) {
+        while (j < La) {
             const unsigned c = __ldg(T + j);
             if (!tr_digit(c)) break;
             m = tr_acc(m, c);
             ++nd;
             ++j;
         }
+        if (j >= La && La < L) atomicOr(incomplete, 1);  // the rest of the field is not resident yet
         f(tr_finish(pos, neg, nd, m, j >= L));
     }
+}
+
+// ---- byte classes as bit masks (bit k = byte k) -----------------------------
+// SWAR over 32-bit words: with t = x & 0x7f7f7f7f, the high bit of byte i of
+// t + (0x80 - c) * 0x01010101 is set iff (byte i & 0x7f) >= c (no carries
+// cross bytes); bytes >= 0x80 belong to no class.
+__device__ __forceinline__ uint32_t tr_ge(uint32_t t, uint32_t c) { return t + (0x80u - c) * 0x01010101u; }
+// bits 7, 15, 23, 31 -> bits 0..3 (the partial products never overlap)
+__device__ __forceinline__ uint32_t tr_movemask(uint32_t m) { return ((m & 0x80808080u) * 0x00204081u) >> 28; }
+__device__ __forceinline__ uint32_t tr_digits4(uint32_t x) {
+    const uint32_t t = x & 0x7f7f7f7fu;
+    return tr_movemask(tr_ge(t, 0x30) & ~tr_ge(t, 0x3a) & ~x);
+}
+
+struct Masks {
+    uint32_t D, S, G, Mn;  // digit, white space, sign, '-'
+    uint32_t start;        // an extraction starts here
+    uint32_t invalid;      // ... and fails at once (no digit follows)
+    uint32_t Dnext;        // digits among the 16 bytes after the slice
+};
+
+// look: the 16 bytes after the slice (0 past L)
+__device__ __forceinline__ Masks tr_masks(const uint32_t *w, const uint32_t *look, int n, unsigned prev) {
+    Masks m{0, 0, 0, 0, 0, 0, 0};
+#pragma unroll
+    for (int q = 0; q < TR_WORDS; ++q) {
+        const uint32_t x = w[q], t = x & 0x7f7f7f7fu, lo7 = ~x;
+        const uint32_t dig = tr_ge(t, 0x30) & ~tr_ge(t, 0x3a) & lo7;
+        const uint32_t ws = ((tr_ge(t, 0x09) & ~tr_ge(t, 0x0e)) | (tr_ge(t, 0x20) & ~tr_ge(t, 0x21))) & lo7;
+        const uint32_t minus = tr_ge(t, 0x2d) & ~tr_ge(t, 0x2e) & lo7;
+        const uint32_t sg = (tr_ge(t, 0x2b) & ~tr_ge(t, 0x2c) & lo7) | minus;
+        m.D |= tr_movemask(dig) << (4 * q);
+        m.S |= tr_movemask(ws) << (4 * q);
+        m.G |= tr_movemask(sg) << (4 * q);
+        m.Mn |= tr_movemask(minus) << (4 * q);
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) m.Dnext |= tr_digits4(look[q]) << (4 * q);
+    const uint32_t valid = n >= 32 ? ~0u : ((1u << n) - 1u);
+    m.D &= valid;
+    m.S &= valid;
+    m.G &= valid;
+    m.Mn &= valid;
+    if (n < 32) m.Dnext = 0;
+    const uint32_t N = ~m.S & valid;
+    const uint32_t Dp = (m.D << 1) | (uint32_t)((prev - 48u) < 10u);
+    const uint32_t Sp = (m.S << 1) | (uint32_t)tr_space(prev);
+    m.start = N & (Sp | (Dp & ~m.D));
+    const uint32_t Dn = (m.D >> 1) | ((m.Dnext & 1u) << 31);
+    m.invalid = m.start & ~(m.D | (m.G & Dn));
+    return m;
+}
+
+// true when a digit run of ten or more may lie in the slice, or the run at
+// its end continues into the next bytes to ten or more: such fields may
+// leave int's range and take the exact walk
+__device__ __forceinline__ bool tr_long_run(const Masks &m) {
+    uint32_t r = m.D;
+#pragma unroll
+    for (int i = 1; i < 10; ++i) r &= m.D >> i;
+    if (r) return true;
+    const int top = __clz(~m.D);          // digits ending the slice
+    const int more = __ffs(~m.Dnext) - 1;  // digits starting the next bytes (-1: all 16)
+    return top + (more < 0 ? 16 : more) >= 10;
+}
+
+// Value of the nd (1..9) decimal digits at T[pos]: eight bytes gathered
+// little-endian (first digit lowest) as two words, '0' subtracted, shifted
+// so the digits fill the top bytes, then pairs and quads combined by
+// multiply-add (10, 100) inside each word and the words by 10000; a ninth
+// digit last.
+template <bool ALIGNED>
+__device__ __forceinline__ unsigned tr_value(const uint8_t *__restrict__ T, int64_t L, int64_t pos, int nd) {
+    uint32_t lo = 0, hi = 0;
+    const int64_t a = pos & ~3ll;
+    if (ALIGNED && a + 12 <= L) {
+        const uint32_t *p = reinterpret_cast<const uint32_t *>(T + a);
+        const uint32_t w0 = __ldg(p), w1 = __ldg(p + 1), w2 = __ldg(p + 2);
+        const unsigned sh = (unsigned)(pos - a) * 8u;
+        lo = __funnelshift_r(w0, w1, sh);
+        hi = __funnelshift_r(w1, w2, sh);
+    } else {
+        for (int i = 0; i < 8 && i < nd; ++i) {
+            const uint32_t b = __ldg(T + pos + i);
+            if (i < 4)
+                lo |= b << (8 * i);
+            else
+                hi |= b << (8 * (i - 4));
+        }
+    }
+    const int n8 = nd < 8 ? nd : 8;
+    lo -= 0x30303030u;  // a borrow out of lo only leaves bytes that are shifted out
+    hi -= 0x30303030u;
+    const unsigned s = 8u * (unsigned)(8 - n8);
+    if (s >= 32) {
+        hi = lo << (s - 32);
+        lo = 0;
+    } else {
+        hi = __funnelshift_l(lo, hi, s);
+        lo <<= s;
+    }
+    lo = (lo * 10u + (lo >> 8)) & 0x00FF00FFu;
+    hi = (hi * 10u + (hi >> 8)) & 0x00FF00FFu;
+    lo = (lo * 100u + (lo >> 16)) & 0xFFFFu;
+    hi = (hi * 100u + (hi >> 16)) & 0xFFFFu;
+    unsigned v = lo * 10000u + hi;
+    if (nd > 8) v = v * 10u + (__ldg(T + pos + 8) - 48u);
+    return v;
 }
 
 template <class T>
@@ -195,24 +303,44 @@ __device__ __forceinline__ T warp_sum(T v) {
     return v;
 }
 
+// the slice of this thread: words, its masks, prev byte and length
 template <bool ALIGNED>
-__global__ void __launch_bounds__(TR_THREADS) tr_count(const uint8_t *__restrict__ T, int64_t L,
-                                                       long long *__restrict__ seg_count,
-                                                       unsigned long long *__restrict__ first_fail) {
+__device__ __forceinline__ int tr_slice(const uint8_t *__restrict__ T, int64_t L, int64_t base, uint32_t *w,
+                                        unsigned *prev, Masks *m) {
+    uint32_t look[4];
+    tr_load<ALIGNED, TR_WORDS>(T, L, base, w);
+    tr_load<ALIGNED, 4>(T, L, base + TR_SLICE, look);
+    const int n = (int)min((int64_t)TR_SLICE, L - base);
+    *prev = base == 0 ? 32u : __ldg(T + base - 1);
+    *m = tr_masks(w, look, n, *prev);
+    return n;
+}
+
+// segments seg0 + blockIdx.x; the bytes [0, La) are resident
+template <bool ALIGNED>
+__global__ void __launch_bounds__(TR_THREADS) tr_count(const uint8_t *__restrict__ T, int64_t L, int64_t La,
+                                                       long long seg0, long long *__restrict__ seg_count,
+                                                       TextScan *__restrict__ res) {
     __shared__ int s_cnt[TR_THREADS / 32];
     __shared__ unsigned long long s_fail[TR_THREADS / 32];
-    const int64_t base = (int64_t)blockIdx.x * TR_SEG + (int64_t)threadIdx.x * TR_SLICE;
+    const long long seg = seg0 + blockIdx.x;
+    const int64_t base = seg * TR_SEG + (int64_t)threadIdx.x * TR_SLICE;
     int cnt = 0;
     unsigned long long fail = TR_NONE;
     if (base < L) {
-        uint32_t w[16];
-        tr_load<ALIGNED>(T, L, base, w);
-        const int n = (int)min((int64_t)TR_SLICE, L - base);
-        const unsigned prev = base == 0 ? 32u : __ldg(T + base - 1);
-        tr_walk(T, L, base, w, n, prev, [&](const Field &f) {
-            ++cnt;
-            if (!f.ok && fail == TR_NONE) fail = (unsigned long long)f.pos;
-        });
+        uint32_t w[TR_WORDS];
+        unsigned prev;
+        Masks m;
+        const int n = tr_slice<ALIGNED>(T, L, base, w, &prev, &m);
+        if (tr_long_run(m)) {
+            tr_walk(T, L, La, base, w, n, prev, &res->incomplete, [&](const Field &f) {
+                ++cnt;
+                if (!f.ok && fail == TR_NONE) fail = (unsigned long long)f.pos;
+            });
+        } else {
+            cnt = __popc(m.start);
+            if (m.invalid) fail = (unsigned long long)(base + __ffs(m.invalid) - 1);
+        }
     }
     cnt = warp_sum(cnt);
 #pragma unroll
@@ -233,13 +361,14 @@ __global__ void __launch_bounds__(TR_THREADS) tr_count(const uint8_t *__restrict
             tot += s_cnt[i];
             mf = s_fail[i] < mf ? s_fail[i] : mf;
         }
-        seg_count[blockIdx.x] = tot;
-        if (mf != TR_NONE) atomicMin(first_fail, mf);
+        seg_count[seg] = tot;
+        if (mf != TR_NONE) atomicMin(&res->first_fail, mf);
     }
 }
 
 // exclusive scan of n counts by one CTA of TR_SCAN_THREADS threads; returns the total
-__device__ long long block_scan_exclusive(const long long *__restrict__ in, long long *__restrict__ out, long long n) {
+__device__ long long block_scan_exclusive(const long long *__restrict__ in, long long *__restrict__ out, long long n,
+                                          long long carry = 0) {
     __shared__ long long s_w[TR_SCAN_THREADS / 32];
     __shared__ long long s_total;
     const long long per = (n + TR_SCAN_THREADS - 1) / TR_SCAN_THREADS;
@@ -266,7 +395,7 @@ __device__ long long block_scan_exclusive(const long long *__restrict__ in, long
         s_total = run;
     }
     __syncthreads();
-    long long run = s_w[wid] + inc - sum;
+    long long run = carry + s_w[wid] + inc - sum;
     for (long long i = b; i < e; ++i) {
         const long long v = in[i];
         out[i] = run;
@@ -277,31 +406,35 @@ __device__ long long block_scan_exclusive(const long long *__restrict__ in, long
     return total;
 }
 
+// segment offsets of one chunk, continuing the running total in res->total;
+// after the last chunk n_tok = total unless a field failed (tr_fields sets it)
 __global__ void __launch_bounds__(TR_SCAN_THREADS) tr_scan(const long long *__restrict__ seg_count,
                                                            long long *__restrict__ seg_ofs, long long nseg,
-                                                           TextScan *__restrict__ res) {
-    const long long total = block_scan_exclusive(seg_count, seg_ofs, nseg);
+                                                           TextScan *__restrict__ res, int last) {
+    const long long carry = res->total;
+    const long long total = block_scan_exclusive(seg_count, seg_ofs, nseg, carry);
     if (threadIdx.x == 0) {
-        res->total = total;
-        res->n_tok = total;  // replaced by tr_fields when a field fails
+        res->total = carry + total;
+        if (last && res->first_fail == TR_NONE) res->n_tok = carry + total;
     }
 }
 
 template <bool ALIGNED>
-__global__ void __launch_bounds__(TR_THREADS) tr_fields(const uint8_t *__restrict__ T, int64_t L,
-                                                        const long long *__restrict__ seg_ofs,
-                                                        TextScan *__restrict__ res, int *__restrict__ tok) {
+__global__ void __launch_bounds__(TR_THREADS) tr_fields(const uint8_t *__restrict__ T, int64_t L, int64_t La,
+                                                        long long seg0, const long long *__restrict__ seg_ofs,
+                                                        TextScan *__restrict__ res, int *__restrict__ tok,
+                                                        long long tok_cap) {
     __shared__ int s_w[TR_THREADS / 32];
     const unsigned long long ff = res->first_fail;
-    const int64_t base = (int64_t)blockIdx.x * TR_SEG + (int64_t)threadIdx.x * TR_SLICE;
-    uint32_t w[16];
+    const long long seg = seg0 + blockIdx.x;
+    const int64_t base = seg * TR_SEG + (int64_t)threadIdx.x * TR_SLICE;
+    uint32_t w[TR_WORDS];
     int n = 0, cnt = 0;
     unsigned prev = 32u;
+    Masks m{0, 0, 0, 0, 0, 0, 0};
     if (base < L) {
-        tr_load<ALIGNED>(T, L, base, w);
-        n = (int)min((int64_t)TR_SLICE, L - base);
-        prev = base == 0 ? 32u : __ldg(T + base - 1);
-        cnt = tr_starts(w, n, prev);
+        n = tr_slice<ALIGNED>(T, L, base, w, &prev, &m);
+        cnt = __popc(m.start);
     }
     // block exclusive scan of cnt
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -316,18 +449,40 @@ __global__ void __launch_bounds__(TR_THREADS) tr_fields(const uint8_t *__restric
     int wofs = 0;
     for (int i = 0; i < wid; ++i) wofs += s_w[i];
     if (base >= L || (ff != TR_NONE && (unsigned long long)base > ff)) return;
-    long long j = seg_ofs[blockIdx.x] + wofs + inc - cnt;
-    tr_walk(T, L, base, w, n, prev, [&](const Field &f) {
-        const unsigned long long p = (unsigned long long)f.pos;
-        if (p < ff) {
-            tok[j] = f.value;
-        } else if (p == ff) {
-            res->n_tok = j;
-            res->fail_value = f.value;
-            res->fail_eof = f.eof;
-        }
-        ++j;
-    });
+    long long j = seg_ofs[seg] + wofs + inc - cnt;
+    if (j + cnt > tok_cap) {  // cannot happen: tok_cap bounds the extractions of any text
+        atomicOr(&res->incomplete, 2);
+        return;
+    }
+    const bool has_fail = ff != TR_NONE && (unsigned long long)(base + TR_SLICE) > ff;
+    if (has_fail || tr_long_run(m)) {
+        tr_walk(T, L, La, base, w, n, prev, &res->incomplete, [&](const Field &f) {
+            const unsigned long long p = (unsigned long long)f.pos;
+            if (p < ff) {
+                tok[j] = f.value;
+            } else if (p == ff) {
+                res->n_tok = j;
+                res->fail_value = f.value;
+                res->fail_eof = f.eof;
+            }
+            ++j;
+        });
+        return;
+    }
+    // every field of the slice is valid and shorter than ten digits: one
+    // field per set bit of the start mask, its digits converted eight at a
+    // time (tr_value)
+    const int more = __ffs(~m.Dnext) - 1;  // digits opening the next bytes (< 10 here)
+    uint32_t st = m.start;
+    while (st) {
+        const int p = __ffs(st) - 1;
+        st &= st - 1;
+        const int q = p + (int)((m.G >> p) & 1u);  // first digit
+        int nd = q < 32 ? __ffs(~(m.D >> q)) - 1 : 0;
+        if (nd < 0 || q + nd == 32) nd = (32 - q) + more;
+        const unsigned v = tr_value<ALIGNED>(T, L, base + q, nd);
+        tok[j++] = ((m.Mn >> p) & 1u) ? -(int)v : (int)v;
+    }
 }
 
 __device__ __forceinline__ bool tr_inside(const int *__restrict__ r, long long xs, long long ys, long long zs,
@@ -340,11 +495,21 @@ struct Window {
     long long xs, ys, zs, dim;
 };
 
+// Records complete after the current chunk: [rec_done, Re), Re = fields so
+// far / 5, or n_tok / 5 once a field has failed (a failure is always known
+// by the chunk that holds it, and n_tok is final then).
+__device__ __forceinline__ void tr_records(const TextScan *res, long long *rb, long long *re) {
+    *rb = res->rec_done;
+    *re = (res->first_fail == TR_NONE ? res->total : res->n_tok) / 5;
+}
+
 __global__ void __launch_bounds__(TR_THREADS) tr_window(const int *__restrict__ tok, const TextScan *__restrict__ res,
                                                         Window win, long long *__restrict__ cta_count) {
     __shared__ int s_w[TR_THREADS / 32];
-    const long long R = res->n_tok / 5;
-    const long long r0 = R * blockIdx.x / gridDim.x, r1 = R * (blockIdx.x + 1) / gridDim.x;
+    long long Rb, Re;
+    tr_records(res, &Rb, &Re);
+    const long long R = Re - Rb;
+    const long long r0 = Rb + R * blockIdx.x / gridDim.x, r1 = Rb + R * (blockIdx.x + 1) / gridDim.x;
     int cnt = 0;
     for (long long r = r0 + threadIdx.x; r < r1; r += TR_THREADS)
         cnt += tr_inside(tok + 5 * r, win.xs, win.ys, win.zs, win.dim) ? 1 : 0;
@@ -358,19 +523,30 @@ __global__ void __launch_bounds__(TR_THREADS) tr_window(const int *__restrict__ 
     }
 }
 
+// CTA slot offsets of the current chunk's records, continuing the running
+// in-window count n_win; fixes the chunk's record range for tr_place.  After
+// the last chunk: the fields around the end and the last byte for the host.
 __global__ void __launch_bounds__(TR_SCAN_THREADS) tr_wscan(const long long *__restrict__ cta_count,
                                                             long long *__restrict__ cta_ofs, int nctas,
                                                             const int *__restrict__ tok, const uint8_t *__restrict__ T,
-                                                            int64_t L, TextScan *__restrict__ res) {
-    const long long total = block_scan_exclusive(cta_count, cta_ofs, nctas);
+                                                            int64_t L, TextScan *__restrict__ res, int last) {
+    long long Rb, Re;
+    tr_records(res, &Rb, &Re);
+    const long long carry = res->n_win;
+    const long long total = block_scan_exclusive(cta_count, cta_ofs, nctas, carry);
     if (threadIdx.x == 0) {
-        res->n_win = total;
-        const long long nt = res->n_tok, R = nt / 5;
-        const long long from = R >= 1 ? 5 * R - 5 : 0;
-        const int cnt = (int)(nt - from);
-        for (int i = 0; i < cnt; ++i) res->tail[i] = tok[from + i];
-        res->tail_n = cnt;
-        res->last_byte = L > 0 ? (int)T[L - 1] : -1;
+        res->n_win = carry + total;
+        res->cur_rb = Rb;
+        res->cur_re = Re;
+        res->rec_done = Re;
+        if (last) {
+            const long long nt = res->n_tok, R = nt / 5;
+            const long long from = R >= 1 ? 5 * R - 5 : 0;
+            const int cnt = (int)(nt - from);
+            for (int i = 0; i < cnt; ++i) res->tail[i] = tok[from + i];
+            res->tail_n = cnt;
+            res->last_byte = L > 0 ? (int)T[L - 1] : -1;
+        }
     }
 }
 
@@ -387,10 +563,10 @@ __device__ __forceinline__ unsigned long long tr_slot_index(unsigned long long s
 
 __global__ void __launch_bounds__(TR_THREADS) tr_place(const int *__restrict__ tok, const TextScan *__restrict__ res,
                                                        Window win, const long long *__restrict__ cta_ofs,
-                                                       uint32_t *__restrict__ vol) {
+                                                       uint32_t *__restrict__ arr) {
     __shared__ int s_w[TR_THREADS / 32];
-    const long long R = res->n_tok / 5;
-    const long long r0 = R * blockIdx.x / gridDim.x, r1 = R * (blockIdx.x + 1) / gridDim.x;
+    const long long Rb = res->cur_rb, R = res->cur_re - Rb;
+    const long long r0 = Rb + R * blockIdx.x / gridDim.x, r1 = Rb + R * (blockIdx.x + 1) / gridDim.x;
     const long long cap = win.dim * win.dim * win.dim;
     long long slot0 = cta_ofs[blockIdx.x];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -408,12 +584,34 @@ __global__ void __launch_bounds__(TR_THREADS) tr_place(const int *__restrict__ t
         }
         if (in) {
             const long long s = slot0 + wofs + __popc(bal & ((1u << lane) - 1u));
-            if (s < cap)
-                vol[tr_slot_index((unsigned long long)s, (unsigned long long)win.dim)] =
-                    tr_pack(tok[5 * r + 3], tok[5 * r + 4]);
+            if (s < cap) arr[s] = tr_pack(tok[5 * r + 3], tok[5 * r + 4]);
         }
         slot0 += tot;
         __syncthreads();
+    }
+}
+
+// arrival order -> volume: arr[(xi*dim + yi)*dim + zi] -> vol[(zi*dim + yi)*dim + xi]
+// through a 32 x 32 (x, z) tile per CTA at one y; slots past the stored ones
+// read as zero
+__global__ void __launch_bounds__(256) tr_transpose(const uint32_t *__restrict__ arr,
+                                                    const TextScan *__restrict__ res, long long dim,
+                                                    uint32_t *__restrict__ vol) {
+    __shared__ uint32_t tile[32][33];
+    const long long cap = dim * dim * dim;
+    const long long S = min(res->n_win, cap);
+    const long long zi0 = (long long)blockIdx.x * 32, xi0 = (long long)blockIdx.y * 32, yi = blockIdx.z;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        const long long xi = xi0 + threadIdx.y + 8 * r, zi = zi0 + threadIdx.x;
+        const long long sl = (xi * dim + yi) * dim + zi;
+        tile[threadIdx.y + 8 * r][threadIdx.x] = (xi < dim && zi < dim && sl < S) ? arr[sl] : 0u;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        const long long zi = zi0 + threadIdx.y + 8 * r, xi = xi0 + threadIdx.x;
+        if (zi < dim && xi < dim) vol[(zi * dim + yi) * dim + xi] = tile[threadIdx.x][threadIdx.y + 8 * r];
     }
 }
 
@@ -488,22 +686,36 @@ mcg_status text_finish(mcg_context *ctx, const TextScan &r, bool loop_runs, cons
     return st;
 }
 
-bool grow_bytes(uint8_t **p, size_t *cap, size_t n) { return ensure(p, cap, n); }
+bool text_args_ok(int dim, const int32_t origin[3], const void *vol) {
+    return vol && origin && dim > 0 && dim <= 4096;
+}
 
-// Parses L bytes of device text into vol.  loop_runs = false when the line
-// skip after the seek reached end of file (the loop body never runs).
-mcg_status text_parse(mcg_context *ctx, const uint8_t *T, int64_t L, bool loop_runs, int dim,
-                      const int32_t origin[3], uint32_t *vol, mcg_text_info *info, cudaStream_t s) {
+constexpr int64_t TR_CHUNK = (int64_t)64 << 20;  // bytes per pipelined chunk, a multiple of TR_SEG
+static_assert(TR_CHUNK % TR_SEG == 0, "chunks hold whole segments");
+
+// Parses the L bytes of text at T (device) into vol.  The text arrives in
+// chunks of TR_CHUNK bytes: feed(i, off, n, cs) enqueues chunk i's bytes
+// [off, off + n) into T on stream cs (a null feed: the text is resident).
+// Chunk i is counted, scanned (carrying the running total), its fields
+// converted and the records it completes placed once chunk i + 1 has
+// landed, so the passes overlap the copies; the transpose runs at the end.  A field longer than a chunk
+// that runs past the resident bytes sets `incomplete`, and the whole text is
+// parsed again once resident.  loop_runs = false when the line skip after
+// the seek reached end of file (the reference loop body never runs).
+template <class Feed>
+mcg_status text_run(mcg_context *ctx, const uint8_t *T, int64_t L, const Feed *feed, bool loop_runs, int dim,
+                    const int32_t origin[3], uint32_t *vol, mcg_text_info *info, cudaStream_t s) {
     const Window win{origin[0], origin[1], origin[2], dim};
     const long long cap = win.dim * win.dim * win.dim;
-    cudaError_t e = cudaMemsetAsync(vol, 0, (size_t)cap * 4, s);
-    if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
     const bool aligned = ((uintptr_t)T & 15) == 0;
     const long long nseg = (L + TR_SEG - 1) / TR_SEG;
     const int nctas = ctx->num_sms * 4;
-    if (nseg > INT_MAX) return MCG_ERR_TOO_LARGE;
-    if (!ensure(&ctx->tr_scan, &ctx->tr_scan_cap, sizeof(TextScan)) || !ensure(&ctx->tr_seg, &ctx->tr_seg_cap, 2 * (size_t)nseg + 2) ||
-        !ensure(&ctx->tr_cta, &ctx->tr_cta_cap, 2 * (size_t)nctas))
+    const long long tok_cap = L / 2 + 64;  // no three extraction starts are adjacent
+    cudaError_t e;
+    if (!ensure(&ctx->tr_scan, &ctx->tr_scan_cap, sizeof(TextScan)) ||
+        !ensure(&ctx->tr_seg, &ctx->tr_seg_cap, 2 * (size_t)nseg + 2) ||
+        !ensure(&ctx->tr_cta, &ctx->tr_cta_cap, 2 * (size_t)nctas) ||
+        !ensure(&ctx->tr_arr, &ctx->tr_arr_cap, (size_t)cap) || !ensure(&ctx->tr_tok, &ctx->tr_tok_cap, (size_t)tok_cap))
         return mcg_cuda_fail(ctx, cudaErrorMemoryAllocation);
     if (!ctx->h_tr_scan && cudaMallocHost((void **)&ctx->h_tr_scan, sizeof(TextScan)) != cudaSuccess) {
         ctx->h_tr_scan = nullptr;
@@ -513,39 +725,87 @@ mcg_status text_parse(mcg_context *ctx, const uint8_t *T, int64_t L, bool loop_r
     TextScan *h_res = reinterpret_cast<TextScan *>(ctx->h_tr_scan);
     long long *seg_count = ctx->tr_seg, *seg_ofs = ctx->tr_seg + nseg + 1;
     if ((e = cudaMemsetAsync(d_res, 0, sizeof(TextScan), s)) != cudaSuccess ||
-        (e = cudaMemsetAsync(&d_res->first_fail, 0xff, sizeof(unsigned long long), s)) != cudaSuccess)
+        (e = cudaMemsetAsync(&d_res->first_fail, 0xff, sizeof(unsigned long long), s)) != cudaSuccess ||
+        (e = cudaMemsetAsync(&d_res->last_byte, 0xff, sizeof(int), s)) != cudaSuccess)
         return mcg_cuda_fail(ctx, e);
-    if (L > 0) {
-        if (aligned)
-            tr_count<true><<<(unsigned)nseg, TR_THREADS, 0, s>>>(T, L, seg_count, &d_res->first_fail);
-        else
-            tr_count<false><<<(unsigned)nseg, TR_THREADS, 0, s>>>(T, L, seg_count, &d_res->first_fail);
-        tr_scan<<<1, TR_SCAN_THREADS, 0, s>>>(seg_count, seg_ofs, nseg, d_res);
-        if ((e = cudaGetLastError()) != cudaSuccess) return mcg_cuda_fail(ctx, e);
-        if ((e = cudaMemcpyAsync(h_res, d_res, sizeof(TextScan), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
-            (e = cudaStreamSynchronize(s)) != cudaSuccess)
-            return mcg_cuda_fail(ctx, e);
-        if (!ensure(&ctx->tr_tok, &ctx->tr_tok_cap, (size_t)h_res->total + 1))
-            return mcg_cuda_fail(ctx, cudaErrorMemoryAllocation);
-        if (aligned)
-            tr_fields<true><<<(unsigned)nseg, TR_THREADS, 0, s>>>(T, L, seg_ofs, d_res, ctx->tr_tok);
-        else
-            tr_fields<false><<<(unsigned)nseg, TR_THREADS, 0, s>>>(T, L, seg_ofs, d_res, ctx->tr_tok);
-        tr_window<<<nctas, TR_THREADS, 0, s>>>(ctx->tr_tok, d_res, win, ctx->tr_cta);
-        tr_wscan<<<1, TR_SCAN_THREADS, 0, s>>>(ctx->tr_cta, ctx->tr_cta + nctas, nctas, ctx->tr_tok, T, L, d_res);
-        tr_place<<<nctas, TR_THREADS, 0, s>>>(ctx->tr_tok, d_res, win, ctx->tr_cta + nctas, vol);
-        if ((e = cudaGetLastError()) != cudaSuccess) return mcg_cuda_fail(ctx, e);
-    } else {
-        // no text: no field, no failure, no window record
-        if ((e = cudaMemsetAsync(&d_res->last_byte, 0xff, sizeof(int), s)) != cudaSuccess) return mcg_cuda_fail(ctx, e);
+    const long long nchunks = (L + TR_CHUNK - 1) / TR_CHUNK;
+    cudaStream_t cs = nullptr;
+    std::vector<cudaEvent_t> landed;
+    auto cleanup = [&]() {
+        for (auto ev : landed)
+            if (ev) cudaEventDestroy(ev);
+        if (cs) cudaStreamDestroy(cs);
+    };
+    mcg_status st = MCG_OK;
+    auto fail = [&](cudaError_t err) {
+        if (cs) cudaStreamSynchronize(cs);
+        cleanup();
+        return mcg_cuda_fail(ctx, err);
+    };
+    if (feed && nchunks > 0) {
+        landed.assign((size_t)nchunks, nullptr);
+        if ((e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking)) != cudaSuccess) return fail(e);
+        for (auto &ev : landed)
+            if ((e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) != cudaSuccess) return fail(e);
+        // the copies wait for earlier work on s (a previous parse reads T)
+        if ((e = cudaEventRecord(landed[0], s)) != cudaSuccess || (e = cudaStreamWaitEvent(cs, landed[0], 0)) != cudaSuccess)
+            return fail(e);
     }
+    auto chunk_bytes = [&](long long i) { return std::min<int64_t>(TR_CHUNK, L - i * TR_CHUNK); };
+    auto parse_chunk = [&](long long i) -> cudaError_t {
+        const long long s0 = i * (TR_CHUNK / TR_SEG), s1 = std::min(nseg, (i + 1) * (TR_CHUNK / TR_SEG));
+        const int64_t La = feed ? std::min<int64_t>(L, (i + 2) * TR_CHUNK) : L;
+        cudaError_t err;
+        if (feed && (err = cudaStreamWaitEvent(s, landed[(size_t)std::min(i + 1, nchunks - 1)], 0)) != cudaSuccess)
+            return err;
+        const unsigned g = (unsigned)(s1 - s0);
+        if (aligned)
+            tr_count<true><<<g, TR_THREADS, 0, s>>>(T, L, La, s0, seg_count, d_res);
+        else
+            tr_count<false><<<g, TR_THREADS, 0, s>>>(T, L, La, s0, seg_count, d_res);
+        tr_scan<<<1, TR_SCAN_THREADS, 0, s>>>(seg_count + s0, seg_ofs + s0, s1 - s0, d_res, i == nchunks - 1);
+        if (aligned)
+            tr_fields<true><<<g, TR_THREADS, 0, s>>>(T, L, La, s0, seg_ofs, d_res, ctx->tr_tok, tok_cap);
+        else
+            tr_fields<false><<<g, TR_THREADS, 0, s>>>(T, L, La, s0, seg_ofs, d_res, ctx->tr_tok, tok_cap);
+        // the records completed by this chunk
+        tr_window<<<nctas, TR_THREADS, 0, s>>>(ctx->tr_tok, d_res, win, ctx->tr_cta);
+        tr_wscan<<<1, TR_SCAN_THREADS, 0, s>>>(ctx->tr_cta, ctx->tr_cta + nctas, nctas, ctx->tr_tok, T, L, d_res,
+                                              i == nchunks - 1);
+        tr_place<<<nctas, TR_THREADS, 0, s>>>(ctx->tr_tok, d_res, win, ctx->tr_cta + nctas, ctx->tr_arr);
+        return cudaGetLastError();
+    };
+    for (long long i = 0; i < nchunks; ++i) {
+        if (feed) {
+            if ((st = (*feed)(i, i * TR_CHUNK, chunk_bytes(i), cs)) != MCG_OK) {
+                cudaStreamSynchronize(cs);
+                cleanup();
+                return st;
+            }
+            if ((e = cudaEventRecord(landed[(size_t)i], cs)) != cudaSuccess) return fail(e);
+        }
+        if (i >= 1 && (e = parse_chunk(i - 1)) != cudaSuccess) return fail(e);
+    }
+    if (nchunks > 0 && (e = parse_chunk(nchunks - 1)) != cudaSuccess) return fail(e);
+    {
+        const unsigned t = (unsigned)((dim + 31) / 32);
+        tr_transpose<<<dim3(t, t, (unsigned)dim), dim3(32, 8), 0, s>>>(ctx->tr_arr, d_res, win.dim, vol);
+    }
+    if ((e = cudaGetLastError()) != cudaSuccess) return fail(e);
     if ((e = cudaMemcpyAsync(h_res, d_res, sizeof(TextScan), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
         (e = cudaStreamSynchronize(s)) != cudaSuccess)
-        return mcg_cuda_fail(ctx, e);
+        return fail(e);
+    if (cs && (e = cudaStreamSynchronize(cs)) != cudaSuccess) return fail(e);
+    cleanup();
     const TextScan r = *h_res;
+    if (r.incomplete & 2) return MCG_ERR_STATE;  // the field bound was violated: a defect, not an input error
+    if (r.incomplete) {
+        // a field longer than a chunk: everything is resident now
+        return text_run<Feed>(ctx, T, L, nullptr, loop_runs, dim, origin, vol, info, s);
+    }
     long long stored = 0;
     int filled = 0;
-    const mcg_status st = text_finish(ctx, r, loop_runs, win, vol, &stored, &filled, s);
+    st = text_finish(ctx, r, loop_runs, win, vol, &stored, &filled, s);
     if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return mcg_cuda_fail(ctx, e);
     if (info) {
         info->bytes = L;
@@ -559,78 +819,11 @@ mcg_status text_parse(mcg_context *ctx, const uint8_t *T, int64_t L, bool loop_r
     return st;
 }
 
-bool text_args_ok(int dim, const int32_t origin[3], const void *vol) {
-    return vol && origin && dim > 0 && dim <= 4096;
-}
+struct NoFeed {
+    mcg_status operator()(long long, int64_t, int64_t, cudaStream_t) const { return MCG_OK; }
+};
 
-// ---- staged upload ---------------------------------------------------------
-constexpr int TR_READERS = 8;
-constexpr size_t TR_PIECE = (size_t)16 << 20;
-
-// read(off, n, dst) copies bytes [off, off + n) of the source; false on error
-template <class Read>
-mcg_status stage_upload(mcg_context *ctx, int64_t L, const Read &read, uint8_t *dst, cudaStream_t s) {
-    if (L <= 0) return MCG_OK;
-    if (!ctx->h_tr_stage) {
-        if (cudaMallocHost((void **)&ctx->h_tr_stage, 2 * TR_READERS * TR_PIECE) != cudaSuccess) {
-            ctx->h_tr_stage = nullptr;
-            return mcg_cuda_fail(ctx, cudaErrorMemoryAllocation);
-        }
-    }
-    cudaEvent_t ready;
-    cudaError_t e = cudaEventCreateWithFlags(&ready, cudaEventDisableTiming);
-    if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
-    cudaEventRecord(ready, s);  // earlier work on s that reads dst comes first
-    const int64_t npieces = (L + (int64_t)TR_PIECE - 1) / (int64_t)TR_PIECE;
-    const int nthreads = (int)std::min<int64_t>(TR_READERS, npieces);
-    std::atomic<int> status{MCG_OK};
-    std::atomic<int> cuda_err{0};
-    std::vector<std::thread> pool;
-    const int device = ctx->device;
-    uint8_t *stage = ctx->h_tr_stage;
-    for (int t = 0; t < nthreads; ++t) {
-        pool.emplace_back([&, t]() {
-            cudaSetDevice(device);
-            cudaStream_t ws = nullptr;
-            cudaEvent_t ev[2] = {nullptr, nullptr};
-            cudaError_t err = cudaStreamCreateWithFlags(&ws, cudaStreamNonBlocking);
-            for (int b = 0; b < 2 && err == cudaSuccess; ++b) err = cudaEventCreateWithFlags(&ev[b], cudaEventDisableTiming);
-            if (err == cudaSuccess) err = cudaStreamWaitEvent(ws, ready, 0);
-            int64_t round = 0;
-            for (int64_t p = t; p < npieces && err == cudaSuccess && status.load() == MCG_OK; p += nthreads, ++round) {
-                const int b = (int)(round & 1);
-                uint8_t *buf = stage + ((size_t)t * 2 + b) * TR_PIECE;
-                if (round >= 2 && (err = cudaEventSynchronize(ev[b])) != cudaSuccess) break;
-                const int64_t off = p * (int64_t)TR_PIECE;
-                const int64_t n = std::min<int64_t>((int64_t)TR_PIECE, L - off);
-                if (!read(off, n, buf)) {
-                    int expect = MCG_OK;
-                    status.compare_exchange_strong(expect, MCG_ERR_IO);
-                    break;
-                }
-                if ((err = cudaMemcpyAsync(dst + off, buf, (size_t)n, cudaMemcpyHostToDevice, ws)) != cudaSuccess) break;
-                err = cudaEventRecord(ev[b], ws);
-            }
-            // the parse runs on s once every copy has landed, and the staging
-            // buffers are reused by the next call: wait for the copies
-            if (ws) {
-                const cudaError_t e2 = cudaStreamSynchronize(ws);
-                if (err == cudaSuccess) err = e2;
-            }
-            for (int b = 0; b < 2; ++b)
-                if (ev[b]) cudaEventDestroy(ev[b]);
-            if (ws) cudaStreamDestroy(ws);
-            if (err != cudaSuccess) {
-                int expect = 0;
-                cuda_err.compare_exchange_strong(expect, (int)err);
-            }
-        });
-    }
-    for (auto &th : pool) th.join();
-    cudaEventDestroy(ready);
-    if (cuda_err.load() != 0) return mcg_cuda_fail(ctx, (cudaError_t)cuda_err.load());
-    return (mcg_status)status.load();
-}
+constexpr int TR_READERS = 16;
 
 bool pread_all(int fd, uint8_t *dst, int64_t n, int64_t off) {
     while (n > 0) {
@@ -647,6 +840,50 @@ bool pread_all(int fd, uint8_t *dst, int64_t n, int64_t off) {
     return true;
 }
 
+// File chunks: host threads pread a chunk into one of two pinned staging
+// buffers, then one copy moves it to the device; the buffer is reused two
+// chunks later, once that copy has finished.
+struct FileFeed {
+    mcg_context *ctx;
+    int fd;
+    int64_t start;  // file offset of text byte 0
+    uint8_t *dst;   // device text
+    cudaEvent_t copied[2];
+    mcg_status operator()(long long i, int64_t off, int64_t n, cudaStream_t cs) const {
+        uint8_t *buf = ctx->h_tr_stage + (size_t)(i & 1) * TR_CHUNK;
+        if (i >= 2 && cudaEventSynchronize(copied[i & 1]) != cudaSuccess) return mcg_cuda_fail(ctx, cudaGetLastError());
+        const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
+        const int nt = (int)std::min<int64_t>(std::min(TR_READERS, hw), (n + (1 << 20) - 1) >> 20);
+        std::atomic<int> ok{1};
+        std::vector<std::thread> pool;
+        const int64_t part = (n + nt - 1) / nt;
+        for (int t = 0; t < nt; ++t) {
+            const int64_t a = t * part, b = std::min(n, a + part);
+            if (a >= b) break;
+            pool.emplace_back([&, a, b]() {
+                if (!pread_all(fd, buf + a, b - a, start + off + a)) ok.store(0);
+            });
+        }
+        for (auto &th : pool) th.join();
+        if (!ok.load()) return MCG_ERR_IO;
+        cudaError_t e = cudaMemcpyAsync(dst + off, buf, (size_t)n, cudaMemcpyHostToDevice, cs);
+        if (e == cudaSuccess) e = cudaEventRecord(copied[i & 1], cs);
+        return e == cudaSuccess ? MCG_OK : mcg_cuda_fail(ctx, e);
+    }
+};
+
+struct HostFeed {
+    mcg_context *ctx;
+    const uint8_t *src;
+    uint8_t *dst;
+    mcg_status operator()(long long, int64_t off, int64_t n, cudaStream_t cs) const {
+        // the driver moves pageable host memory at about the pinned rate on
+        // this platform: no staging copy
+        const cudaError_t e = cudaMemcpyAsync(dst + off, src + off, (size_t)n, cudaMemcpyHostToDevice, cs);
+        return e == cudaSuccess ? MCG_OK : mcg_cuda_fail(ctx, e);
+    }
+};
+
 }  // namespace
 }  // namespace mcg
 
@@ -658,8 +895,8 @@ extern "C" mcg_status mcg_text_records_parse(mcg_context *ctx, const void *text,
     if (!ctx || len < 0 || (len > 0 && !text) || !text_args_ok(dim, origin, vol)) return MCG_ERR_INVALID_ARG;
     cudaError_t e = cudaSetDevice(ctx->device);
     if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
-    return text_parse(ctx, static_cast<const uint8_t *>(text), len, true, dim, origin, static_cast<uint32_t *>(vol),
-                      info, (cudaStream_t)stream);
+    return text_run<NoFeed>(ctx, static_cast<const uint8_t *>(text), len, nullptr, true, dim, origin,
+                            static_cast<uint32_t *>(vol), info, (cudaStream_t)stream);
 }
 
 extern "C" mcg_status mcg_text_records_load(mcg_context *ctx, const void *text, int64_t len, int32_t dim,
@@ -668,24 +905,10 @@ extern "C" mcg_status mcg_text_records_load(mcg_context *ctx, const void *text, 
     if (!ctx || len < 0 || (len > 0 && !text) || !text_args_ok(dim, origin, vol)) return MCG_ERR_INVALID_ARG;
     cudaError_t e = cudaSetDevice(ctx->device);
     if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
-    const cudaStream_t s = (cudaStream_t)stream;
-    if (!grow_bytes(&ctx->tr_text, &ctx->tr_text_cap, (size_t)len + 16)) return mcg_cuda_fail(ctx, cudaErrorMemoryAllocation);
-    cudaPointerAttributes attr;
-    const bool pinned = cudaPointerGetAttributes(&attr, text) == cudaSuccess && attr.type == cudaMemoryTypeHost;
-    cudaGetLastError();
-    mcg_status st;
-    if (pinned) {
-        e = cudaMemcpyAsync(ctx->tr_text, text, (size_t)len, cudaMemcpyHostToDevice, s);
-        st = e == cudaSuccess ? MCG_OK : mcg_cuda_fail(ctx, e);
-    } else {
-        const uint8_t *src = static_cast<const uint8_t *>(text);
-        st = stage_upload(ctx, len, [src](int64_t off, int64_t n, uint8_t *dst) {
-            memcpy(dst, src + off, (size_t)n);
-            return true;
-        }, ctx->tr_text, s);
-    }
-    if (st != MCG_OK) return st;
-    return text_parse(ctx, ctx->tr_text, len, true, dim, origin, static_cast<uint32_t *>(vol), info, s);
+    if (!ensure(&ctx->tr_text, &ctx->tr_text_cap, (size_t)len + 16)) return mcg_cuda_fail(ctx, cudaErrorMemoryAllocation);
+    const HostFeed feed{ctx, static_cast<const uint8_t *>(text), ctx->tr_text};
+    return text_run(ctx, ctx->tr_text, len, &feed, true, dim, origin, static_cast<uint32_t *>(vol), info,
+                    (cudaStream_t)stream);
 }
 
 extern "C" mcg_status mcg_text_records_load_file(mcg_context *ctx, const char *path, int64_t tail_bytes, int32_t dim,
@@ -694,7 +917,6 @@ extern "C" mcg_status mcg_text_records_load_file(mcg_context *ctx, const char *p
     if (!ctx || !path || !text_args_ok(dim, origin, vol)) return MCG_ERR_INVALID_ARG;
     cudaError_t e = cudaSetDevice(ctx->device);
     if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
-    const cudaStream_t s = (cudaStream_t)stream;
     const int fd = open(path, O_RDONLY);
     if (fd < 0) return MCG_ERR_IO;
     struct stat sb;
@@ -727,14 +949,25 @@ extern "C" mcg_status mcg_text_records_load_file(mcg_context *ctx, const char *p
         loop_runs = found;
     }
     const int64_t L = flen - start;
-    if (!grow_bytes(&ctx->tr_text, &ctx->tr_text_cap, (size_t)L + 16)) {
-        close(fd);
-        return mcg_cuda_fail(ctx, cudaErrorMemoryAllocation);
+    FileFeed feed{ctx, fd, start, nullptr, {nullptr, nullptr}};
+    mcg_status st = MCG_OK;
+    if (!ensure(&ctx->tr_text, &ctx->tr_text_cap, (size_t)L + 16)) st = mcg_cuda_fail(ctx, cudaErrorMemoryAllocation);
+    if (st == MCG_OK && !ctx->h_tr_stage) {
+        if (cudaMallocHost((void **)&ctx->h_tr_stage, 2 * (size_t)TR_CHUNK) != cudaSuccess) {
+            ctx->h_tr_stage = nullptr;
+            st = mcg_cuda_fail(ctx, cudaErrorMemoryAllocation);
+        }
     }
-    const mcg_status st = stage_upload(ctx, L, [fd, start](int64_t off, int64_t n, uint8_t *dst) {
-        return pread_all(fd, dst, n, start + off);
-    }, ctx->tr_text, s);
+    for (int b = 0; b < 2 && st == MCG_OK; ++b)
+        if ((e = cudaEventCreateWithFlags(&feed.copied[b], cudaEventDisableTiming)) != cudaSuccess)
+            st = mcg_cuda_fail(ctx, e);
+    if (st == MCG_OK) {
+        feed.dst = ctx->tr_text;
+        st = text_run(ctx, ctx->tr_text, L, &feed, loop_runs, dim, origin, static_cast<uint32_t *>(vol), info,
+                      (cudaStream_t)stream);
+    }
+    for (int b = 0; b < 2; ++b)
+        if (feed.copied[b]) cudaEventDestroy(feed.copied[b]);
     close(fd);
-    if (st != MCG_OK) return st;
-    return text_parse(ctx, ctx->tr_text, L, loop_runs, dim, origin, static_cast<uint32_t *>(vol), info, s);
+    return st;
 }

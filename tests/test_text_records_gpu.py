@@ -174,3 +174,22 @@ def test_dump_512_round_trip(mcg):
     del text
     v2 = mcg.load_text_records(host, n, out=v.data)
     assert torch.equal(v2.data, vals)
+
+
+def test_chunk_pipeline(mcg, tmp_path):
+    """Texts longer than the 64 MiB copy/parse chunks: records straddling
+    chunk ends, a field longer than a whole chunk (parsed again once the
+    text is resident), and a failure two chunks in; host memory and file."""
+    chunk = 64 << 20
+    filler = b"9 20 0 1 1\n"  # x = 9: outside the window
+    a = filler * (chunk // len(filler) + 1001)
+    big = b"10 20 1 " + b"0" * (chunk + 12345) + b"7 8\n"
+    text = a + b"10 20 0 3 4\n" + big + filler * 999 + b"11 21 1 -5 6"
+    check(mcg, text, DIM, ORIGIN, ("host",))
+    p = tmp_path / "long.vol"
+    p.write_bytes(text)
+    want, st = oracle.text_load(text, DIM, ORIGIN)
+    got, stats, status = gpu_load(mcg, str(p), DIM, ORIGIN, tail_bytes=None)
+    assert status == 0 and stats["stored"] == st["stored"] and np.array_equal(got, want)
+    bad = a + filler * 600000 + b"10 20 0 3 4\n10 20 1 7x 8\n" + filler * 10
+    check(mcg, bad, DIM, ORIGIN, ("host",))
