@@ -10,7 +10,6 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
-#include <fstream>
 #include <map>
 #include <string>
 #include <vector>
@@ -693,48 +692,30 @@ void cu_voxel_to_mesh(short2 *_local_volume_data, unsigned int _size_x, unsigned
 }
 
 void cu_voxel_rlc_to_mesh(const char *file_input, const char *file_output, int volume_dim) {
-    // text records "x y z sdf weight"; the records inside the window
-    // [512, 512+dim) x [512, 512+dim) x [0, dim) fill the volume in arrival
-    // order with z fastest, then y, then x (:3319-3358); grid 3 mm (:3270).
-    // The reference starts parsing 11e9 bytes before the end of the file;
-    // here the start is clamped to the beginning of shorter files.
-    const int xs = 512, ys = 512, zs = 0;
-    std::ifstream ifs(file_input);
-    if (!ifs.is_open()) {
-        printf("fail to open %s", file_input);
-        return;
-    }
-    ifs.seekg(0, std::ios::end);
-    const std::streamoff len = ifs.tellg();
-    const std::streamoff back = 11000000000LL;
-    ifs.seekg(len > back ? len - back : 0, std::ios::beg);
-    if (len > back) {
-        std::string skip;
-        std::getline(ifs, skip);
-    }
-    const size_t dim = (size_t)volume_dim;
-    std::vector<cu_voxel_t> host(dim * dim * dim);
-    for (auto &v : host) { v.tsdf = 0; v.w = 0; }
-    size_t xi = 0, yi = 0, zi = 0;
-    long long x, y, z, sdf, w;
-    while (ifs >> x >> y >> z >> sdf >> w) {
-        if (xs <= x && x < xs + volume_dim && ys <= y && y < ys + volume_dim && zs <= z && z < zs + volume_dim) {
-            host[zi * dim * dim + yi * dim + xi].w = (ushort)w;
-            host[zi * dim * dim + yi * dim + xi].tsdf = (short)sdf;
-            if (++zi >= dim) { zi = 0; ++yi; }
-            if (yi >= dim) { yi = 0; ++xi; }
-            if (xi >= dim) break;
-        }
-    }
+    // text records "x y z sdf weight" of the last 11e9 bytes; the records
+    // inside [512, 512+dim) x [512, 512+dim) x [0, dim) fill the volume in
+    // arrival order, z fastest, then y, then x (:3289-3358), parsed on the
+    // GPU by mcg_text_records_load_file; grid 3 mm (:3270).  A file shorter
+    // than the tail is read whole (the reference's seek fails there).
     cu_voxel volume;
     memset(&volume, 0, sizeof(volume));
     volume.grid_s = 0.003f;
     volume.size = make_int3(volume_dim, volume_dim, volume_dim);
     volume.size_xy = volume_dim * volume_dim;
-    check(cudaMalloc((void **)&volume.data, host.size() * sizeof(cu_voxel_t)), "cu_voxel_rlc_to_mesh");
-    check(cudaMemcpy(volume.data, host.data(), host.size() * sizeof(cu_voxel_t), cudaMemcpyHostToDevice),
-          "cu_voxel_rlc_to_mesh");
+    const size_t n = (size_t)volume_dim * volume_dim * volume_dim;
+    check(cudaMalloc((void **)&volume.data, n * sizeof(cu_voxel_t)), "cu_voxel_rlc_to_mesh");
     try {
+        mcg_context *ctx = thread_ctx();
+        const int32_t origin[3] = {512, 512, 0};
+        mcg_text_info info;
+        const mcg_status st = mcg_text_records_load_file(ctx, file_input, 11000000000LL, volume_dim, origin,
+                                                         volume.data, &info, nullptr);
+        if (st == MCG_ERR_IO) {
+            printf("fail to open %s", file_input);
+            cu_voxel_delete(&volume);
+            return;
+        }
+        check_status(st, ctx, "cu_voxel_rlc_to_mesh");
         mesh_to_file(volume, file_output, "cu_voxel_rlc_to_mesh");
     } catch (...) {
         cu_voxel_delete(&volume);

@@ -1,6 +1,7 @@
 // Exercises the reference-compatible C++ interface (include/structure.h,
 // cu_memory.hpp, cu_marching_cubes_v1.h, cu_kinect_fusion_v1.h) the way a
-// caller of the reference does: volume in, mesh file out; integrate; RLE.
+// caller of the reference does: volume in, mesh file out; integrate; RLE;
+// a text-record dump to a mesh (cu_voxel_rlc_to_mesh).
 // Usage: dropin_main <workdir>   (prints one JSON line of results)
 #include <cuda_runtime.h>
 #include <math.h>
@@ -118,6 +119,21 @@ int main(int argc, char **argv) {
     std::vector<float> meter(16 * 12, 1.5f);
     std::vector<float3> vtx(16 * 12);
     cu_meter_to_vertex(k, make_int2(16, 12), meter.data(), vtx.data());
+    // 6. cu_voxel_rlc_to_mesh: the sphere as text records of the window at
+    //    (512, 512, 0), x outermost, z innermost, trailing newline
+    {
+        FILE *f = fopen((dir + "/sphere_dump.vol").c_str(), "w");
+        if (f) {
+            for (int x = 0; x < n; ++x)
+                for (int y = 0; y < n; ++y)
+                    for (int z = 0; z < n; ++z) {
+                        const short2 s = h[((size_t)z * n + y) * n + x];
+                        fprintf(f, "%d %d %d %d %d\n", 512 + x, 512 + y, z, (int)s.x, (int)(unsigned short)s.y);
+                    }
+            fclose(f);
+        }
+        cu_voxel_rlc_to_mesh((dir + "/sphere_dump.vol").c_str(), (dir + "/text.ply").c_str(), n);
+    }
     printf("{\"triangles\": %lld, \"mesh_size\": %zu, \"shared\": %d, \"tsdf_equal\": %zu, \"voxels\": %zu, "
            "\"inner\": [%d, %d], \"outer\": [%d, %d], \"orig\": [%d, %d], \"probe\": [%d, %d], "
            "\"vtx0\": [%g, %g, %g]}\n",

@@ -58,6 +58,14 @@ def test_cpp_dropin_runs(tmp_path, orc):
     head, body = ply.split(b"end_header\n", 1)
     assert b"element vertex %d" % (3 * ntri) in head and b"element face %d" % ntri in head
     assert len(body) == 3 * ntri * 24 + ntri * 13
+    # cu_voxel_rlc_to_mesh on the same sphere dumped as text records: the
+    # same triangles at grid 3 mm instead of 1 cm
+    tply = open(os.path.join(str(tmp_path), "text.ply"), "rb").read()
+    thead, tbody = tply.split(b"end_header\n", 1)
+    assert b"element face %d" % ntri in thead and len(tbody) == len(body)
+    P = np.frombuffer(body, np.uint8)[: 3 * ntri * 24].reshape(-1, 6 * 4).copy().view(np.float32)
+    Q = np.frombuffer(tbody, np.uint8)[: 3 * ntri * 24].reshape(-1, 6 * 4).copy().view(np.float32)
+    assert np.allclose(Q[:, :3] / 0.003, P[:, :3] / 0.01, atol=1e-3) and np.allclose(Q[:, 3:], P[:, 3:], atol=1e-4)
     obj = open(os.path.join(str(tmp_path), "sphere.obj")).read()
     assert obj.count("\nf ") + obj.startswith("f ") > 0.9 * ntri
     # RLE round trip keeps every tsdf; window write / read
