@@ -294,9 +294,19 @@ mcg_status mcg_rle_header(const uint8_t *image, int64_t size, int32_t dims[3], f
 mcg_status mcg_rle_encode_host(const void *vol, int32_t nx, int32_t ny, int32_t nz, float min_t, float max_t,
                                float grid_s, int32_t lossless, uint8_t *image, int64_t capacity, int64_t *size);
 mcg_status mcg_rle_decode_host(const uint8_t *image, int64_t size, void *vol, int64_t capacity_voxels);
-/* Decode a host file image into a device short2 volume of capacity voxels.  Synchronous. */
+/* Decode a host file image into a device short2 volume of capacity voxels
+ * (kf.cu:1533-1563 reads and decodes slice by slice on the host): the
+ * compressed image moves to the device in slabs of whole slices and the
+ * runs are expanded on the GPU, one CTA per slice; the validity checks are
+ * the host decoder's (MCG_ERR_FORMAT).  Synchronous. */
 mcg_status mcg_rle_decode(mcg_context *ctx, const uint8_t *image, int64_t size, void *vol,
                           int64_t capacity_voxels, mcg_stream_t stream);
+/* The same from a file, streamed: pieces are read by host threads into
+ * pinned buffers and copied while the slices already resident expand.
+ * dims / params receive the header (size.xyz; min_t, max_t, grid_s).
+ * MCG_ERR_IO when the file cannot be read.  Synchronous. */
+mcg_status mcg_rle_decode_file(mcg_context *ctx, const char *path, void *vol, int64_t capacity_voxels,
+                               int32_t dims[3], float params[3], mcg_stream_t stream);
 
 /* ---- text-record volume loader: kf.cu:3289-3361 ---------------------------- */
 /* The loop of cu_voxel_rlc_to_mesh: integers read five at a time as

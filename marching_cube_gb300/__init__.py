@@ -840,10 +840,24 @@ def run_length_encode(v: Voxel, file_name, lossless=False):
         f.write(img)
 
 
-def run_length_decode(file_name, device=None) -> Voxel:
-    """cu_voxel_run_length_decode (kf.cu:1533-1563), whole-volume form."""
-    with open(file_name, "rb") as f:
-        return rle_decode(f.read(), device)
+def run_length_decode(file_name, device=None, ctx=None, stream=None) -> Voxel:
+    """cu_voxel_run_length_decode (kf.cu:1533-1563), whole-volume form: the
+    file streams to the GPU in pieces and is expanded there."""
+    try:
+        with open(file_name, "rb") as f:
+            head = f.read(40)
+    except OSError as ex:
+        raise MCGError(MCG_ERR_IO, "mcg_rle_decode_file: %s" % ex)
+    (nx, ny, nz), _ = rle_header(head)
+    if device is None:
+        device = torch.device("cuda", torch.cuda.current_device())
+    data = torch.empty((nz, ny, nx, 2), dtype=torch.int16, device=device)
+    ctx = ctx or default_context(data.device.index)
+    dims = (ctypes.c_int32 * 3)()
+    params = (ctypes.c_float * 3)()
+    ctx.check(_lib.mcg_rle_decode_file(ctx.handle, os.fsencode(file_name), _ptr(data), nx * ny * nz, dims, params,
+                                       _stream(stream)), "mcg_rle_decode_file")
+    return Voxel(data, params[0], params[1], params[2])
 
 
 # ---------------------------------------------------------------------------

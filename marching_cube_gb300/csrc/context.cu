@@ -80,6 +80,12 @@ mcg_status mcg_destroy(mcg_context *ctx) {
     delete[] ctx->batch_caps;
     cudaFree(ctx->rle_slices);
     cudaFree(ctx->rle_image);
+    cudaFree(ctx->rd_dir);
+    cudaFree(ctx->rd_err);
+    cudaFree(ctx->rd_sum);
+    cudaFree(ctx->rd_entry);
+    cudaFree(ctx->rd_first);
+    if (ctx->h_rd_stage) cudaFreeHost(ctx->h_rd_stage);
     cudaFree(ctx->depth_scaled);
     cudaFree(ctx->ray_x);
     if (ctx->h_ray_x) cudaFreeHost(ctx->h_ray_x);

@@ -533,50 +533,58 @@ void cu_voxel_run_length_encode(cu_voxel *v_local, const char *file_name, int3 b
 
 void cu_voxel_run_length_decode(cu_voxel *v_local, const char *file_name, int3 begin_local, int3 begin_global,
                                 int3 size) {
-    std::vector<uint8_t> img;
-    if (!read_file(file_name, img)) {
+    uint8_t head[40];
+    FILE *fp = fopen(file_name, "rb");
+    const size_t got = fp ? fread(head, 1, sizeof(head), fp) : 0;
+    if (fp) fclose(fp);
+    if (!fp) {
         fprintf(stderr, "cu_voxel_run_length_decode - fail to open %s file.\n", file_name);
         return;
     }
     int32_t dims[3];
     float params[3];
-    if (mcg_rle_header(img.data(), (int64_t)img.size(), dims, params) != MCG_OK) {
+    if (mcg_rle_header(head, (int64_t)got, dims, params) != MCG_OK) {
         fprintf(stderr, "cu_voxel_run_length_decode - invalid format.\n");
         return;
     }
+    mcg_context *ctx = thread_ctx();
+    const size_t n = (size_t)dims[0] * dims[1] * dims[2];
     if (v_local->data == NULL) {
-        // whole volume (:1542-1563)
+        // whole volume (:1542-1563), streamed from the file and expanded on the GPU
         v_local->size = make_int3(dims[0], dims[1], dims[2]);
         v_local->size_xy = dims[0] * dims[1];
         v_local->min_t = params[0];
         v_local->max_t = params[1];
         v_local->grid_s = params[2];
-        const size_t n = (size_t)dims[0] * dims[1] * dims[2];
         check(cudaMalloc((void **)&v_local->data, n * sizeof(cu_voxel_t)), "cu_voxel_run_length_decode");
-        mcg_context *ctx = thread_ctx();
-        check_status(mcg_rle_decode(ctx, img.data(), (int64_t)img.size(), v_local->data, (int64_t)n, nullptr), ctx,
-                     "mcg_rle_decode");
+        check_status(mcg_rle_decode_file(ctx, file_name, v_local->data, (int64_t)n, dims, params, nullptr), ctx,
+                     "mcg_rle_decode_file");
         return;
     }
-    // window read into an allocated volume (:1564-1600)
+    // window read into an allocated volume (:1564-1600): the whole file is
+    // expanded on the GPU, then the window copied device to device
     if (begin_local.x + size.x > v_local->size.x || begin_local.y + size.y > v_local->size.y ||
         begin_local.z + size.z > v_local->size.z || begin_global.x + size.x > dims[0] ||
         begin_global.y + size.y > dims[1] || begin_global.z + size.z > dims[2] || v_local->grid_s != params[2]) {
         fprintf(stderr, "cu_voxel_run_length_decode - out of bound.\n");
         return;
     }
-    std::vector<cu_voxel_t> global((size_t)dims[0] * dims[1] * dims[2]);
-    if (mcg_rle_decode_host(img.data(), (int64_t)img.size(), global.data(), (int64_t)global.size()) != MCG_OK) {
+    cu_voxel_t *global = nullptr;
+    check(cudaMalloc((void **)&global, n * sizeof(cu_voxel_t)), "cu_voxel_run_length_decode");
+    const mcg_status st = mcg_rle_decode_file(ctx, file_name, global, (int64_t)n, dims, params, nullptr);
+    if (st != MCG_OK) {
+        cudaFree(global);
         fprintf(stderr, "cu_voxel_run_length_decode - malformed file.\n");
         return;
     }
-    for (int z = 0; z < size.z; ++z)
-        for (int y = 0; y < size.y; ++y)
-            check(cudaMemcpy(cu_voxel_access_yz(v_local, y + begin_local.y, z + begin_local.z) + begin_local.x,
-                             &global[((size_t)(z + begin_global.z) * dims[1] + y + begin_global.y) * dims[0] +
-                                     begin_global.x],
-                             sizeof(cu_voxel_t) * size.x, cudaMemcpyHostToDevice),
-                  "cu_voxel_run_length_decode");
+    cudaError_t e = cudaSuccess;
+    for (int z = 0; z < size.z && e == cudaSuccess; ++z)
+        e = cudaMemcpy2D(cu_voxel_access_yz(v_local, begin_local.y, z + begin_local.z) + begin_local.x,
+                         sizeof(cu_voxel_t) * v_local->size.x,
+                         global + ((size_t)(z + begin_global.z) * dims[1] + begin_global.y) * dims[0] + begin_global.x,
+                         sizeof(cu_voxel_t) * dims[0], sizeof(cu_voxel_t) * size.x, size.y, cudaMemcpyDeviceToDevice);
+    cudaFree(global);
+    check(e, "cu_voxel_run_length_decode");
 }
 
 // ---------------------------------------------------------------------------

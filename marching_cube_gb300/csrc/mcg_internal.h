@@ -101,6 +101,20 @@ struct mcg_context {
     size_t rle_slices_cap = 0;
     uint8_t *rle_image = nullptr;
     size_t rle_image_cap = 0;
+    // GPU run-length decoder: slice offsets then lengths, error flag, pinned
+    // staging of file pieces
+    long long *rd_dir = nullptr;  // slice offsets, lengths, first chunks
+    size_t rd_dir_cap = 0;
+    int rd_dir_n = 0;
+    int *rd_err = nullptr;
+    size_t rd_err_cap = 0;
+    unsigned char *rd_sum = nullptr;  // per-chunk summaries, entry states, first voxels
+    size_t rd_sum_cap = 0;
+    unsigned char *rd_entry = nullptr;
+    size_t rd_entry_cap = 0;
+    long long *rd_first = nullptr;
+    size_t rd_first_cap = 0;
+    uint8_t *h_rd_stage = nullptr;
 
     // integrate scratch
     float *depth_scaled = nullptr;

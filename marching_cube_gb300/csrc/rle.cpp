@@ -14,9 +14,9 @@
 //
 // The reference codes slices one after another on one host thread and copies
 // every slice separately.  Here a device volume is encoded by the GPU
-// (rle_gpu.cu); host volumes are encoded, and images decoded, slice-parallel
-// on all host threads, decoded slabs moving to the device in one
-// cudaMemcpyAsync each.
+// (rle_gpu.cu) and images are decoded by the GPU (rle_decode.cu); host
+// volumes are encoded, and images decoded to host memory, slice-parallel on
+// all host threads.
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string.h>
@@ -122,13 +122,6 @@ void parallel_for(int n, F f) {
     for (auto &x : th) x.join();
 }
 
-// slab of slices moved per copy
-int slab_slices(int64_t xy) {
-    const int64_t target = 64ll << 20;  // bytes
-    int64_t s = target / (xy * 4);
-    return (int)std::max<int64_t>(1, s);
-}
-
 }  // namespace
 }  // namespace mcg
 
@@ -214,55 +207,6 @@ mcg_status mcg_rle_decode_host(const uint8_t *image, int64_t size, void *vol, in
         if (!decode_slice(image + off[z], len[z], v + (int64_t)z * xy, xy)) bad = true;
     });
     return bad ? MCG_ERR_FORMAT : MCG_OK;
-}
-
-mcg_status mcg_rle_decode(mcg_context *ctx, const uint8_t *image, int64_t size, void *vol,
-                          int64_t capacity_voxels, mcg_stream_t stream) {
-    if (!ctx || !image || !vol) return MCG_ERR_INVALID_ARG;
-    int32_t dims[3];
-    float params[3];
-    mcg_status st = mcg_rle_header(image, size, dims, params);
-    if (st != MCG_OK) return st;
-    const int64_t xy = (int64_t)dims[0] * dims[1];
-    if (xy * dims[2] > capacity_voxels) return MCG_ERR_CAPACITY;
-    // slice directory
-    std::vector<int64_t> off(dims[2]), len(dims[2]);
-    int64_t p = 40;
-    for (int z = 0; z < dims[2]; ++z) {
-        if (p + 4 > size) return MCG_ERR_FORMAT;
-        uint32_t s32;
-        memcpy(&s32, image + p, 4);
-        p += 4;
-        if (p + (int64_t)s32 > size) return MCG_ERR_FORMAT;
-        off[z] = p;
-        len[z] = s32;
-        p += s32;
-    }
-    cudaError_t e = cudaSetDevice(ctx->device);
-    if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
-    cudaStream_t s = (cudaStream_t)stream;
-    const int nz = dims[2];
-    const int slab = std::min(nz, slab_slices(xy));
-    HVox *host = nullptr;
-    if (cudaMallocHost((void **)&host, sizeof(HVox) * xy * slab) != cudaSuccess)
-        return mcg_cuda_fail(ctx, cudaErrorMemoryAllocation);
-    for (int z0 = 0; z0 < nz && st == MCG_OK; z0 += slab) {
-        const int ns = std::min(slab, nz - z0);
-        e = cudaStreamSynchronize(s);  // previous slab copy done with host buffer
-        if (e != cudaSuccess) { st = mcg_cuda_fail(ctx, e); break; }
-        std::atomic<bool> bad(false);
-        parallel_for(ns, [&](int i) {
-            if (!decode_slice(image + off[z0 + i], len[z0 + i], host + (int64_t)i * xy, xy)) bad = true;
-        });
-        if (bad) { st = MCG_ERR_FORMAT; break; }
-        e = cudaMemcpyAsync((HVox *)vol + (int64_t)z0 * xy, host, sizeof(HVox) * xy * ns,
-                            cudaMemcpyHostToDevice, s);
-        if (e != cudaSuccess) { st = mcg_cuda_fail(ctx, e); break; }
-    }
-    e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess && st == MCG_OK) st = mcg_cuda_fail(ctx, e);
-    cudaFreeHost(host);
-    return st;
 }
 
 }  // extern "C"
