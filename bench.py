@@ -54,6 +54,7 @@ def parse():
     ap.add_argument("--no-stress", action="store_true")
     ap.add_argument("--no-raycast", action="store_true")
     ap.add_argument("--no-text-load", action="store_true")
+    ap.add_argument("--text-dim", type=int, default=512, help="window of the text-record load (<= volume size)")
     ap.add_argument("--stress-n", type=int, default=1024, help="stress volume edge (default 1024)")
     return ap.parse_args()
 
@@ -297,7 +298,7 @@ def bench_raycast(mcg, synthetic, torch, v, reps=20):
             "hit_fraction": float((d > 0).float().mean())}
 
 
-def bench_text_load(mcg, synthetic, torch, v, hbm, reps=10, sample_bytes=48 << 20):
+def bench_text_load(mcg, synthetic, torch, v, hbm, dim=512, reps=10, sample_bytes=48 << 20):
     """Text-record loader (cu_voxel_rlc_to_mesh's volume load): the headline
     512^3 volume dumped as "x y z sdf weight" records of the window at
     (512, 512, 0), x outermost, z innermost (~3 GB of text), loaded back
@@ -305,7 +306,9 @@ def bench_text_load(mcg, synthetic, torch, v, hbm, reps=10, sample_bytes=48 << 2
     (d) from a page-cached file; beside it the reference loop over
     libstdc++ streams on a bounded sample, one core."""
     import numpy as np
-    n = v.data.shape[0]
+    n = min(dim, v.data.shape[0])
+    if n < v.data.shape[0]:
+        v = mcg.Voxel(v.data[:n, :n, :n].contiguous(), v.min_t, v.max_t, v.grid_s)
     text = synthetic.text_dump(v.data, mcg.TEXT_ORIGIN)
     L = text.numel()
     out = torch.empty_like(v.data)
@@ -373,7 +376,7 @@ def bench_text_load(mcg, synthetic, torch, v, hbm, reps=10, sample_bytes=48 << 2
         cpu = {"value": None, "error": str(ex)}
     del host, pinned
     alg = L + 4 * n ** 3
-    return {"workload": "text dump of the 512^3 window at (512,512,0), %d records" % n ** 3,
+    return {"workload": "text dump of the %d^3 window at (512,512,0), %d records" % (n, n ** 3),
             "text_bytes": L, "device_ms": dev_ms, "device_gbs": L / (dev_ms * 1e-3) / 1e9,
             "records_per_s": n ** 3 / (dev_ms * 1e-3),
             "roofline": {"bound": "alu", "alg_bytes": alg, "achieved": alg / (dev_ms * 1e-3) / 1e9,
@@ -773,7 +776,7 @@ def main():
     text_load = None
     if not args.no_text_load:
         try:
-            text_load = bench_text_load(mcg, synthetic, torch, v, hbm)
+            text_load = bench_text_load(mcg, synthetic, torch, v, hbm, dim=args.text_dim)
         except Exception as ex:  # pragma: no cover
             text_load = {"error": str(ex)}
         torch.cuda.empty_cache()
