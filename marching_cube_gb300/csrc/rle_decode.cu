@@ -92,11 +92,15 @@ struct Sum {
     long long v[3];
 };
 
+__device__ __forceinline__ long long sum_pick(const Sum &x, unsigned e) {  // x.v[e] without local memory
+    return e == 0u ? x.v[0] : (e == 1u ? x.v[1] : x.v[2]);
+}
+
 __device__ __forceinline__ Sum sum_then(const Sum &a, const Sum &b) {
     Sum r;
     r.f = rd_then(a.f, b.f);
 #pragma unroll
-    for (int e = 0; e < 3; ++e) r.v[e] = a.v[e] + b.v[rd_apply(a.f, (unsigned)e)];
+    for (int e = 0; e < 3; ++e) r.v[e] = a.v[e] + sum_pick(b, rd_apply(a.f, (unsigned)e));
     return r;
 }
 
@@ -155,38 +159,87 @@ __device__ __forceinline__ void rd_chunk(const Dir &d, long long c, int *z, long
     *cw = (int)min((long long)RD_CHUNK, *nw - *c0);
 }
 
-// the chunk's words (+2 past its end for a literal that straddles it) into W
+// the chunk's words (+2 past its end for a literal that straddles it) into W,
+// zeros after them.  The chunk starts at any byte: 16-byte pieces are read
+// from the aligned address below it and shifted into place; only pieces
+// holding kept words are read, which stay within 32 bytes past the slice's
+// bytes (the image buffer has 64 bytes of slack after the image).
 __device__ __forceinline__ void rd_load(const uint8_t *__restrict__ img, const Dir &d, int z, long long c0, int cw,
                                         long long nw, uint16_t *W) {
-    const uint8_t *src = img + d.off[z];
-    for (int i = threadIdx.x; i < cw + 2; i += RD_THREADS) {
-        const long long wi = c0 + i;
-        W[i] = wi < nw ? (uint16_t)(src[2 * wi] | ((unsigned)src[2 * wi + 1] << 8)) : (uint16_t)0;
+    const uint8_t *first = img + d.off[z] + 2 * c0;
+    const uint4 *p = reinterpret_cast<const uint4 *>((uintptr_t)first & ~(uintptr_t)15);
+    const unsigned sh = (unsigned)((uintptr_t)first & 15);
+    const unsigned q = sh >> 2, r = 8u * (sh & 3u);
+    const long long lim = min((long long)cw + 2, nw - c0);  // words to keep
+    constexpr int PIECES = (RD_CHUNK + 8) / 8;                // 8 words per piece
+    const long long loaded = (lim + 7) / 8;                   // pieces holding kept words
+    for (int j = threadIdx.x; j < PIECES; j += RD_THREADS) {
+        if (j >= loaded) {  // nothing to keep: no read past the slice's bytes
+            reinterpret_cast<uint4 *>(W)[j] = make_uint4(0, 0, 0, 0);
+            continue;
+        }
+        const uint4 lo = __ldg(p + j), hi = __ldg(p + j + 1);
+        const unsigned x[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
+        unsigned o[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            // words k+q and k+q+1 of x without a dynamic register index
+            const unsigned a = q == 0 ? x[k] : q == 1 ? x[k + 1] : q == 2 ? x[k + 2] : x[k + 3];
+            const unsigned b = q == 0 ? x[k + 1] : q == 1 ? x[k + 2] : q == 2 ? x[k + 3] : x[k + 4];
+            o[k] = __funnelshift_r(a, b, r);
+        }
+        const long long w0 = 8ll * j;  // first word of the piece
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            if (w0 + 2 * k >= lim) o[k] = 0;
+            else if (w0 + 2 * k + 1 >= lim) o[k] &= 0xffffu;
+        }
+        reinterpret_cast<uint4 *>(W)[j] = make_uint4(o[0], o[1], o[2], o[3]);
     }
     __syncthreads();
+}
+
+// this thread's 16 words and the 2 after them, from shared memory into
+// registers with two 16-byte loads (conflict-free) and one 4-byte load
+__device__ __forceinline__ void rd_words(const uint16_t *W, int b, unsigned w[RD_WPT + 2]) {
+    const uint4 *p = reinterpret_cast<const uint4 *>(W + b);
+    const uint4 a = p[0], c = p[1];
+    const unsigned x[8] = {a.x, a.y, a.z, a.w, c.x, c.y, c.z, c.w};
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        w[2 * k] = x[k] & 0xffffu;
+        w[2 * k + 1] = x[k] >> 16;
+    }
+    const unsigned t = *reinterpret_cast<const unsigned *>(W + b + RD_WPT);
+    w[RD_WPT] = t & 0xffffu;
+    w[RD_WPT + 1] = t >> 16;
 }
 
 // pass 1: summaries of chunks c0 + blockIdx.x
 __global__ void __launch_bounds__(RD_THREADS) rle_summarize(const uint8_t *__restrict__ img, Dir d, long long cfirst,
                                                             Sum *__restrict__ sums) {
-    __shared__ uint16_t W[RD_CHUNK + 2];
+    __shared__ __align__(16) uint16_t W[RD_CHUNK + 8];
     __shared__ Sum s_w[RD_THREADS / 32];
     const long long c = cfirst + blockIdx.x;
     int z, cw;
     long long c0, nw;
     rd_chunk(d, c, &z, &c0, &cw, &nw);
     rd_load(img, d, z, c0, cw, nw, W);
-    const int b = threadIdx.x * RD_WPT, e = min(cw, b + RD_WPT);
+    const int b = threadIdx.x * RD_WPT, nk = max(0, min(cw, b + RD_WPT) - b);
+    unsigned w[RD_WPT + 2];
+    rd_words(W, b, w);
     Sum t;
     t.f = 0;
 #pragma unroll
     for (unsigned en = 0; en < 3; ++en) {
         unsigned s = en;
         long long v = 0;
-        for (int i = b; i < e; ++i) {
-            const unsigned w = W[i];
-            if (s == 0u) v += w & 0x3fff;
-            s = rd_apply(rd_word_map(w), s);
+#pragma unroll
+        for (int k = 0; k < RD_WPT; ++k) {
+            if (k < nk) {
+                if (s == 0u) v += w[k] & 0x3fff;
+                s = rd_apply(rd_word_map(w[k]), s);
+            }
         }
         t.v[en] = v;
         t.f |= s << (2 * en);
@@ -214,9 +267,9 @@ __global__ void __launch_bounds__(RD_THREADS) rle_slice_scan(Dir d, int z0, long
         const Sum pre = sum_block_scan(x, s_w, &total);
         if (c < ce) {
             entry[c] = (unsigned char)rd_apply(pre.f, state);
-            first[c] = out + pre.v[state];
+            first[c] = out + sum_pick(pre, state);
         }
-        out += total.v[state];
+        out += sum_pick(total, state);
         state = rd_apply(total.f, state);
     }
     if (threadIdx.x == 0 && out < xy) atomicOr(err, 1);
@@ -227,7 +280,7 @@ __global__ void __launch_bounds__(RD_THREADS) rle_expand(const uint8_t *__restri
                                                          long long xy, const unsigned char *__restrict__ entry_of,
                                                          const long long *__restrict__ first_of,
                                                          uint32_t *__restrict__ vol, int *__restrict__ err) {
-    __shared__ uint16_t W[RD_CHUNK + 2];
+    __shared__ __align__(16) uint16_t W[RD_CHUNK + 8];
     __shared__ int rs[RD_CHUNK];
     __shared__ uint32_t rv[RD_CHUNK];
     __shared__ unsigned s_f[RD_THREADS / 32];
@@ -242,9 +295,13 @@ __global__ void __launch_bounds__(RD_THREADS) rle_expand(const uint8_t *__restri
     const unsigned state = entry_of[c];
     uint32_t *out_slice = vol + (long long)z * xy;
     bool bad = false;
-    const int b = threadIdx.x * RD_WPT, e = min(cw, b + RD_WPT);
+    const int b = threadIdx.x * RD_WPT, nk = max(0, min(cw, b + RD_WPT) - b);
+    unsigned w[RD_WPT + 2];
+    rd_words(W, b, w);
     unsigned f = RD_ID;
-    for (int i = b; i < e; ++i) f = rd_then(f, rd_word_map(W[i]));
+#pragma unroll
+    for (int k = 0; k < RD_WPT; ++k)
+        if (k < nk) f = rd_then(f, rd_word_map(w[k]));
     unsigned fall;
     const unsigned fpre = rd_block_scan<unsigned>(f, RD_ID, [](unsigned a, unsigned c2) { return rd_then(a, c2); },
                                                   s_f, &fall);
@@ -252,12 +309,15 @@ __global__ void __launch_bounds__(RD_THREADS) rle_expand(const uint8_t *__restri
     int nrec = 0;
     long long nvox = 0;
     unsigned s = entry;
-    for (int i = b; i < e; ++i) {
-        if (s == 0u) {
-            ++nrec;
-            nvox += W[i] & 0x3fff;
+#pragma unroll
+    for (int k = 0; k < RD_WPT; ++k) {
+        if (k < nk) {
+            if (s == 0u) {
+                ++nrec;
+                nvox += w[k] & 0x3fff;
+            }
+            s = rd_apply(rd_word_map(w[k]), s);
         }
-        s = rd_apply(rd_word_map(W[i]), s);
     }
     int rtot;
     long long vtot;
@@ -267,28 +327,31 @@ __global__ void __launch_bounds__(RD_THREADS) rle_expand(const uint8_t *__restri
     s = entry;
     int r = r0;
     long long o = v0;
-    for (int i = b; i < e; ++i) {
-        const unsigned w = W[i];
-        if (s == 0u) {
-            const unsigned cnt = w & 0x3fff, kind = w >> 14;
-            uint32_t val;
-            bool lit_ok = true;
-            if (kind == 1u) {
-                val = rd_pack((unsigned)kMaxTsdf, 0u);
-            } else if (kind == 2u) {
-                val = rd_pack((unsigned)(-kMaxTsdf), 0u);
-            } else {
-                lit_ok = c0 + i + 2 < nw;
-                val = rd_pack(W[i + 1], W[i + 2]);
+#pragma unroll
+    for (int k = 0; k < RD_WPT; ++k) {
+        if (k < nk) {
+            const unsigned wk = w[k];
+            if (s == 0u) {
+                const unsigned cnt = wk & 0x3fff, kind = wk >> 14;
+                uint32_t val;
+                bool lit_ok = true;
+                if (kind == 1u) {
+                    val = rd_pack((unsigned)kMaxTsdf, 0u);
+                } else if (kind == 2u) {
+                    val = rd_pack((unsigned)(-kMaxTsdf), 0u);
+                } else {
+                    lit_ok = c0 + b + k + 2 < nw;
+                    val = rd_pack(w[k + 1], w[k + 2]);
+                }
+                const long long start = out + o;
+                if (start < n && (cnt == 0u || start + (long long)cnt > n || !lit_ok)) bad = true;
+                rs[r] = (int)min(o, (long long)INT32_MAX);
+                rv[r] = val;
+                ++r;
+                o += cnt;
             }
-            const long long start = out + o;
-            if (start < n && (cnt == 0u || start + (long long)cnt > n || !lit_ok)) bad = true;
-            rs[r] = (int)min(o, (long long)INT32_MAX);
-            rv[r] = val;
-            ++r;
-            o += cnt;
+            s = rd_apply(rd_word_map(wk), s);
         }
-        s = rd_apply(rd_word_map(w), s);
     }
     __syncthreads();
     const long long end = min(n, out + vtot);
@@ -336,7 +399,7 @@ constexpr int64_t RD_SLAB = (int64_t)64 << 20;  // image bytes per copy
 // directory (offsets, lengths, chunk bases) and the per-chunk arrays
 mcg_status prepare(mcg_context *ctx, int nz, int64_t size) {
     const size_t chunks = (size_t)(size / (2 * RD_CHUNK)) + (size_t)nz + 1;  // bounds the chunks of any image
-    if (!ensure(&ctx->rle_image, &ctx->rle_image_cap, (size_t)size + 16) ||
+    if (!ensure(&ctx->rle_image, &ctx->rle_image_cap, (size_t)size + 64) ||
         !ensure(&ctx->rd_dir, &ctx->rd_dir_cap, 3 * (size_t)nz + 1) || !ensure(&ctx->rd_err, &ctx->rd_err_cap, 1) ||
         !ensure(&ctx->rd_sum, &ctx->rd_sum_cap, chunks * sizeof(Sum)) ||
         !ensure(&ctx->rd_first, &ctx->rd_first_cap, chunks) || !ensure(&ctx->rd_entry, &ctx->rd_entry_cap, chunks))
