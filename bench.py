@@ -54,6 +54,7 @@ def parse():
     ap.add_argument("--no-stress", action="store_true")
     ap.add_argument("--no-raycast", action="store_true")
     ap.add_argument("--no-text-load", action="store_true")
+    ap.add_argument("--no-mesh-write", action="store_true")
     ap.add_argument("--text-dim", type=int, default=512, help="window of the text-record load (<= volume size)")
     ap.add_argument("--stress-n", type=int, default=1024, help="stress volume edge (default 1024)")
     return ap.parse_args()
@@ -388,6 +389,40 @@ def bench_text_load(mcg, synthetic, torch, v, hbm, dim=512, reps=10, sample_byte
             "e2e_pinned": {"ms": res["pinned"] * 1e3, "gbs": L / res["pinned"] / 1e9, "h2d_bytes": L},
             "e2e_file": file_res,
             "cpu_baseline": cpu}
+
+
+def bench_mesh_write(mcg, torch, vol, cell, ctx, reps=5, sample_frac=0.25):
+    """Mesh writers (kf.cu:3394-3424 PLY, 3625-3726 OBJ) on the headline
+    soup: the reference's bytes built on the GPU and copied out (host
+    buffers, no file system), beside the reference's writer (std::map of
+    "%.4f" keys + fprintf, the oracle) on one core over the first quarter
+    of the soup."""
+    m = mcg.extract(vol, cell, soup=True, normals=True, ctx=ctx)
+    nv = m.num_vertices
+    res = {"soup_vertices": nv}
+    for name, fn in (("obj", lambda: mcg.mesh_obj(m, ctx=ctx)), ("ply", lambda: mcg.mesh_ply(m, ctx=ctx))):
+        out = fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            out = fn()
+        torch.cuda.synchronize()
+        dt = (time.perf_counter() - t0) / reps
+        nbytes = sum(len(x) for x in out) if isinstance(out, tuple) else len(out)
+        res[name] = {"ms": dt * 1e3, "bytes": nbytes, "mvertices_per_s": nv / dt / 1e6}
+    try:
+        import oracle as orc
+        k = (int(nv * sample_frac) // 3) * 3
+        s = m.soup[:k].cpu().numpy()
+        n = m.normals[:k].cpu().numpy()
+        t0 = time.perf_counter()
+        orc.mesh_obj(s, n)
+        dt = time.perf_counter() - t0
+        res["cpu_obj"] = {"mvertices_per_s": k / dt / 1e6, "cores": 1, "kind": "port",
+                          "sample": "first %d soup vertices" % k, "seconds": dt}
+    except Exception as ex:  # pragma: no cover
+        res["cpu_obj"] = {"error": str(ex)}
+    return res
 
 
 def bench_indexed(mcg, torch, vol, cell, ctx, reps=10):
@@ -781,6 +816,13 @@ def main():
             text_load = {"error": str(ex)}
         torch.cuda.empty_cache()
 
+    mesh_write = None
+    if not args.no_mesh_write:
+        try:
+            mesh_write = bench_mesh_write(mcg, torch, v.data, cell, ctx)
+        except Exception as ex:  # pragma: no cover
+            mesh_write = {"error": str(ex)}
+
     indexed = None
     if not args.no_indexed:
         try:
@@ -830,6 +872,7 @@ def main():
         "indexed": indexed,
         "raycast": raycast,
         "text_load": text_load,
+        "mesh_write": mesh_write,
         "stress": stress,
     }
     if rank == 0:

@@ -308,6 +308,35 @@ mcg_status mcg_rle_decode(mcg_context *ctx, const uint8_t *image, int64_t size, 
 mcg_status mcg_rle_decode_file(mcg_context *ctx, const char *path, void *vol, int64_t capacity_voxels,
                                int32_t dims[3], float params[3], mcg_stream_t stream);
 
+/* ---- mesh writers: kf.cu:3394-3424 (PLY), 3625-3726 (OBJ) ------------------- */
+/* Binary little-endian PLY of a soup, the reference's bytes: header, per
+ * vertex position + normal (float3 each), per triangle uint8 3 + int32
+ * 3t, 3t+1, 3t+2.  soup / normals: device arrays of n_vertices entries
+ * (normals 3 floats each).  image = NULL with capacity 0 returns the size in
+ * *size; a smaller capacity gives MCG_ERR_CAPACITY.  Built on the device,
+ * copied out once.  Synchronous. */
+mcg_status mcg_mesh_ply(mcg_context *ctx, const mcg_vertex_voxel *soup, const float *normals, int64_t n_vertices,
+                        uint8_t *image, int64_t capacity, int64_t *size, mcg_stream_t stream);
+/* OBJ text with the reference's vertex merge (a vertex is new when the text
+ * "%.4f_%.4f_%.4f" of its position is new; "v %f %f %f" + "vn %f %f %f" per
+ * new vertex, "f a b c" per triangle of three distinct ids) and the
+ * qi_volume listing ("qi tsdf w vx vy vz", then "%d %hd %hd %d %d %d" per
+ * vertex), byte for byte, built on the device (hash merge of the exact
+ * integer keys, GPU number formatting).  NULL buffers with capacities 0
+ * return the sizes; a smaller capacity gives MCG_ERR_CAPACITY; qi may be
+ * NULL.  MCG_ERR_TOO_LARGE for positions at 104.8575 or more from the
+ * origin (where the reference's key buffer overflows) or non-finite /
+ * huge values.  Synchronous. */
+mcg_status mcg_mesh_obj(mcg_context *ctx, const mcg_vertex_voxel *soup, const float *normals, int64_t n_vertices,
+                        uint8_t *obj, int64_t obj_capacity, int64_t *obj_size, uint8_t *qi, int64_t qi_capacity,
+                        int64_t *qi_size, mcg_stream_t stream);
+/* Writes path by its extension (".ply" or ".obj"; anything else:
+ * MCG_ERR_INVALID_ARG, the reference prints "Invalid file extension"); for
+ * OBJ also qi_path when not NULL (the reference writes "qi_volume.txt").
+ * MCG_ERR_IO when a file cannot be written. */
+mcg_status mcg_mesh_write(mcg_context *ctx, const mcg_vertex_voxel *soup, const float *normals, int64_t n_vertices,
+                          const char *path, const char *qi_path, mcg_stream_t stream);
+
 /* ---- text-record volume loader: kf.cu:3289-3361 ---------------------------- */
 /* The loop of cu_voxel_rlc_to_mesh: integers read five at a time as
  * "x y z sdf weight" records with `ifs >> int` (C++ formatted input:

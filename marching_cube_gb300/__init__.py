@@ -916,3 +916,57 @@ def load_text_records(source, dim, origin=TEXT_ORIGIN, tail_bytes=TEXT_TAIL_BYTE
         stats.update({k: getattr(info, k) for k, _ in _capi.TextInfo._fields_ if k != "reserved"})
     ctx.check(st, what)
     return Voxel(out, 0.0, 0.0, float(grid_s))
+
+
+# ---------------------------------------------------------------------------
+# mesh writers (kf.cu:3394-3424 PLY, 3625-3726 OBJ), built on the GPU
+# ---------------------------------------------------------------------------
+def _mesh_args(mesh: Mesh, n):
+    n = mesh.num_vertices if n is None else int(n)
+    if mesh.soup is None or mesh.normals is None:
+        raise ValueError("the writers need the soup and its normals")
+    if n > mesh.soup.shape[0] or n > mesh.normals.shape[0]:
+        raise ValueError("n exceeds the soup")
+    return n
+
+
+def mesh_ply(mesh: Mesh, n=None, ctx=None, stream=None) -> bytes:
+    """The reference's binary PLY image of the soup (header, positions +
+    normals, faces (3i, 3i+1, 3i+2))."""
+    import numpy as np
+    n = _mesh_args(mesh, n)
+    ctx = ctx or default_context(mesh.soup.device.index)
+    size = ctypes.c_int64(0)
+    ctx.check(_lib.mcg_mesh_ply(ctx.handle, _ptr(mesh.soup), _ptr(mesh.normals), n, None, 0, ctypes.byref(size),
+                                _stream(stream)), "mcg_mesh_ply")
+    out = np.empty(size.value, np.uint8)
+    ctx.check(_lib.mcg_mesh_ply(ctx.handle, _ptr(mesh.soup), _ptr(mesh.normals), n,
+                                out.ctypes.data_as(ctypes.c_void_p), out.size, ctypes.byref(size), _stream(stream)),
+              "mcg_mesh_ply")
+    return out.tobytes()
+
+
+def mesh_obj(mesh: Mesh, n=None, ctx=None, stream=None):
+    """(OBJ text, qi_volume text) of the soup with the reference's vertex
+    merge by "%.4f" keys, as bytes."""
+    import numpy as np
+    n = _mesh_args(mesh, n)
+    ctx = ctx or default_context(mesh.soup.device.index)
+    os_, qs = ctypes.c_int64(0), ctypes.c_int64(0)
+    ctx.check(_lib.mcg_mesh_obj(ctx.handle, _ptr(mesh.soup), _ptr(mesh.normals), n, None, 0, ctypes.byref(os_),
+                                None, 0, ctypes.byref(qs), _stream(stream)), "mcg_mesh_obj")
+    obj = np.empty(max(os_.value, 1), np.uint8)
+    qi = np.empty(max(qs.value, 1), np.uint8)
+    ctx.check(_lib.mcg_mesh_obj(ctx.handle, _ptr(mesh.soup), _ptr(mesh.normals), n,
+                                obj.ctypes.data_as(ctypes.c_void_p), obj.size, ctypes.byref(os_),
+                                qi.ctypes.data_as(ctypes.c_void_p), qi.size, ctypes.byref(qs), _stream(stream)),
+              "mcg_mesh_obj")
+    return obj[:os_.value].tobytes(), qi[:qs.value].tobytes()
+
+
+def mesh_write(mesh: Mesh, path, qi_path=None, n=None, ctx=None, stream=None):
+    """Write the soup as path (".ply" or ".obj"), and qi_path for OBJ."""
+    n = _mesh_args(mesh, n)
+    ctx = ctx or default_context(mesh.soup.device.index)
+    ctx.check(_lib.mcg_mesh_write(ctx.handle, _ptr(mesh.soup), _ptr(mesh.normals), n, os.fsencode(path),
+                                  os.fsencode(qi_path) if qi_path else None, _stream(stream)), "mcg_mesh_write")

@@ -106,6 +106,11 @@ SIGNATURES = {
     "mcg_rle_decode": (c_int, [c_void_p, c_void_p, c_int64, c_void_p, c_int64, c_void_p]),
     "mcg_rle_decode_file": (c_int, [c_void_p, ctypes.c_char_p, c_void_p, c_int64, ctypes.POINTER(c_int32),
                                     ctypes.POINTER(c_float), c_void_p]),
+    "mcg_mesh_ply": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_int64, ctypes.POINTER(c_int64),
+                             c_void_p]),
+    "mcg_mesh_obj": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_int64, ctypes.POINTER(c_int64),
+                             c_void_p, c_int64, ctypes.POINTER(c_int64), c_void_p]),
+    "mcg_mesh_write": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, ctypes.c_char_p, ctypes.c_char_p, c_void_p]),
     "mcg_text_records_parse": (c_int, [c_void_p, c_void_p, c_int64, c_int32, ctypes.POINTER(c_int32), c_void_p,
                                        ctypes.POINTER(TextInfo), c_void_p]),
     "mcg_text_records_load": (c_int, [c_void_p, c_void_p, c_int64, c_int32, ctypes.POINTER(c_int32), c_void_p,

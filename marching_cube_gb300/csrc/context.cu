@@ -86,6 +86,10 @@ mcg_status mcg_destroy(mcg_context *ctx) {
     cudaFree(ctx->rd_entry);
     cudaFree(ctx->rd_first);
     if (ctx->h_rd_stage) cudaFreeHost(ctx->h_rd_stage);
+    cudaFree(ctx->mw_keys);
+    cudaFree(ctx->mw_int);
+    cudaFree(ctx->mw_len);
+    cudaFree(ctx->mw_text);
     cudaFree(ctx->depth_scaled);
     cudaFree(ctx->ray_x);
     if (ctx->h_ray_x) cudaFreeHost(ctx->h_ray_x);

@@ -10,7 +10,6 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
-#include <map>
 #include <string>
 #include <vector>
 
@@ -592,66 +591,6 @@ void cu_voxel_run_length_decode(cu_voxel *v_local, const char *file_name, int3 b
 // ---------------------------------------------------------------------------
 namespace {
 
-// binary little-endian PLY, one vertex per soup record, faces (3i, 3i+1, 3i+2)
-// (:3394-3424)
-bool write_ply(const char *path, const std::vector<vertex_voxel> &v, const std::vector<float3> &n) {
-    FILE *fp = fopen(path, "wb");
-    if (!fp) return false;
-    const int nv = (int)v.size(), nf = nv / 3;
-    fprintf(fp, "ply\nformat binary_little_endian 1.0\nelement vertex %d\n", nv);
-    fprintf(fp, "property float32 x\nproperty float32 y\nproperty float32 z\n");
-    fprintf(fp, "property float32 nx\nproperty float32 ny\nproperty float32 nz\n");
-    fprintf(fp, "element face %d\nproperty list uint8 int32 vertex_indices\nend_header\n", nf);
-    for (int i = 0; i < nv; ++i) {
-        fwrite(&v[i].ver_pos, sizeof(float3), 1, fp);
-        fwrite(&n[i], sizeof(float3), 1, fp);
-    }
-    const unsigned char three = 3;
-    for (int i = 0; i < nf; ++i) {
-        const int f[3] = {3 * i, 3 * i + 1, 3 * i + 2};
-        fwrite(&three, 1, 1, fp);
-        fwrite(f, sizeof(int), 3, fp);
-    }
-    fclose(fp);
-    return true;
-}
-
-// OBJ with vertices merged by their "%.4f_%.4f_%.4f" key and degenerate
-// faces dropped (:3656-3723); also the per-vertex voxel dump qi_volume.txt
-bool write_obj(const char *path, const std::vector<vertex_voxel> &v, const std::vector<float3> &n) {
-    FILE *fp = fopen(path, "w");
-    if (!fp) return false;
-    FILE *qi = fopen("qi_volume.txt", "wt");
-    if (qi) fprintf(qi, "qi tsdf w vx vy vz\n");
-    std::map<std::string, int> index;
-    std::vector<int> id(v.size());
-    char key[64];
-    int count = 0;
-    for (size_t i = 0; i < v.size(); ++i) {
-        snprintf(key, sizeof(key), "%.4f_%.4f_%.4f", v[i].ver_pos.x, v[i].ver_pos.y, v[i].ver_pos.z);
-        auto it = index.find(key);
-        if (it == index.end()) {
-            fprintf(fp, "v %f %f %f\n", v[i].ver_pos.x, v[i].ver_pos.y, v[i].ver_pos.z);
-            fprintf(fp, "vn %f %f %f\n", n[i].x, n[i].y, n[i].z);
-            index.emplace(key, ++count);
-            id[i] = count;
-            if (qi)
-                fprintf(qi, "%d %hd %hd %d %d %d\n", count, v[i].tsdf, v[i].w, v[i].vox_pos.x, v[i].vox_pos.y,
-                        v[i].vox_pos.z);
-        } else {
-            id[i] = it->second;
-        }
-    }
-    if (qi) fclose(qi);
-    for (size_t t = 0; t + 2 < v.size(); t += 3) {
-        const int a = id[t], b = id[t + 1], c = id[t + 2];
-        if (a == b || a == c || b == c) continue;
-        fprintf(fp, "f %d %d %d\n", a, b, c);
-    }
-    fclose(fp);
-    return true;
-}
-
 void mesh_to_file(cu_voxel &volume, const char *file_output, const char *who) {
     MarchingCubes mc;
     cu_array<vertex_voxel> tri;
@@ -660,20 +599,21 @@ void mesh_to_file(cu_voxel &volume, const char *file_output, const char *who) {
     cu_array<float3> normals;
     cu_array<vertex_voxel> mesh = mc.run(volume, tri, vi2vox, ver_voxel, normals);
     printf("%s - # of triangles = %lld\n", who, (long long)mc.counts().triangles);
-    std::vector<vertex_voxel> hv(mesh.size());
-    std::vector<float3> hn(mesh.size());
-    if (!hv.empty()) {
-        mesh.download(hv.data());
-        check(cudaMemcpy(hn.data(), normals.ptr(), hn.size() * sizeof(float3), cudaMemcpyDeviceToHost), who);
-    }
+    // the writers run on the GPU (mesh_writers.cu): the reference's PLY bytes,
+    // and its OBJ with the "%.4f" vertex merge plus qi_volume.txt
     const char *ext = strrchr(file_output, '.');
-    if (ext && strcmp(ext, ".ply") == 0) {
-        if (!write_ply(file_output, hv, hn)) fprintf(stderr, "%s - cannot write %s\n", who, file_output);
-    } else if (ext && strcmp(ext, ".obj") == 0) {
-        if (!write_obj(file_output, hv, hn)) fprintf(stderr, "%s - cannot write %s\n", who, file_output);
-    } else {
+    const bool obj = ext && strcmp(ext, ".obj") == 0;
+    mcg_context *ctx = thread_ctx();
+    const mcg_status st =
+        mcg_mesh_write(ctx, reinterpret_cast<const mcg_vertex_voxel *>(mesh.ptr()),
+                       reinterpret_cast<const float *>(normals.ptr()), (int64_t)mesh.size(), file_output,
+                       obj ? "qi_volume.txt" : nullptr, nullptr);
+    if (st == MCG_ERR_INVALID_ARG)
         fprintf(stderr, "%s - Invalid file extension (%s)\n", who, ext ? ext : "");
-    }
+    else if (st == MCG_ERR_IO)
+        fprintf(stderr, "%s - cannot write %s\n", who, file_output);
+    else
+        check_status(st, ctx, who);
 }
 
 }  // namespace

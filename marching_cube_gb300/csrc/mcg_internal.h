@@ -116,6 +116,18 @@ struct mcg_context {
     size_t rd_first_cap = 0;
     uint8_t *h_rd_stage = nullptr;
 
+    // mesh writers: key table, int scratch (first index per slot; slot,
+    // uid, id, order per vertex; kept triangles; flags), lengths/offsets and
+    // the assembled file body
+    unsigned long long *mw_keys = nullptr;
+    size_t mw_keys_cap = 0;
+    int *mw_int = nullptr;
+    size_t mw_int_cap = 0;
+    long long *mw_len = nullptr;
+    size_t mw_len_cap = 0;
+    unsigned char *mw_text = nullptr;
+    size_t mw_text_cap = 0;
+
     // integrate scratch
     float *depth_scaled = nullptr;
     size_t depth_scaled_cap = 0;

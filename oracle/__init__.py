@@ -70,6 +70,8 @@ def lib():
                                                       i32, vp, vp, vp, vp, vp, i32]),
             "orc_text_load": (i32, [ctypes.c_char_p, i64, i32, i32, i32, i32, vp, vp]),
             "orc_text_load_file": (i32, [ctypes.c_char_p, i64, i32, i32, i32, i32, vp, vp]),
+            "orc_mesh_ply": (i64, [vp, vp, i64, vp, i64]),
+            "orc_mesh_obj": (None, [vp, vp, i64, vp, i64, vp, i64, vp]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -429,3 +431,31 @@ def text_load_file(path, dim, origin=(512, 512, 0), tail_bytes=REFERENCE_TAIL_BY
     if r != 0:
         raise OSError("cannot open %s" % path)
     return vol, {"stored": int(st[0]), "iterations": int(st[1]), "status": int(st[2])}
+
+
+# ---------------------------------------------------------------------------
+# mesh writers (kf.cu:3394-3424 PLY, 3625-3726 OBJ), glibc formatting
+# ---------------------------------------------------------------------------
+def mesh_ply(soup, normals):
+    """Binary PLY image (bytes) of a soup: soup (n, 28) uint8 vertex_voxel
+    records, normals (n, 3) float32."""
+    soup = np.ascontiguousarray(soup, np.uint8).reshape(-1, 28)
+    normals = np.ascontiguousarray(normals, np.float32).reshape(-1, 3)
+    n = len(soup)
+    size = lib().orc_mesh_ply(_p(soup), _p(normals), n, None, 0)
+    out = np.empty(size, np.uint8)
+    lib().orc_mesh_ply(_p(soup), _p(normals), n, _p(out), size)
+    return out.tobytes()
+
+
+def mesh_obj(soup, normals):
+    """(OBJ image, qi_volume image) of a soup, as bytes."""
+    soup = np.ascontiguousarray(soup, np.uint8).reshape(-1, 28)
+    normals = np.ascontiguousarray(normals, np.float32).reshape(-1, 3)
+    n = len(soup)
+    sizes = np.zeros(2, np.int64)
+    lib().orc_mesh_obj(_p(soup), _p(normals), n, None, 0, None, 0, _p(sizes))
+    obj = np.empty(sizes[0], np.uint8)
+    qi = np.empty(sizes[1], np.uint8)
+    lib().orc_mesh_obj(_p(soup), _p(normals), n, _p(obj), int(sizes[0]), _p(qi), int(sizes[1]), _p(sizes))
+    return obj.tobytes(), qi.tobytes()

@@ -58,6 +58,15 @@ def test_cpp_dropin_runs(tmp_path, orc):
     head, body = ply.split(b"end_header\n", 1)
     assert b"element vertex %d" % (3 * ntri) in head and b"element face %d" % ntri in head
     assert len(body) == 3 * ntri * 24 + ntri * 13
+    # the OBJ and qi_volume.txt are the reference writer's bytes for the soup
+    import torch
+    import marching_cube_gb300 as mcg
+    mesh = mcg.extract(torch.from_numpy(vol).cuda(), 0.01, soup=True, normals=True)
+    nv = mesh.num_vertices
+    obj, qi = orc.mesh_obj(mesh.soup[:nv].cpu().numpy(), mesh.normals[:nv].cpu().numpy())
+    assert open(os.path.join(str(tmp_path), "sphere.obj"), "rb").read() == obj
+    assert open(os.path.join(str(tmp_path), "qi_volume.txt"), "rb").read() == qi
+    assert ply == orc.mesh_ply(mesh.soup[:nv].cpu().numpy(), mesh.normals[:nv].cpu().numpy())
     # cu_voxel_rlc_to_mesh on the same sphere dumped as text records: the
     # same triangles at grid 3 mm instead of 1 cm
     tply = open(os.path.join(str(tmp_path), "text.ply"), "rb").read()
