@@ -55,6 +55,7 @@ def parse():
     ap.add_argument("--no-raycast", action="store_true")
     ap.add_argument("--no-text-load", action="store_true")
     ap.add_argument("--no-mesh-write", action="store_true")
+    ap.add_argument("--no-icp", action="store_true")
     ap.add_argument("--text-dim", type=int, default=512, help="window of the text-record load (<= volume size)")
     ap.add_argument("--stress-n", type=int, default=1024, help="stress volume edge (default 1024)")
     return ap.parse_args()
@@ -422,6 +423,76 @@ def bench_mesh_write(mcg, torch, vol, cell, ctx, reps=5, sample_frac=0.25):
                           "sample": "first %d soup vertices" % k, "seconds": dt}
     except Exception as ex:  # pragma: no cover
         res["cpu_obj"] = {"error": str(ex)}
+    return res
+
+
+def bench_icp(mcg, synthetic, torch, reps=10):
+    """Frame-to-frame tracking (kf.cu:2105-2218): two 640x480 frames of the
+    blended-spheres scene 1.8 degrees / 4 cm apart; per frame the depth
+    pyramid (masks, pyramid_down, mask_to_data) is built once and timed
+    separately, then ICP runs over 3 levels (15 / 11 / 8 iterations at most)
+    from the identity; beside it the oracle's ICP (the same algorithm in C,
+    one core) on the same maps."""
+    import numpy as np
+    scene = synthetic.BlendedSpheres(seed=3)
+    w, h, f = 640, 480, 525.0
+    k0 = mcg.intrinsic(f, f, 319.5, 239.5)
+    P1, P2 = scene.pose(0, 200), scene.pose(1, 200)
+    depth = [scene.depth_frame(*P, w=w, h=h, fx=f, fy=f, cx=319.5, cy=239.5, device="cuda").float().contiguous()
+             for P in (P1, P2)]
+
+    def build(d):
+        lv, k = [], k0
+        for i in range(3):
+            if i > 0:
+                m = mcg.float_data_to_mask(d)
+                d, dm = mcg.pyramid_down(d, m)
+                mcg.float_mask_to_data(dm, d)
+                k = mcg.intrinsic_pyramid_down(k)
+            v = mcg.meter_to_vertex(d, k)
+            lv.append((v, mcg.vertex_to_normal(v)))
+        return lv
+
+    maps = [build(d) for d in depth]
+    e0 = mcg.extrinsic(np.eye(3), np.zeros(3))
+    inl = torch.zeros((h, w), dtype=torch.uint8, device="cuda")
+    for _ in range(3):
+        ok, e, iters = mcg.icp_pyramid(k0, e0, maps[0], maps[1], inlier=inl)
+        build(depth[1])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        build(depth[1])
+    torch.cuda.synchronize()
+    pyr_ms = (time.perf_counter() - t0) / reps * 1e3
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        ok, e, iters = mcg.icp_pyramid(k0, e0, maps[0], maps[1], inlier=inl)
+    torch.cuda.synchronize()
+    icp_ms = (time.perf_counter() - t0) / reps * 1e3
+    res = {"frame": [w, h], "levels": 3, "ok": ok, "iterations": iters, "pyramid_and_maps_ms": pyr_ms,
+           "icp_ms": icp_ms, "ms_per_iteration": icp_ms / max(1, sum(iters))}
+    try:
+        import math
+        import oracle as orc
+        ks = [orc.intrinsic(f, f, 319.5, 239.5)]
+        for _ in range(2):
+            ks.append(orc.intrinsic(ks[-1].fx / 2, ks[-1].fy / 2, ks[-1].cx / 2, ks[-1].cy / 2))
+        hm = [[(v.cpu().numpy(), n.cpu().numpy()) for v, n in lv] for lv in maps]
+        oe = orc.extrinsic(np.eye(3), np.zeros(3))
+        t0 = time.perf_counter()
+        for lv, it_max in ((2, 8), (1, 11), (0, 15)):
+            okc, (r, t), _, _ = orc.icp(math.cos(math.radians(20)), 0.10, math.radians(20), 0.10, it_max, ks[lv], oe,
+                                        hm[0][lv][0], hm[0][lv][1], hm[1][lv][0], hm[1][lv][1])
+            oe = orc.Extrinsic()
+            for i in range(9):
+                oe.r[i] = float(r[i])
+            for i in range(3):
+                oe.t[i] = float(t[i])
+        res["cpu_icp"] = {"ms": (time.perf_counter() - t0) * 1e3, "cores": 1, "kind": "port",
+                          "sample": "the same 3-level ICP on the same maps"}
+    except Exception as ex:  # pragma: no cover
+        res["cpu_icp"] = {"error": str(ex)}
     return res
 
 
@@ -823,6 +894,13 @@ def main():
         except Exception as ex:  # pragma: no cover
             mesh_write = {"error": str(ex)}
 
+    icp = None
+    if not args.no_icp:
+        try:
+            icp = bench_icp(mcg, synthetic, torch)
+        except Exception as ex:  # pragma: no cover
+            icp = {"error": str(ex)}
+
     indexed = None
     if not args.no_indexed:
         try:
@@ -873,6 +951,7 @@ def main():
         "raycast": raycast,
         "text_load": text_load,
         "mesh_write": mesh_write,
+        "icp": icp,
         "stress": stress,
     }
     if rank == 0:

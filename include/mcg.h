@@ -271,6 +271,46 @@ mcg_status mcg_raycast(mcg_context *ctx, const void *vol, int32_t nx, int32_t ny
                        const mcg_intrinsic *k, const mcg_extrinsic *e, int32_t w, int32_t h, float *depth,
                        float *normal, mcg_stream_t stream);
 
+/* ---- depth pyramid and ICP: kf.cu:66-80, 226-261, 988-1301 ---------------- */
+/* d_pyramid_down: dst (dw x dh) from src (sw x sh): the mean of the valid
+ * src values within sigma of the centre pixel (2x, 2y) over the clipped
+ * 5 x 5 window from (2x - 2, 2y - 2); masks are 0 / 0xff per pixel. */
+mcg_status mcg_pyramid_down(mcg_context *ctx, int32_t sw, int32_t sh, int32_t dw, int32_t dh, const float *src,
+                            const uint8_t *src_mask, float *dst, uint8_t *dst_mask, float sigma, mcg_stream_t stream);
+/* to_mask = 1: d_float_data_to_mask (mask = data != 0 ? 0xff : 0);
+ * to_mask = 0: d_float_mask_to_data (data = 0 where mask == 0). */
+mcg_status mcg_depth_mask(mcg_context *ctx, int64_t n, float *data, uint8_t *mask, int32_t to_mask,
+                          mcg_stream_t stream);
+/* nwf_icp_projective_3d_params */
+typedef struct mcg_icp_params {
+    float nt;          /* a match needs dot(n1, R n2) > nt */
+    float dt;          /* ... and |v1 - (R v2 + t)| < dt */
+    float rt, tt;      /* bounds of one step's rotation (rad) / translation components */
+    int32_t it_max;    /* iterations (the reference's icp_it_max of the level) */
+    int32_t bilinear;  /* 0: nearest pixel (step 1), 1: bilinear sub-pixel (step 4) */
+} mcg_icp_params;
+/* One correspondence pass at pose_rel (steps 1/4, 2, 3): v21 (3 floats per
+ * pixel of map 1; x = FLT_MAX where there is no match), A (6 columns of
+ * w1*h1 floats), b, inlier flags; each output may be NULL (A and b
+ * together).  Maps are float3 device arrays (vertex and unit normal; a zero
+ * normal marks an invalid pixel).  Synchronous. */
+mcg_status mcg_icp_correspond(mcg_context *ctx, const mcg_icp_params *params, const mcg_intrinsic *k2,
+                              const mcg_extrinsic *pose_rel, int32_t w1, int32_t h1, int32_t w2, int32_t h2,
+                              const float *v1, const float *n1, const float *v2, const float *n2, float *v21,
+                              float *A, float *b, uint8_t *inlier, mcg_stream_t stream);
+/* _cu_icp_projective_3d: point-to-plane ICP aligning map 2 to map 1 (pose
+ * maps map-2 points into map 1's frame), starting from and updating
+ * *pose_rel.  Per iteration one fused correspondence + normal-equation
+ * kernel (binary64 sums of the reference's binary32 products) and one
+ * device solve (Cholesky, |det| > 1e-15, 1-norm rcond > 5e-5, increment
+ * bounds, Rodrigues exp, compose, stop when the distance grows or drops
+ * below 1e-5); no host round trip inside the loop.  *ok = the reference's
+ * return value; the pose and the inlier map (may be NULL) are written only
+ * when *ok.  Synchronous at the end. */
+mcg_status mcg_icp(mcg_context *ctx, const mcg_icp_params *params, const mcg_intrinsic *k2, mcg_extrinsic *pose_rel,
+                   int32_t w1, int32_t h1, int32_t w2, int32_t h2, const float *v1, const float *n1, const float *v2,
+                   const float *n2, uint8_t *inlier, int32_t *ok, int32_t *iterations, mcg_stream_t stream);
+
 /* ---- RLE volume codec: kf.cu:1303-1600 ----------------------------------- */
 /* upper bound of the encoded file image size */
 int64_t mcg_rle_bound(int32_t nx, int32_t ny, int32_t nz);

@@ -970,3 +970,121 @@ def mesh_write(mesh: Mesh, path, qi_path=None, n=None, ctx=None, stream=None):
     ctx = ctx or default_context(mesh.soup.device.index)
     ctx.check(_lib.mcg_mesh_write(ctx.handle, _ptr(mesh.soup), _ptr(mesh.normals), n, os.fsencode(path),
                                   os.fsencode(qi_path) if qi_path else None, _stream(stream)), "mcg_mesh_write")
+
+
+# ---------------------------------------------------------------------------
+# depth pyramid and ICP (kf.cu:66-80, 226-261, 988-1301)
+# ---------------------------------------------------------------------------
+import math as _math
+
+ICP_DT = 0.10                                   # kf.cu:1966 (100 mm)
+ICP_NT = float(_math.cos(_math.radians(20.0)))  # kf.cu:1967
+ICP_RT = _math.radians(20.0)                    # kf.cu:1968
+ICP_TT = 0.10                                   # kf.cu:1969
+ICP_IT_MAX = (15, 11, 8)                        # kf.cu:1970, per level (0 = full size)
+PYRAMID_SIGMA = 0.06                            # kf.cu:2117
+
+
+def icp_params(it_max, bilinear=False, dt=ICP_DT, nt=ICP_NT, rt=ICP_RT, tt=ICP_TT):
+    p = _capi.IcpParams()
+    p.nt, p.dt, p.rt, p.tt = float(nt), float(dt), float(rt), float(tt)
+    p.it_max = int(it_max)
+    p.bilinear = 1 if bilinear else 0
+    return p
+
+
+def intrinsic_pyramid_down(k):
+    """float_camera_intrinsic_pyramid_down (cu_geometry_functions.h:218-225): fc / 2, cc / 2."""
+    return intrinsic(k.fx / 2.0, k.fy / 2.0, k.cx / 2.0, k.cy / 2.0)
+
+
+def float_data_to_mask(data, mask=None, ctx=None, stream=None):
+    """d_float_data_to_mask: 0xff where data != 0 (uint8 tensor)."""
+    mask = torch.empty(data.shape, dtype=torch.uint8, device=data.device) if mask is None else mask
+    ctx = ctx or default_context(data.device.index)
+    ctx.check(_lib.mcg_depth_mask(ctx.handle, data.numel(), _ptr(data), _ptr(mask), 1, _stream(stream)),
+              "mcg_depth_mask")
+    return mask
+
+
+def float_mask_to_data(mask, data, ctx=None, stream=None):
+    """d_float_mask_to_data: data = 0 where mask == 0 (in place)."""
+    ctx = ctx or default_context(data.device.index)
+    ctx.check(_lib.mcg_depth_mask(ctx.handle, data.numel(), _ptr(data), _ptr(mask), 0, _stream(stream)),
+              "mcg_depth_mask")
+    return data
+
+
+def pyramid_down(src, mask, dst_shape=None, sigma=PYRAMID_SIGMA, ctx=None, stream=None):
+    """d_pyramid_down (kf.cu:226-261): (dst, dst_mask) of half size (or
+    dst_shape = (h, w)); dst is zero where dst_mask is 0."""
+    sh, sw = src.shape
+    dh, dw = dst_shape if dst_shape is not None else (sh >> 1, sw >> 1)
+    dst = torch.zeros((dh, dw), dtype=torch.float32, device=src.device)
+    dmask = torch.empty((dh, dw), dtype=torch.uint8, device=src.device)
+    ctx = ctx or default_context(src.device.index)
+    ctx.check(_lib.mcg_pyramid_down(ctx.handle, sw, sh, dw, dh, _ptr(src), _ptr(mask), _ptr(dst), _ptr(dmask),
+                                    float(sigma), _stream(stream)), "mcg_pyramid_down")
+    return dst, dmask
+
+
+def _maps(v1, n1, v2, n2):
+    for m in (v1, n1, v2, n2):
+        if m.dtype != torch.float32 or m.dim() != 3 or m.shape[2] != 3 or not m.is_contiguous():
+            raise ValueError("vertex / normal maps are contiguous (h, w, 3) float32 tensors")
+    if v1.shape != n1.shape or v2.shape != n2.shape:
+        raise ValueError("vertex and normal maps of a frame have one shape")
+    return v1.shape[1], v1.shape[0], v2.shape[1], v2.shape[0]
+
+
+def icp_correspond(params, k2, pose, v1, n1, v2, n2, ctx=None, stream=None):
+    """One correspondence pass at `pose` (steps 1/4, 2, 3): dict of v21
+    (h1, w1, 3), A (6, h1*w1), b (h1*w1,), inlier (h1, w1) uint8."""
+    w1, h1, w2, h2 = _maps(v1, n1, v2, n2)
+    dev = v1.device
+    out = {"v21": torch.empty((h1, w1, 3), dtype=torch.float32, device=dev),
+           "A": torch.empty((6, h1 * w1), dtype=torch.float32, device=dev),
+           "b": torch.empty(h1 * w1, dtype=torch.float32, device=dev),
+           "inlier": torch.empty((h1, w1), dtype=torch.uint8, device=dev)}
+    ctx = ctx or default_context(dev.index)
+    ctx.check(_lib.mcg_icp_correspond(ctx.handle, ctypes.byref(params), ctypes.byref(k2), ctypes.byref(pose), w1, h1,
+                                      w2, h2, _ptr(v1), _ptr(n1), _ptr(v2), _ptr(n2), _ptr(out["v21"]),
+                                      _ptr(out["A"]), _ptr(out["b"]), _ptr(out["inlier"]), _stream(stream)),
+              "mcg_icp_correspond")
+    return out
+
+
+def icp(params, k2, pose, v1, n1, v2, n2, inlier=None, ctx=None, stream=None):
+    """_cu_icp_projective_3d: align map 2 (v2, n2) to map 1 starting from
+    `pose` (an Extrinsic mapping map-2 points into map 1's frame).  Returns
+    (ok, pose, iterations); the returned pose and `inlier` are updated only
+    when ok."""
+    w1, h1, w2, h2 = _maps(v1, n1, v2, n2)
+    out = _capi.Extrinsic()
+    ctypes.memmove(ctypes.byref(out), ctypes.byref(pose), ctypes.sizeof(out))
+    ok, iters = ctypes.c_int32(0), ctypes.c_int32(0)
+    ctx = ctx or default_context(v1.device.index)
+    ctx.check(_lib.mcg_icp(ctx.handle, ctypes.byref(params), ctypes.byref(k2), ctypes.byref(out), w1, h1, w2, h2,
+                           _ptr(v1), _ptr(n1), _ptr(v2), _ptr(n2), _ptr(inlier), ctypes.byref(ok), ctypes.byref(iters),
+                           _stream(stream)), "mcg_icp")
+    return bool(ok.value), out, int(iters.value)
+
+
+def icp_pyramid(k0, pose, maps1, maps2, it_max=ICP_IT_MAX, bilinear=False, inlier=None, ctx=None, stream=None):
+    """The fusion loop's tracking (kf.cu:2213-2218): ICP from the coarsest
+    level to the finest, each level starting from the pose of the one
+    before; stops at the first level that fails.  maps1 / maps2: lists of
+    (vertex, normal) per level, level 0 the full size; k0 the level-0
+    intrinsic (halved per level); the inlier map is that of level 0."""
+    ks = [k0]
+    for _ in range(1, len(maps1)):
+        ks.append(intrinsic_pyramid_down(ks[-1]))
+    ok, iters = True, []
+    for lv in range(len(maps1) - 1, -1, -1):
+        p = icp_params(it_max[lv], bilinear)
+        ok, pose, it = icp(p, ks[lv], pose, maps1[lv][0], maps1[lv][1], maps2[lv][0], maps2[lv][1],
+                           inlier=inlier if lv == 0 else None, ctx=ctx, stream=stream)
+        iters.append(it)
+        if not ok:
+            break
+    return ok, pose, iters[::-1]

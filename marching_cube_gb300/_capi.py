@@ -42,6 +42,11 @@ class TextInfo(ctypes.Structure):
                 ("fail_offset", c_int64), ("filled_rest", c_int32), ("reserved", c_int32)]
 
 
+class IcpParams(ctypes.Structure):
+    _fields_ = [("nt", c_float), ("dt", c_float), ("rt", c_float), ("tt", c_float), ("it_max", c_int32),
+                ("bilinear", c_int32)]
+
+
 class Intrinsic(ctypes.Structure):
     _fields_ = [("fx", c_float), ("fy", c_float), ("cx", c_float), ("cy", c_float),
                 ("dc", c_float * 5)]
@@ -111,6 +116,15 @@ SIGNATURES = {
     "mcg_mesh_obj": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_int64, ctypes.POINTER(c_int64),
                              c_void_p, c_int64, ctypes.POINTER(c_int64), c_void_p]),
     "mcg_mesh_write": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, ctypes.c_char_p, ctypes.c_char_p, c_void_p]),
+    "mcg_pyramid_down": (c_int, [c_void_p, c_int32, c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p,
+                                 c_void_p, c_float, c_void_p]),
+    "mcg_depth_mask": (c_int, [c_void_p, c_int64, c_void_p, c_void_p, c_int32, c_void_p]),
+    "mcg_icp_correspond": (c_int, [c_void_p, ctypes.POINTER(IcpParams), ctypes.POINTER(Intrinsic),
+                                   ctypes.POINTER(Extrinsic), c_int32, c_int32, c_int32, c_int32, c_void_p, c_void_p,
+                                   c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "mcg_icp": (c_int, [c_void_p, ctypes.POINTER(IcpParams), ctypes.POINTER(Intrinsic), ctypes.POINTER(Extrinsic),
+                        c_int32, c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                        ctypes.POINTER(c_int32), ctypes.POINTER(c_int32), c_void_p]),
     "mcg_text_records_parse": (c_int, [c_void_p, c_void_p, c_int64, c_int32, ctypes.POINTER(c_int32), c_void_p,
                                        ctypes.POINTER(TextInfo), c_void_p]),
     "mcg_text_records_load": (c_int, [c_void_p, c_void_p, c_int64, c_int32, ctypes.POINTER(c_int32), c_void_p,

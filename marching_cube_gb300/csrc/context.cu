@@ -90,6 +90,11 @@ mcg_status mcg_destroy(mcg_context *ctx) {
     cudaFree(ctx->mw_int);
     cudaFree(ctx->mw_len);
     cudaFree(ctx->mw_text);
+    cudaFree(ctx->icp_state);
+    if (ctx->h_icp_state) cudaFreeHost(ctx->h_icp_state);
+    cudaFree(ctx->icp_partial);
+    cudaFree(ctx->icp_pose);
+    cudaFree(ctx->icp_inlier);
     cudaFree(ctx->depth_scaled);
     cudaFree(ctx->ray_x);
     if (ctx->h_ray_x) cudaFreeHost(ctx->h_ray_x);

@@ -128,6 +128,18 @@ struct mcg_context {
     unsigned char *mw_text = nullptr;
     size_t mw_text_cap = 0;
 
+    // ICP: loop state (device + pinned copy), per-CTA sums, a pose for the
+    // single correspondence pass, inlier flags of the passes
+    unsigned char *icp_state = nullptr;
+    size_t icp_state_cap = 0;
+    unsigned char *h_icp_state = nullptr;  // pinned
+    double *icp_partial = nullptr;
+    size_t icp_partial_cap = 0;
+    float *icp_pose = nullptr;
+    size_t icp_pose_cap = 0;
+    uint8_t *icp_inlier = nullptr;
+    size_t icp_inlier_cap = 0;
+
     // integrate scratch
     float *depth_scaled = nullptr;
     size_t depth_scaled_cap = 0;

@@ -71,6 +71,16 @@ def lib():
             "orc_text_load": (i32, [ctypes.c_char_p, i64, i32, i32, i32, i32, vp, vp]),
             "orc_text_load_file": (i32, [ctypes.c_char_p, i64, i32, i32, i32, i32, vp, vp]),
             "orc_mesh_ply": (i64, [vp, vp, i64, vp, i64]),
+            "orc_float_data_to_mask": (None, [i64, vp, vp]),
+            "orc_float_mask_to_data": (None, [i64, vp, vp]),
+            "orc_pyramid_down": (None, [i32, i32, i32, i32, vp, vp, vp, vp, f32]),
+            "orc_icp_correspond": (None, [i32, f32, f32, vp, vp, vp, i32, i32, i32, i32, vp, vp, vp, vp, vp, vp, vp,
+                                          vp]),
+            "orc_icp_normal_equations": (None, [i64, vp, vp, vp, vp]),
+            "orc_icp_solve": (i32, [vp, vp, vp, vp]),
+            "orc_so3_exp": (None, [vp, vp]),
+            "orc_icp": (i32, [i32, f32, f32, f32, f32, i32, vp, vp, vp, i32, i32, i32, i32, vp, vp, vp, vp, vp, vp, vp,
+                              vp, vp]),
             "orc_mesh_obj": (None, [vp, vp, i64, vp, i64, vp, i64, vp]),
         }
         for name, (res, args) in sig.items():
@@ -459,3 +469,74 @@ def mesh_obj(soup, normals):
     qi = np.empty(sizes[1], np.uint8)
     lib().orc_mesh_obj(_p(soup), _p(normals), n, _p(obj), int(sizes[0]), _p(qi), int(sizes[1]), _p(sizes))
     return obj.tobytes(), qi.tobytes()
+
+
+# ---------------------------------------------------------------------------
+# depth pyramid and ICP (kf.cu:66-80, 226-261, 988-1301)
+# ---------------------------------------------------------------------------
+def float_data_to_mask(data):
+    data = np.ascontiguousarray(data, np.float32)
+    mask = np.empty(data.shape, np.uint8)
+    lib().orc_float_data_to_mask(data.size, _p(data), _p(mask))
+    return mask
+
+
+def float_mask_to_data(mask, data):
+    data = np.array(data, np.float32, copy=True)
+    mask = np.ascontiguousarray(mask, np.uint8)
+    lib().orc_float_mask_to_data(data.size, _p(mask), _p(data))
+    return data
+
+
+def pyramid_down(src, mask, dst_shape, sigma=0.06):
+    """(dst, dst_mask) of kf.cu:226-261; src / mask (h, w); dst left 0
+    where the mask is 0 (the reference leaves it unwritten)."""
+    src = np.ascontiguousarray(src, np.float32)
+    mask = np.ascontiguousarray(mask, np.uint8)
+    sh, sw = src.shape
+    dh, dw = dst_shape
+    dst = np.zeros((dh, dw), np.float32)
+    dmask = np.zeros((dh, dw), np.uint8)
+    lib().orc_pyramid_down(sw, sh, dw, dh, _p(src), _p(mask), _p(dst), _p(dmask), float(sigma))
+    return dst, dmask
+
+
+def _k4(k):
+    return np.array([k.fx, k.fy, k.cx, k.cy], np.float32)
+
+
+def _pose(e):
+    return np.array(list(e.r), np.float32), np.array(list(e.t), np.float32)
+
+
+def icp_correspond(nt, dt, k, e, v1, n1, v2, n2, bilinear=False):
+    """One correspondence pass: (v21 (h1, w1, 3), A (6, n), b (n), inlier (h1, w1))."""
+    v1, n1, v2, n2 = (np.ascontiguousarray(a, np.float32) for a in (v1, n1, v2, n2))
+    h1, w1 = v1.shape[:2]
+    h2, w2 = v2.shape[:2]
+    r, t = _pose(e)
+    v21 = np.zeros((h1, w1, 3), np.float32)
+    A = np.zeros((6, h1 * w1), np.float32)
+    b = np.zeros(h1 * w1, np.float32)
+    inl = np.zeros((h1, w1), np.uint8)
+    lib().orc_icp_correspond(1 if bilinear else 0, float(nt), float(dt), _p(_k4(k)), _p(r), _p(t), w1, h1, w2, h2,
+                             _p(v1), _p(n1), _p(v2), _p(n2), _p(v21), _p(A), _p(b), _p(inl))
+    return v21, A, b, inl
+
+
+def icp(nt, dt, rt, tt, it_max, k, e, v1, n1, v2, n2, bilinear=False):
+    """_cu_icp_projective_3d: (ok, (r, t) updated pose, iterations, inlier map)."""
+    v1, n1, v2, n2 = (np.ascontiguousarray(a, np.float32) for a in (v1, n1, v2, n2))
+    h1, w1 = v1.shape[:2]
+    h2, w2 = v2.shape[:2]
+    r, t = _pose(e)
+    n = h1 * w1
+    v21 = np.zeros(3 * n, np.float32)
+    A = np.zeros(6 * n, np.float32)
+    b = np.zeros(n, np.float32)
+    inl = np.zeros((h1, w1), np.uint8)
+    iters = np.zeros(1, np.int32)
+    ok = lib().orc_icp(1 if bilinear else 0, float(nt), float(dt), float(rt), float(tt), int(it_max), _p(_k4(k)),
+                       _p(r), _p(t), w1, h1, w2, h2, _p(v1), _p(n1), _p(v2), _p(n2), _p(inl), _p(v21), _p(A), _p(b),
+                       _p(iters))
+    return bool(ok), (r, t), int(iters[0]), inl
