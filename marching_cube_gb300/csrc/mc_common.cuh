@@ -23,10 +23,20 @@ constexpr int BX = 32, BY = 8, BZ = 8;
 constexpr int BRICK_CUBES = BX * BY * BZ;  // 2048
 constexpr int CHUNK = 256;                 // bricks per scan chunk
 // per-chunk sums written by the count pass: triangles, active bricks,
-// occupied cubes, heavy bricks (more than HEAVY_TRIS triangles: more than one
-// pass of a 256-thread CTA over their soup vertices)
-constexpr int CHUNK_FIELDS = 4;
+// occupied cubes, then heavy bricks by class.  A brick is heavy when it has
+// more than HEAVY_TRIS triangles (more than one pass of a 256-thread CTA over
+// its soup vertices); class k holds the bricks with more than
+// HEAVY_TRIS << (NHEAVY - 1 - k) triangles not in a lower class, so class 0
+// is the heaviest.  The active list holds the classes in order, then the
+// light bricks: the longest bricks start first and the tail stays short.
+constexpr int NHEAVY = 4;
+constexpr int CHUNK_FIELDS = 3 + NHEAVY;
 constexpr unsigned int HEAVY_TRIS = 85;
+__host__ __device__ __forceinline__ int heavy_class(unsigned int t) {
+    for (int k = 0; k < NHEAVY; ++k)
+        if (t > (HEAVY_TRIS << (NHEAVY - 1 - k))) return k;
+    return -1;
+}
 
 __host__ __device__ constexpr int pad128(int bytes) { return (bytes + 127) / 128 * 128; }
 

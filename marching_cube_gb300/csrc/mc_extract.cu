@@ -373,7 +373,8 @@ __global__ void __launch_bounds__(CLS_THREADS)
                 atomicAdd(c + 0, t);
                 atomicAdd(c + 1, 1u);
                 atomicAdd(c + 2, o);
-                if (t > HEAVY_TRIS) atomicAdd(c + 3, 1u);
+                const int hc = heavy_class(t);
+                if (hc >= 0) atomicAdd(c + 3 + hc, 1u);
             }
         }
         if (!TMA) __syncthreads();  // S.sitem[0] is rewritten at the top
@@ -387,97 +388,106 @@ __global__ void __launch_bounds__(CLS_THREADS)
 
 // ---- scan: brick counts -> soup offsets + active brick list ---------------------
 // One CTA per chunk of CHUNK consecutive bricks.  Classify has accumulated
-// each chunk's (triangles, active bricks, occupied cubes); a CTA adds up the
-// chunks before its own for its base offsets, scans its bricks, and writes
-// 64-bit soup offsets and its part of the active-brick list (brick order).
-// CTA 0 also writes the totals.
+// each chunk's triangles, active bricks, occupied cubes and heavy bricks by
+// class; a CTA adds up the chunks before its own for its base offsets, scans
+// its bricks, and writes 64-bit soup offsets and its part of the active-brick
+// list: heavy classes first (heaviest first), then the light bricks, each in
+// brick order.  CTA 0 also writes the totals.
 __global__ void __launch_bounds__(CHUNK)
     mc_scan_kernel(const uint32_t *__restrict__ brick_tris, const uint32_t *__restrict__ chunk, long long nb,
                    unsigned long long *__restrict__ brick_vofs, uint32_t *__restrict__ active,
                    MeshTotals *__restrict__ totals) {
-    __shared__ unsigned long long s_part[7][CHUNK / 32];
+    // acc: [0] base tris, [1] base active, [2, 2+NH) base heavy per class,
+    // [2+NH] all tris, [3+NH] all active, [4+NH] all occupied, [5+NH, 5+2NH) all heavy
+    constexpr int NH = NHEAVY, NACC = 5 + 2 * NH, NF = NH + 2;  // scanned per brick: tris, classes, light
+    __shared__ unsigned long long s_part[NACC][CHUNK / 32];
     __shared__ unsigned long long s_base_v;
-    __shared__ unsigned int s_base_h, s_base_l, s_heavy;
+    __shared__ unsigned int s_base[NH + 1];  // list offset of this chunk's first brick of each class / light
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const long long j = blockIdx.x;
     const long long nchunks = (nb + CHUNK - 1) / CHUNK;
-    // base offsets: sums over the chunks before this one; every CTA also sums
-    // all chunks' heavy bricks (the light ones follow them in the list), CTA 0
-    // the totals.
-    // acc: base tris, base active, base heavy, all tris, all active, all occupied, all heavy
-    unsigned long long acc[7] = {0, 0, 0, 0, 0, 0, 0};
+    unsigned long long acc[NACC];
+#pragma unroll
+    for (int k = 0; k < NACC; ++k) acc[k] = 0;
     for (long long i = tid; i < nchunks; i += CHUNK) {
         const uint32_t *c = chunk + i * CHUNK_FIELDS;
-        const unsigned long long cv = c[0], ca = c[1], ch = c[3];
+        const unsigned long long cv = c[0], ca = c[1];
         if (i < j) {
             acc[0] += cv;
             acc[1] += ca;
-            acc[2] += ch;
+#pragma unroll
+            for (int k = 0; k < NH; ++k) acc[2 + k] += c[3 + k];
         }
-        acc[3] += cv;
-        acc[4] += ca;
-        acc[5] += c[2];
-        acc[6] += ch;
+        acc[2 + NH] += cv;
+        acc[3 + NH] += ca;
+        acc[4 + NH] += c[2];
+#pragma unroll
+        for (int k = 0; k < NH; ++k) acc[5 + NH + k] += c[3 + k];
     }
 #pragma unroll
-    for (int k = 0; k < 7; ++k) {
+    for (int k = 0; k < NACC; ++k) {
 #pragma unroll
         for (int o = 16; o; o >>= 1) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], o);
         if (lane == 0) s_part[k][warp] = acc[k];
     }
     __syncthreads();
     if (tid == 0) {
-        unsigned long long r[7] = {0, 0, 0, 0, 0, 0, 0};
-        for (int k = 0; k < 7; ++k)
+        unsigned long long r[NACC];
+        for (int k = 0; k < NACC; ++k) {
+            r[k] = 0;
             for (int w = 0; w < CHUNK / 32; ++w) r[k] += s_part[k][w];
+        }
         s_base_v = r[0];
-        s_base_h = (unsigned int)r[2];
-        s_base_l = (unsigned int)(r[1] - r[2]);
-        s_heavy = (unsigned int)r[6];
+        unsigned long long start = 0, heavy_before = 0;  // list start of the class; heavy bricks of earlier chunks
+        for (int k = 0; k < NH; ++k) {
+            s_base[k] = (unsigned int)(start + r[2 + k]);
+            start += r[5 + NH + k];
+            heavy_before += r[2 + k];
+        }
+        s_base[NH] = (unsigned int)(start + (r[1] - heavy_before));
         if (j == 0) {
-            totals->occupied = r[5];
-            totals->triangles = r[3];
-            totals->vertices = 3ull * r[3];
-            totals->active_bricks = (unsigned int)r[4];
+            totals->occupied = r[4 + NH];
+            totals->triangles = r[2 + NH];
+            totals->vertices = 3ull * r[2 + NH];
+            totals->active_bricks = (unsigned int)r[3 + NH];
         }
     }
     __syncthreads();
     const unsigned long long base_v = s_base_v;
-    // scan of this chunk's bricks; the active list holds the heavy bricks
-    // (more than HEAVY_TRIS triangles) first, then the light ones, each in
-    // brick order, so the longest bricks start first and the tail is short
     const long long b = j * CHUNK + tid;
     const unsigned int t = b < nb ? brick_tris[b] : 0u;
-    const unsigned int fh = t > HEAVY_TRIS, fl = t != 0 && !fh;
-    unsigned int it = t, ih = fh, il = fl;
+    const int cls = t == 0 ? -1 : (heavy_class(t) >= 0 ? heavy_class(t) : NH);  // NH: light
+    unsigned int f[NF], x[NF];
+    f[0] = t;
+#pragma unroll
+    for (int k = 0; k <= NH; ++k) f[1 + k] = cls == k ? 1u : 0u;
+#pragma unroll
+    for (int k = 0; k < NF; ++k) x[k] = f[k];
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-        const unsigned int x = __shfl_up_sync(0xffffffffu, it, o);
-        const unsigned int y = __shfl_up_sync(0xffffffffu, ih, o);
-        const unsigned int z = __shfl_up_sync(0xffffffffu, il, o);
-        if (lane >= o) {
-            it += x;
-            ih += y;
-            il += z;
+#pragma unroll
+        for (int k = 0; k < NF; ++k) {
+            const unsigned int u = __shfl_up_sync(0xffffffffu, x[k], o);
+            if (lane >= o) x[k] += u;
         }
     }
-    __shared__ unsigned int s_w[3][CHUNK / 32];
+    __shared__ unsigned int s_w[NF][CHUNK / 32];
     if (lane == 31) {
-        s_w[0][warp] = it;
-        s_w[1][warp] = ih;
-        s_w[2][warp] = il;
+#pragma unroll
+        for (int k = 0; k < NF; ++k) s_w[k][warp] = x[k];
     }
     __syncthreads();
-    unsigned int wt = 0, wh = 0, wl = 0;
-    for (int w = 0; w < warp; ++w) {
-        wt += s_w[0][w];
-        wh += s_w[1][w];
-        wl += s_w[2][w];
+    unsigned int wp[NF];
+#pragma unroll
+    for (int k = 0; k < NF; ++k) {
+        wp[k] = 0;
+        for (int w = 0; w < warp; ++w) wp[k] += s_w[k][w];
     }
     if (b < nb) {
-        brick_vofs[b] = 3ull * (base_v + wt + it - t);
-        if (fh) active[s_base_h + wh + ih - fh] = (uint32_t)b;
-        if (fl) active[s_heavy + s_base_l + wl + il - fl] = (uint32_t)b;
+        brick_vofs[b] = 3ull * (base_v + wp[0] + x[0] - t);
+#pragma unroll
+        for (int k = 0; k <= NH; ++k)
+            if (f[1 + k]) active[s_base[k] + wp[1 + k] + x[1 + k] - 1] = (uint32_t)b;
     }
 }
 
@@ -1047,7 +1057,8 @@ __global__ void __launch_bounds__(CTHREADS)
                 atomicAdd(c + 0, t);
                 atomicAdd(c + 1, 1u);
                 atomicAdd(c + 2, o);
-                if (t > HEAVY_TRIS) atomicAdd(c + 3, 1u);
+                const int hc = heavy_class(t);
+                if (hc >= 0) atomicAdd(c + 3 + hc, 1u);
                 atomicAdd(&vol_sums[2 * v + 0], (unsigned long long)t);
                 atomicAdd(&vol_sums[2 * v + 1], (unsigned long long)o);
             }
