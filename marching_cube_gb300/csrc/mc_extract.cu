@@ -593,19 +593,15 @@ __device__ __forceinline__ void occupied_list(GenSmem<VT> &S, const typename Vox
             if (warp == 1) { cnt += S.wsum[0][0]; vsum += S.wsum[0][1]; }
             const int cy = tid & (BY - 1), cz = tid / BY;
             unsigned int m = cr.occ;
-            const bool small = S.wsum[0][1] + S.wsum[1][1] <= BRICK_CUBES;
             while (m) {
                 const int x = __ffs(m) - 1;
                 m &= m - 1;
                 const unsigned int ci = cube_index(cr, x);
-                const unsigned int nvc = S.nv[ci];
                 S.occ_cube[cnt] = (unsigned short)((cz * BY + cy) * BX + x);
                 S.occ_ci[cnt] = (unsigned char)ci;
                 S.occ_off[cnt] = (unsigned short)vsum;
-                if (small)
-                    for (unsigned int q = 0; q < nvc; ++q) S.vmap[vsum + q] = (unsigned short)cnt;
                 ++cnt;
-                vsum += nvc;
+                vsum += S.nv[ci];
             }
             if (tid == 0) {
                 S.nocc = S.wsum[0][0] + S.wsum[1][0];
@@ -613,6 +609,16 @@ __device__ __forceinline__ void occupied_list(GenSmem<VT> &S, const typename Vox
             }
         }
         __syncthreads();
+        // vertex -> occupied cube map, one occupied cube per thread (a row
+        // per thread would serialise up to 32 x 15 writes)
+        if (S.total <= BRICK_CUBES) {
+            const unsigned int nocc = S.nocc;
+            for (unsigned int i = tid; i < nocc; i += THREADS) {
+                const unsigned int off = S.occ_off[i], nvc = S.nv[S.occ_ci[i]];
+                for (unsigned int q = 0; q < nvc; ++q) S.vmap[off + q] = (unsigned short)i;
+            }
+            __syncthreads();
+        }
 }
 
 template <int VT>
