@@ -16,8 +16,8 @@
 //               its bounds, exp([w]x) (Rodrigues), compose and the stopping
 //               rule of kf.cu:1177-1262, and the loop state on the device.
 // All it_max iterations are enqueued at once; once the loop has ended the
-// remaining launches return at their first instruction, so a sequence of
-// ICP calls can be captured in a CUDA graph.  Per-pixel arithmetic is the
+// remaining launches return at their first instruction.  The host reads the
+// loop state once, after the last launch.  Per-pixel arithmetic is the
 // reference's binary32 in source order (--fmad=false).
 #include <cuda_runtime.h>
 #include <float.h>
