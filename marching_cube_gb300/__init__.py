@@ -375,6 +375,78 @@ def extract_into(volume, cell, outputs: dict, capacity, ctx=None, stream=None):
     return ctx
 
 
+class ExtractStream:
+    """Extraction of a sequence of host volumes (a fusion run's frames, a
+    directory of volumes) with the host link kept busy in both directions:
+    volume i+1 is copied to the device while volume i is extracted and its
+    soup + normals are copied back.  Two contexts, two device volumes and
+    two output sets alternate; copies in each direction have their own
+    stream.  Host buffers should be pinned (page-locked) for the copies to
+    overlap."""
+
+    def __init__(self, shape, cell, capacity, device=None, normals=True):
+        nz, ny, nx = (int(x) for x in shape)
+        if device is None:
+            device = torch.device("cuda", torch.cuda.current_device())
+        self.device = torch.device(device)
+        self.cell = float(cell)
+        self.capacity = int(capacity)
+        self.ctx = [Context(self.device.index), Context(self.device.index)]
+        self.vol = [torch.empty((nz, ny, nx, 2), dtype=torch.int16, device=self.device) for _ in range(2)]
+        self.out = [{"soup": torch.empty((self.capacity, VERTEX_VOXEL_BYTES), dtype=torch.uint8, device=self.device),
+                     "normals": torch.empty((self.capacity, 3), dtype=torch.float32, device=self.device)
+                     if normals else None} for _ in range(2)]
+        self.s_in = torch.cuda.Stream(self.device)
+        self.s_out = torch.cuda.Stream(self.device)
+        self.s_run = [torch.cuda.Stream(self.device), torch.cuda.Stream(self.device)]
+
+    def run(self, host_volumes, host_outputs):
+        """host_volumes: (nz, ny, nx, 2) int16 host tensors; host_outputs:
+        dicts with "soup" ((capacity, 28) uint8) and "normals" ((capacity, 3)
+        float32) host tensors, one per volume (they may repeat once their
+        copy has been consumed).  Returns the counts of every volume (status
+        MCG_ERR_CAPACITY when a soup was cut at the capacity)."""
+        ev_in = [torch.cuda.Event(), torch.cuda.Event()]
+        ev_run = [torch.cuda.Event(), torch.cuda.Event()]
+        ev_out = [torch.cuda.Event(), torch.cuda.Event()]
+        used = [False, False]
+        results = [None] * len(host_volumes)
+        pending = [None, None]  # volume index last extracted with each buffer set
+
+        def collect(b):
+            if pending[b] is not None:
+                results[pending[b]] = counts(self.ctx[b])
+                pending[b] = None
+
+        for i, hv in enumerate(host_volumes):
+            b = i & 1
+            if used[b]:  # the buffers of volume i - 2: extraction read, outputs copied out
+                self.s_in.wait_event(ev_run[b])
+            with torch.cuda.stream(self.s_in):
+                self.vol[b].copy_(hv, non_blocking=True)
+            ev_in[b].record(self.s_in)
+            collect(b)
+            self.s_run[b].wait_event(ev_in[b])
+            if used[b]:
+                self.s_run[b].wait_event(ev_out[b])
+            extract_into(self.vol[b], self.cell, self.out[b], self.capacity, ctx=self.ctx[b],
+                         stream=self.s_run[b])
+            ev_run[b].record(self.s_run[b])
+            pending[b] = i
+            self.s_out.wait_event(ev_run[b])
+            ho = host_outputs[i]
+            with torch.cuda.stream(self.s_out):
+                for k in ("soup", "normals"):
+                    if self.out[b][k] is not None and ho.get(k) is not None:
+                        ho[k].copy_(self.out[b][k], non_blocking=True)
+            ev_out[b].record(self.s_out)
+            used[b] = True
+        self.s_out.synchronize()
+        for b in (0, 1):
+            collect(b)
+        return results
+
+
 def extract_batched(volumes, cells, *, soup=True, normals=True, vi2vox=False, ver_voxel=False, tri_cube=False,
                     ctx=None, stream=None):
     """Marching cubes over many volumes (same voxel type, any sizes) with one
