@@ -177,7 +177,7 @@ mcg_status mcg_mc_extract_batched(mcg_context *ctx, const mcg_volume *vols, cons
  * budget), or a real-time loop that forbids allocation once running
  * (cudaMalloc/cudaFree may synchronise the device and take unbounded time).
  * It takes no context and allocates nothing: its scratch is one static
- * device array of MCG_NOALLOC_SCRATCH_BYTES (about 1.25 MiB) that every
+ * device array of MCG_NOALLOC_SCRATCH_BYTES (about 1.75 MiB) that every
  * device the library is loaded on holds until the process exits.  Volumes
  * with more than MCG_NOALLOC_MAX_BRICKS bricks of 32x8x8 cubes (e.g. larger
  * than 513^3 voxels) are rejected with MCG_ERR_TOO_LARGE.  The first call on
@@ -188,7 +188,7 @@ mcg_status mcg_mc_extract_batched(mcg_context *ctx, const mcg_volume *vols, cons
  * results: serialise them.  The call waits for its stream to finish and
  * fills *counts (status MCG_ERR_CAPACITY if the soup was truncated). */
 #define MCG_NOALLOC_MAX_BRICKS 65536
-#define MCG_NOALLOC_SCRATCH_BYTES (65536 * 20 + 256)
+#define MCG_NOALLOC_SCRATCH_BYTES (65536 * 28 + 256)
 mcg_status mcg_mc_extract_noalloc(const mcg_volume *vol, const mcg_mesh_out *out,
                                   mcg_mesh_counts *counts, mcg_stream_t stream);
 /* kf.cu:3227-3242 d_voxel_extract_surface_normal(s) for n arbitrary vertex

@@ -44,7 +44,14 @@ mcg_status mcg_create(mcg_context **out, int device) {
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
     if (e == cudaSuccess) e = cudaMalloc((void **)&ctx->d_totals, sizeof(mcg::MeshTotals));
     if (e == cudaSuccess) e = cudaMemset(ctx->d_totals, 0, sizeof(mcg::MeshTotals));
-    if (e == cudaSuccess) e = cudaMallocHost((void **)&ctx->h_totals, sizeof(mcg::MeshTotals));
+    if (e == cudaSuccess)
+        e = cudaHostAlloc((void **)&ctx->h_totals, sizeof(mcg::MeshTotals), cudaHostAllocMapped | cudaHostAllocPortable);
+    // the count and generate launches write the totals straight into host memory
+    // through this address; without one the host copies them
+    if (e == cudaSuccess && cudaHostGetDevicePointer((void **)&ctx->h_totals_dev, ctx->h_totals, 0) != cudaSuccess) {
+        cudaGetLastError();
+        ctx->h_totals_dev = nullptr;
+    }
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->counts_ready, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->btab_copied, cudaEventDisableTiming);
     if (e != cudaSuccess) {
@@ -65,6 +72,7 @@ mcg_status mcg_destroy(mcg_context *ctx) {
     cudaFree(ctx->brick_occ);
     cudaFree(ctx->brick_vofs);
     cudaFree(ctx->active);
+    cudaFree(ctx->list_vofs);
     cudaFree(ctx->brick_uniq);
     cudaFree(ctx->brick_uofs);
     cudaFree(ctx->edge_map);

@@ -69,15 +69,15 @@ constexpr int GSTAGES = 2;
 
 // Row masks: bit k of neg / dead = voxel (x0 + k) of a 33-voxel row is
 // negative / has weight 0, k = 0..32.  One thread builds one row from 16-byte
-// shared-memory loads (`row` must be 16-byte aligned and readable for 36
-// voxels): about 4 integer operations per voxel instead of a warp vote per
-// row.
+// shared-memory loads of its first 32 voxels (`row` 16-byte aligned) and the
+// 33rd voxel `last`: about 4 integer operations per voxel instead of a warp
+// vote per row.  The two-argument form takes the 33rd voxel from the row.
 template <int VT>
 struct RowMask;
 
 template <>
 struct RowMask<MCG_VOXEL_SHORT2> {
-    static __device__ __forceinline__ void build(const short2 *row, unsigned long long &neg,
+    static __device__ __forceinline__ void build(const short2 *row, short2 last, unsigned long long &neg,
                                                  unsigned long long &dead) {
         const uint4 *q = reinterpret_cast<const uint4 *>(row);
         unsigned int n = 0, d = 0;
@@ -91,15 +91,18 @@ struct RowMask<MCG_VOXEL_SHORT2> {
                 d |= (unsigned int)(w[j] < 0x10000u) << (4 * k + j);  // w (high half) == 0
             }
         }
-        const unsigned int w32 = q[8].x;
-        neg = (unsigned long long)n | ((unsigned long long)((w32 >> 15) & 1u) << 32);
-        dead = (unsigned long long)d | ((unsigned long long)(w32 < 0x10000u) << 32);
+        neg = (unsigned long long)n | ((unsigned long long)(last.x < 0) << 32);
+        dead = (unsigned long long)d | ((unsigned long long)(last.y == 0) << 32);
+    }
+    static __device__ __forceinline__ void build(const short2 *row, unsigned long long &neg,
+                                                 unsigned long long &dead) {
+        build(row, row[32], neg, dead);
     }
 };
 
 template <>
 struct RowMask<MCG_VOXEL_FLOAT2> {
-    static __device__ __forceinline__ void build(const float2 *row, unsigned long long &neg,
+    static __device__ __forceinline__ void build(const float2 *row, float2 last, unsigned long long &neg,
                                                  unsigned long long &dead) {
         const float4 *q = reinterpret_cast<const float4 *>(row);
         unsigned int n = 0, d = 0;
@@ -111,9 +114,12 @@ struct RowMask<MCG_VOXEL_FLOAT2> {
             d |= (unsigned int)(v.y == 0.f) << (2 * k);
             d |= (unsigned int)(v.w == 0.f) << (2 * k + 1);
         }
-        const float4 v32 = q[16];
-        neg = (unsigned long long)n | ((unsigned long long)(v32.x < 0.f) << 32);
-        dead = (unsigned long long)d | ((unsigned long long)(v32.y == 0.f) << 32);
+        neg = (unsigned long long)n | ((unsigned long long)(last.x < 0.f) << 32);
+        dead = (unsigned long long)d | ((unsigned long long)(last.y == 0.f) << 32);
+    }
+    static __device__ __forceinline__ void build(const float2 *row, unsigned long long &neg,
+                                                 unsigned long long &dead) {
+        build(row, row[32], neg, dead);
     }
 };
 
@@ -216,121 +222,201 @@ __device__ __forceinline__ void classify_brick(Smem &S, const typename Vox<VT>::
         }
 }
 
-// next brick of the launch for this CTA (dynamic: CTAs take bricks in order
-// from a counter, so a CTA that drew cheap bricks takes more), -1 when done
+// next work item of the launch for this CTA (dynamic: CTAs take items in
+// order from a counter, so a CTA that drew cheap items takes more), -1 when
+// done; launches have fewer than 2^31 items
+__device__ __forceinline__ int next_item(unsigned int *ticket, int n) {
+    const unsigned int t = atomicAdd(ticket, 1u);
+    return t < (unsigned int)n ? (int)t : -1;
+}
+
+// the same over a 64-bit count
 __device__ __forceinline__ long long next_brick(unsigned int *ticket, long long n) {
     const unsigned int t = atomicAdd(ticket, 1u);
     return (long long)t < n ? (long long)t : -1ll;
 }
 
-// Single-volume classify: one work item is a group of G bricks adjacent in x
-// whose tiles share one TMA box of (32 G + 4) x 9 x 9 voxels -- wider boxes
-// keep more of each DRAM row per request (a 36-voxel box streams the volume
-// at about 5.7 TB/s, a 132-voxel box at about 7 TB/s on GB300).
-constexpr int CLS_THREADS = 256;
-
-template <int G>
+// Single-volume classify: one work item is a group of G bricks adjacent in x.
+// Its voxels arrive by two TMA boxes on one mbarrier: the bricks' own
+// 32 G x 9 x 9 voxels (rows of 512 bytes at the preferred G), and a box
+// 16 bytes wide at voxel column x0 + 32 G for the 33rd voxel of the last
+// brick's rows.  A halo of 4 voxels on every row of the main box would add a
+// partial line to each row request: on GB300 a 68-voxel box streams a 512^3
+// short2 volume at about 5.7 TB/s, a 64-voxel box at 6.3 and a 128-voxel box
+// at 7.0.
+template <int G, int XH>
 struct ClsGeom {
-    static constexpr int TXW = BX * G + 4;  // tile width in voxels
+    static constexpr int TXW = BX * G + XH;  // main box width in voxels (XH: in-box halo, 0 or 4)
     static constexpr int TILE = TXW * CTY * CTZ;
 };
 
-template <int VT, int G, int CSTAGES>
+// halo box: the first 16 bytes of each of the ROWS rows right of the main box
+template <int VT>
+struct ClsHalo {
+    static constexpr int HW = 16 / Vox<VT>::bytes;  // voxels per halo row
+    static constexpr int N = HW * ROWS;
+};
+
+template <int VT, int G, int XH, int CSTAGES, int NT>
 struct ClsSmemG {
-    static constexpr int STAGE_BYTES = pad128(ClsGeom<G>::TILE * Vox<VT>::bytes);
+    static constexpr int STAGE_BYTES = pad128(ClsGeom<G, XH>::TILE * Vox<VT>::bytes);
+    static constexpr int HALO_BYTES = XH ? 0 : pad128(ClsHalo<VT>::N * Vox<VT>::bytes);
     unsigned char tiles[CSTAGES][STAGE_BYTES];
+    unsigned char halo[CSTAGES][HALO_BYTES];
     unsigned long long neg[G * ROWS], dead[G * ROWS];  // [brick h of the group][row]
     uint64_t bars[CSTAGES];
-    long long sitem[CSTAGES];  // work item of each stage's tile, -1 when none
-    unsigned int red[CLS_THREADS / 32][2];
-    unsigned int mix[CLS_THREADS / 32];
+    int4 sorg[CSTAGES];  // stage's item: {x0, y0, z0, first brick x}; x0 < 0 when none
+    unsigned int red[NT / 32][2];
+    unsigned int mix[NT / 32];
     unsigned char ntri[256];
     int abort;
 };
 
-template <int VT, bool TMA, int G, int CSTAGES>
-__global__ void __launch_bounds__(CLS_THREADS)
-    mc_classify_kernel(const __grid_constant__ CUtensorMap map, const typename Vox<VT>::T *__restrict__ vol,
-                       int nx, int ny, int nz, int nbx, int nby, long long nitems, int ngx, int zbase, int zlim,
-                       uint32_t *__restrict__ brick_tris, uint32_t *__restrict__ chunk,
-                       unsigned int *__restrict__ flags, unsigned int *__restrict__ ticket) {
+// True when the voxels of the item that lie inside the volume (tile and halo
+// column) hold both negative and non-negative values.  Rows, columns and the
+// halo outside the volume arrive zero-filled and are left out, so the border
+// items of an all-negative volume stay on the one-pass path.  Called by every
+// thread; contains a barrier.
+template <int VT, int G, int XH, int NT, class Smem>
+__device__ __forceinline__ bool item_mixed(Smem &S, const typename Vox<VT>::T *tile, const typename Vox<VT>::T *hal,
+                                           int nx, int ny, int nz, int x0, int y0, int z0) {
+    using V = Vox<VT>;
+    constexpr int WPR = ClsGeom<G, XH>::TXW * V::bytes / 16;  // 16-byte words per row
+    constexpr int VPW = 16 / V::bytes;                   // voxels per word
+    const uint4 *q = reinterpret_cast<const uint4 *>(tile);
+    const int ry = ny - y0, rz = nz - z0, rx = nx - x0;  // inside: ly < ry, lz < rz, lx < rx
+    unsigned int neg_any = 0, pos_any = 0;
+    for (int i = threadIdx.x; i < WPR * ROWS; i += NT) {
+        const int r = i / WPR, lx = (i - r * WPR) * VPW;
+        const int lz = r / CTY, ly = r - lz * CTY;
+        if (ly >= ry || lz >= rz || lx >= rx) continue;
+        const uint4 v = q[i];
+        if (VT == MCG_VOXEL_SHORT2) {
+            // bit 15 of each word is the tsdf sign
+            neg_any |= v.x | v.y | v.z | v.w;
+            pos_any |= ~(v.x & v.y & v.z & v.w);
+        } else {
+            // x and z are the tsdf of two voxels; -0.0f is not negative
+            const bool n0 = __uint_as_float(v.x) < 0.f, n1 = __uint_as_float(v.z) < 0.f;
+            neg_any |= (unsigned int)(n0 | n1) << 15;
+            pos_any |= (unsigned int)(!n0 | !n1) << 15;
+        }
+    }
+    if (XH == 0 && threadIdx.x < ROWS && ClsGeom<G, XH>::TXW < rx) {
+        const int r = threadIdx.x, lz = r / CTY, ly = r - lz * CTY;
+        if (ly < ry && lz < rz) {
+            if (V::neg(hal[r * ClsHalo<VT>::HW])) neg_any |= 0x8000u;
+            else pos_any |= 0x8000u;
+        }
+    }
+    neg_any = __reduce_or_sync(0xffffffffu, neg_any & 0x8000u);
+    pos_any = __reduce_or_sync(0xffffffffu, pos_any & 0x8000u);
+    if ((threadIdx.x & 31) == 0) S.mix[threadIdx.x >> 5] = (neg_any ? 1u : 0u) | (pos_any ? 2u : 0u);
+    __syncthreads();
+    unsigned int m = 0;
+#pragma unroll
+    for (int w = 0; w < NT / 32; ++w) m |= S.mix[w];
+    return m == 3u;
+}
+
+// Persistent CTAs of NT threads take work items from a counter into a ring
+// of CSTAGES tile stages (one thread issues the loads and polls the
+// barriers with a time bound).
+template <int VT, bool TMA, int G, int XH, int CSTAGES, int NT>
+__global__ void __launch_bounds__(NT)
+    mc_classify_kernel(const __grid_constant__ CUtensorMap map, const __grid_constant__ CUtensorMap hmap,
+                       const typename Vox<VT>::T *__restrict__ vol, int nx, int ny, int nz, int nbx, int nby,
+                       int nitems, int ngx, int zbase, int zlim, uint32_t *__restrict__ brick_tris,
+                       uint32_t *__restrict__ chunk, unsigned int *__restrict__ flags,
+                       unsigned int *__restrict__ ticket) {
+    static_assert(NT >= G * CUBE_ROWS && NT >= ROWS && NT % 32 == 0, "one thread per cube row and per halo row");
     using V = Vox<VT>;
     using T = typename V::T;
-    using Geo = ClsGeom<G>;
+    using Geo = ClsGeom<G, XH>;
+    using H = ClsHalo<VT>;
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    ClsSmemG<VT, G, CSTAGES> &S = *reinterpret_cast<ClsSmemG<VT, G, CSTAGES> *>(smem_raw);
+    ClsSmemG<VT, G, XH, CSTAGES, NT> &S = *reinterpret_cast<ClsSmemG<VT, G, XH, CSTAGES, NT> *>(smem_raw);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    for (int c = tid; c < 256; c += CLS_THREADS) S.ntri[c] = (c == 0 || c == 255) ? 0 : c_nverts[c] / 3;
-    auto origin = [&](long long item, int &bx0, int &y0, int &z0) {
-        const long long r = item / ngx;
-        bx0 = (int)(item % ngx) * G;
-        y0 = (int)(r % nby) * BY;
-        z0 = (int)(r / nby) * BZ + zbase;
+    for (int c = tid; c < 256; c += NT) S.ntri[c] = (c == 0 || c == 255) ? 0 : c_nverts[c] / 3;
+    // stage st's item (drawn by thread 0, which alone divides): origin into
+    // S.sorg[st] and, with TMA, its loads -- the halo box only when column
+    // x0 + TXW is inside the volume (its voxel is used by no cube otherwise)
+    auto stage_item = [&](int st, int it) {
+        if (it < 0) {
+            S.sorg[st] = make_int4(-1, 0, 0, 0);
+            return;
+        }
+        const unsigned int r = (unsigned int)it / (unsigned int)ngx;
+        const int bx0 = (int)((unsigned int)it - r * (unsigned int)ngx) * G;
+        const int y0 = (int)(r % (unsigned int)nby) * BY, z0 = (int)(r / (unsigned int)nby) * BZ + zbase;
+        const int x0 = bx0 * BX;
+        S.sorg[st] = make_int4(x0, y0, z0, bx0);
+        if (TMA) {
+            const bool halo = XH == 0 && x0 + Geo::TXW < nx;
+            mbar_arrive_expect_tx(&S.bars[st], (Geo::TILE + (halo ? H::N : 0)) * V::bytes);
+            tma_load_3d(S.tiles[st], &map, &S.bars[st], x0, y0, z0);
+            if (halo) tma_load_3d(S.halo[st], &hmap, &S.bars[st], x0 + Geo::TXW, y0, z0);
+        }
     };
-    // thread 0 draws the item of the next refill one iteration ahead, so the
-    // counter's round trip overlaps the current item
-    long long pend = -1;
+    // Thread 0 draws the ticket of the next refill one iteration ahead and
+    // reads it only at that refill: the counter is contended by every CTA, and
+    // a use right after the atomic would hold warp 0 -- and with it the whole
+    // CTA at the next barrier -- for the round trip.  The first stages take
+    // CSTAGES consecutive tickets with one atomic.
+    unsigned int ptk = 0xffffffffu;
     if (tid == 0) {
         S.abort = 0;
         if (TMA) {
             for (int s = 0; s < CSTAGES; ++s) mbar_init(&S.bars[s], 1);
             fence_barrier_init();
-            bool more = true;
-            for (int s = 0; s < CSTAGES; ++s) {
-                const long long it = more ? next_brick(ticket, nitems) : -1ll;
-                more = it >= 0;
-                S.sitem[s] = it;
-                if (!more) continue;
-                int bx0, y0, z0;
-                origin(it, bx0, y0, z0);
-                mbar_arrive_expect_tx(&S.bars[s], Geo::TILE * V::bytes);
-                tma_load_3d(S.tiles[s], &map, &S.bars[s], bx0 * BX, y0, z0);
-            }
-            if (more) pend = next_brick(ticket, nitems);
+            const unsigned int t0 = atomicAdd(ticket, (unsigned int)CSTAGES);
+            for (int s = 0; s < CSTAGES; ++s) stage_item(s, t0 + s < (unsigned int)nitems ? (int)(t0 + s) : -1);
+            if (t0 + CSTAGES < (unsigned int)nitems) ptk = atomicAdd(ticket, 1u);
         }
     }
     __syncthreads();
     for (int i = 0;; ++i) {
         const int s = TMA ? i % CSTAGES : 0;
         if (!TMA) {
-            if (tid == 0) S.sitem[0] = next_brick(ticket, nitems);
+            if (tid == 0) stage_item(0, next_item(ticket, nitems));
             __syncthreads();
         }
-        const long long item = S.sitem[s];
-        if (item < 0) break;  // uniform: every thread reads the same entry
-        int bx0, y0, z0;
-        origin(item, bx0, y0, z0);
-        const int x0 = bx0 * BX;
+        const int4 org = S.sorg[s];
+        if (org.x < 0) break;  // uniform: every thread reads the same entry
+        const int x0 = org.x, y0 = org.y, z0 = org.z, bx0 = org.w;
         T *tile = reinterpret_cast<T *>(S.tiles[s]);
+        T *hal = XH ? nullptr : reinterpret_cast<T *>(S.halo[s]);
         if (TMA) {
             // one thread polls the barrier; the others wait at __syncthreads
             if (tid == 0 && !mbar_wait(&S.bars[s], (uint32_t)((i / CSTAGES) & 1))) S.abort = 1;
         } else {
             fill_tile<VT, Geo::TXW, CTY, CTZ>(tile, vol, nx, ny, nz, x0, y0, z0);
+            if (XH == 0 && tid < ROWS) {
+                const int gx = x0 + Geo::TXW, gy = y0 + tid % CTY, gz = z0 + tid / CTY;
+                hal[tid * H::HW] = (gx < nx && gy < ny && gz < nz) ? vol[lin3(nx, ny, gx, gy, gz)] : V::fill();
+            }
         }
         __syncthreads();
         if (S.abort) break;
-        const bool mixed = tile_mixed<VT, Geo::TILE>(S, tile);
+        const bool mixed = item_mixed<VT, G, XH, NT>(S, tile, hal, nx, ny, nz, x0, y0, z0);
         if (mixed) {
-            // row masks: 33 bits of row r starting at voxel x0 + 32 h (16-byte aligned)
-            for (int m = tid; m < G * ROWS; m += CLS_THREADS) {
+            // row masks: 33 bits of row r starting at voxel x0 + 32 h; the 33rd
+            // voxel of the last brick's rows is the halo column's
+            const bool has_halo = x0 + Geo::TXW < nx;
+            for (int m = tid; m < G * ROWS; m += NT) {
                 const int h = m / ROWS, r = m - h * ROWS;
-                RowMask<VT>::build(tile + r * Geo::TXW + h * BX, S.neg[m], S.dead[m]);
+                const T *row = tile + r * Geo::TXW + h * BX;
+                const T last = (XH || h < G - 1) ? row[BX] : (has_halo ? hal[r * H::HW] : V::fill());
+                RowMask<VT>::build(row, last, S.neg[m], S.dead[m]);
             }
             __syncthreads();
         }
         // the tile has been read for the last time: refill its stage now, so the
         // load overlaps the cube rows below
         if (TMA && tid == 0) {
-            const long long nit = pend;
-            S.sitem[s] = nit;
-            if (nit >= 0) {
-                int nbx0, ny0, nz0;
-                origin(nit, nbx0, ny0, nz0);
-                mbar_arrive_expect_tx(&S.bars[s], Geo::TILE * V::bytes);
-                tma_load_3d(S.tiles[s], &map, &S.bars[s], nbx0 * BX, ny0, nz0);
-                pend = next_brick(ticket, nitems);
-            }
+            const int it = ptk < (unsigned int)nitems ? (int)ptk : -1;
+            stage_item(s, it);
+            if (it >= 0) ptk = atomicAdd(ticket, 1u);
         }
         if (mixed) {
             if (tid < G * CUBE_ROWS) {
@@ -356,7 +442,7 @@ __global__ void __launch_bounds__(CLS_THREADS)
                     S.red[warp][1] = occ;
                 }
             }
-            __syncthreads();  // tile s consumed, red[] complete
+            __syncthreads();  // red[] complete
         }
         if (tid < G && bx0 + tid < nbx) {
             const int h = tid;
@@ -377,7 +463,8 @@ __global__ void __launch_bounds__(CLS_THREADS)
                 if (hc >= 0) atomicAdd(c + 3 + hc, 1u);
             }
         }
-        if (!TMA) __syncthreads();  // S.sitem[0] is rewritten at the top
+        // with one stage, the entry read at the top is the one just rewritten
+        if (!TMA || CSTAGES == 1) __syncthreads();
     }
     if (S.abort && tid == 0) {
         atomicOr(flags, 1u);
@@ -392,17 +479,22 @@ __global__ void __launch_bounds__(CLS_THREADS)
 // class; a CTA adds up the chunks before its own for its base offsets, scans
 // its bricks, and writes 64-bit soup offsets and its part of the active-brick
 // list: heavy classes first (heaviest first), then the light bricks, each in
-// brick order.  CTA 0 also writes the totals.
+// brick order, with each entry's soup offset beside it (list_vofs, when
+// given).  CTA 0 also writes the totals, to `host` as well when given (a
+// mapped host copy).  The last CTA to have read the chunk sums zeroes them for
+// the next count phase.
 __global__ void __launch_bounds__(CHUNK)
-    mc_scan_kernel(const uint32_t *__restrict__ brick_tris, const uint32_t *__restrict__ chunk, long long nb,
+    mc_scan_kernel(const uint32_t *__restrict__ brick_tris, uint32_t *__restrict__ chunk, long long nb,
                    unsigned long long *__restrict__ brick_vofs, uint32_t *__restrict__ active,
-                   MeshTotals *__restrict__ totals) {
+                   unsigned long long *__restrict__ list_vofs, MeshTotals *__restrict__ totals,
+                   MeshTotals *__restrict__ host) {
     // acc: [0] base tris, [1] base active, [2, 2+NH) base heavy per class,
     // [2+NH] all tris, [3+NH] all active, [4+NH] all occupied, [5+NH, 5+2NH) all heavy
     constexpr int NH = NHEAVY, NACC = 5 + 2 * NH, NF = NH + 2;  // scanned per brick: tris, classes, light
     __shared__ unsigned long long s_part[NACC][CHUNK / 32];
     __shared__ unsigned long long s_base_v;
     __shared__ unsigned int s_base[NH + 1];  // list offset of this chunk's first brick of each class / light
+    __shared__ bool s_last;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const long long j = blockIdx.x;
     const long long nchunks = (nb + CHUNK - 1) / CHUNK;
@@ -430,8 +522,10 @@ __global__ void __launch_bounds__(CHUNK)
         for (int o = 16; o; o >>= 1) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], o);
         if (lane == 0) s_part[k][warp] = acc[k];
     }
-    __syncthreads();
+    __syncthreads();  // this CTA's reads of the chunk sums are done
     if (tid == 0) {
+        __threadfence();
+        s_last = atomicAdd(&totals->scan_done, 1u) == gridDim.x - 1;
         unsigned long long r[NACC];
         for (int k = 0; k < NACC; ++k) {
             r[k] = 0;
@@ -450,6 +544,14 @@ __global__ void __launch_bounds__(CHUNK)
             totals->triangles = r[2 + NH];
             totals->vertices = 3ull * r[2 + NH];
             totals->active_bricks = (unsigned int)r[3 + NH];
+            if (host) {
+                host->occupied = r[4 + NH];
+                host->triangles = r[2 + NH];
+                host->vertices = 3ull * r[2 + NH];
+                host->active_bricks = (unsigned int)r[3 + NH];
+                host->flags = *(volatile unsigned int *)&totals->flags;  // the count launch has finished
+                __threadfence_system();
+            }
         }
     }
     __syncthreads();
@@ -484,10 +586,19 @@ __global__ void __launch_bounds__(CHUNK)
         for (int w = 0; w < warp; ++w) wp[k] += s_w[k][w];
     }
     if (b < nb) {
-        brick_vofs[b] = 3ull * (base_v + wp[0] + x[0] - t);
+        const unsigned long long v = 3ull * (base_v + wp[0] + x[0] - t);
+        brick_vofs[b] = v;
 #pragma unroll
         for (int k = 0; k <= NH; ++k)
-            if (f[1 + k]) active[s_base[k] + wp[1 + k] + x[1 + k] - 1] = (uint32_t)b;
+            if (f[1 + k]) {
+                const unsigned int w = s_base[k] + wp[1 + k] + x[1 + k] - 1;
+                active[w] = (uint32_t)b;
+                if (list_vofs) list_vofs[w] = v;
+            }
+    }
+    if (s_last) {  // every CTA has read the chunk sums
+        for (long long i = tid; i < nchunks * CHUNK_FIELDS; i += CHUNK) chunk[i] = 0;
+        if (tid == 0) totals->scan_done = 0;
     }
 }
 
@@ -500,7 +611,9 @@ struct GenParams {
     int zbase, zlim;  // z of brick layer 0; cubes exist for z < zlim
     const uint32_t *active;
     const unsigned long long *brick_vofs;
+    const unsigned long long *list_vofs;  // soup offset of each active-list entry
     MeshTotals *totals;
+    MeshTotals *host;  // mapped host copy of the totals (flags written at exit), or null
     mcg_vertex_voxel *soup;
     float *normals;
     int32_t *vi2vox;
@@ -526,8 +639,11 @@ struct GenSmem {
     signed char tri[256][16];
     unsigned char nv[256];
     unsigned short vmap[BRICK_CUBES];      // soup vertex -> list entry, when the brick has <= 2048
-    long long sbrick[GSTAGES];             // brick id and soup offset of each stage's tile
+    long long sbrick[GSTAGES];             // brick id, soup offset and origin of each stage's tile
     unsigned long long svbase[GSTAGES];
+    int4 spos[GSTAGES];
+    unsigned long long pipe_v;  // refill pipeline (thread 0): the brick staged at the next
+    unsigned int pipe_b;        // refill and its soup offset; pipe_b ~0u = none
     unsigned int wsum[2][2];
     unsigned int nocc, total;
     int abort;
@@ -862,23 +978,48 @@ __global__ void __launch_bounds__(THREADS, 4) mc_generate_kernel(const __grid_co
         }
     }
     __syncthreads();
-    const long long nactive = p.totals->active_bricks;
+    const unsigned int nactive = p.totals->active_bricks;
     unsigned int *ticket = &p.totals->gen_ticket;
-    long long pend = -1;  // thread 0: list entry of the next refill, drawn one iteration ahead
+    // stage st <- brick b (soup offset v): thread 0 records the brick, its
+    // offset and origin for the CTA and starts the tile load
+    auto stage_brick = [&](int st, long long b, unsigned long long v) {
+        S.sbrick[st] = b;
+        if (b < 0) return;
+        S.svbase[st] = v;
+        const BrickPos bp = slab_pos(b, p.nbx, p.nby, p.zbase);
+        S.spos[st] = make_int4(bp.x0, bp.y0, bp.z0, 0);
+        mbar_arrive_expect_tx(&S.bars[st], GTILE * V::bytes);
+        tma_load_3d(S.tiles[st], &map, &S.bars[st], bp.x0 - TXO, bp.y0 - TYO, bp.z0 - TZO);
+    };
+    // The first GSTAGES + 1 bricks of each CTA are fixed: round r gives list
+    // entry r * grid + c to CTA c, c counted backwards in odd rounds, so the
+    // heaviest bricks at the head of the list spread over all CTAs with the
+    // heaviest and lightest of adjacent rounds paired.  Later bricks come from
+    // the counter, past those rounds.
+    //
+    // Thread 0's refill pipeline: the ticket for a refill is drawn at the top
+    // of the brick before, and its list entry and soup offset are copied
+    // (asynchronously, into shared memory) at that brick's end, to be staged
+    // at the end of the next brick.  Each result is used a whole brick after
+    // it was asked for, so no refill waits on the contended counter or on
+    // global memory (a wait in warp 0 would hold the whole CTA at its next
+    // barrier).
+    const unsigned int grid = gridDim.x, c = blockIdx.x;
+    const unsigned int tbase = (GSTAGES + 1) * grid;  // list entry of ticket 0
+    unsigned int ptk = 0xffffffffu;  // list entry of the ticket drawn at the top of this brick
     if (TMA && tid == 0) {
-        bool more = true;
-        for (int s = 0; s < GSTAGES; ++s) {
-            const long long w = more ? next_brick(ticket, nactive) : -1ll;
-            more = w >= 0;
-            S.sbrick[s] = more ? (long long)p.active[w] : -1ll;
-            if (!more) continue;
-            const long long b = S.sbrick[s];
-            S.svbase[s] = p.brick_vofs[b];
-            const BrickPos bp = slab_pos(b, p.nbx, p.nby, p.zbase);
-            mbar_arrive_expect_tx(&S.bars[s], GTILE * V::bytes);
-            tma_load_3d(S.tiles[s], &map, &S.bars[s], bp.x0 - TXO, bp.y0 - TYO, bp.z0 - TZO);
+#pragma unroll
+        for (int r = 0; r < GSTAGES; ++r) {
+            const unsigned int w = r * grid + ((r & 1) ? grid - 1 - c : c);
+            stage_brick(r, w < nactive ? (long long)p.active[w] : -1ll, w < nactive ? p.list_vofs[w] : 0ull);
         }
-        if (more) pend = next_brick(ticket, nactive);
+        const unsigned int w = GSTAGES * grid + ((GSTAGES & 1) ? grid - 1 - c : c);
+        S.pipe_b = 0xffffffffu;
+        if (w < nactive) {
+            cp_async_4(&S.pipe_b, p.active + w);
+            cp_async_8(&S.pipe_v, p.list_vofs + w);
+        }
+        if (tbase < nactive) ptk = 0;  // not ~0u: draw tickets at the tops of the bricks
     }
     if (TMA) __syncthreads();
     for (int it = 0;; ++it) {
@@ -886,13 +1027,22 @@ __global__ void __launch_bounds__(THREADS, 4) mc_generate_kernel(const __grid_co
         const T *tile = reinterpret_cast<const T *>(S.tiles[s]);
         long long b;
         unsigned long long vbase;
+        BrickPos bp;
         if (TMA) {
             b = S.sbrick[s];
             if (b < 0) break;  // uniform
-            if (tid == 0 && !mbar_wait(&S.bars[s], (uint32_t)((it / GSTAGES) & 1))) S.abort = 1;
+            if (tid == 0) {
+                // the ticket of the refill after the next one (used at this brick's end)
+                if (ptk != 0xffffffffu) ptk = tbase + atomicAdd(ticket, 1u);
+                if (!mbar_wait(&S.bars[s], (uint32_t)((it / GSTAGES) & 1))) S.abort = 1;
+            }
             __syncthreads();
             if (S.abort) break;
             vbase = S.svbase[s];
+            const int4 sp = S.spos[s];
+            bp.x0 = sp.x;
+            bp.y0 = sp.y;
+            bp.z0 = sp.z;
         } else {
             if (tid == 0) {
                 const long long w = next_brick(ticket, nactive);
@@ -902,12 +1052,11 @@ __global__ void __launch_bounds__(THREADS, 4) mc_generate_kernel(const __grid_co
             b = S.sbrick[0];
             if (b < 0) break;
             vbase = p.brick_vofs[b];
-            const BrickPos fp = slab_pos(b, p.nbx, p.nby, p.zbase);
-            fill_tile<VT, TX, TY, TZ>(reinterpret_cast<T *>(S.tiles[s]), vol, nx, ny, nz, fp.x0 - TXO,
-                                      fp.y0 - TYO, fp.z0 - TZO);
+            bp = slab_pos(b, p.nbx, p.nby, p.zbase);
+            fill_tile<VT, TX, TY, TZ>(reinterpret_cast<T *>(S.tiles[s]), vol, nx, ny, nz, bp.x0 - TXO,
+                                      bp.y0 - TYO, bp.z0 - TZO);
             __syncthreads();
         }
-        const BrickPos bp = slab_pos(b, p.nbx, p.nby, p.zbase);
         if (MODE == 0) {
             GenOut o;
             o.soup = p.soup;
@@ -924,15 +1073,15 @@ __global__ void __launch_bounds__(THREADS, 4) mc_generate_kernel(const __grid_co
         }
         __syncthreads();  // tile s, the list and the stage are free again
         if (TMA && tid == 0) {
-            const long long wn = pend;
-            S.sbrick[s] = wn >= 0 ? (long long)p.active[wn] : -1ll;
-            if (wn >= 0) {
-                pend = next_brick(ticket, nactive);
-                const long long nb2 = S.sbrick[s];
-                S.svbase[s] = p.brick_vofs[nb2];
-                const BrickPos np = slab_pos(nb2, p.nbx, p.nby, p.zbase);
-                mbar_arrive_expect_tx(&S.bars[s], GTILE * V::bytes);
-                tma_load_3d(S.tiles[s], &map, &S.bars[s], np.x0 - TXO, np.y0 - TYO, np.z0 - TZO);
+            cp_async_wait_all();
+            const unsigned int pb = S.pipe_b;
+            stage_brick(s, pb == 0xffffffffu ? -1ll : (long long)pb, S.pipe_v);
+            S.pipe_b = 0xffffffffu;
+            if (ptk < nactive) {
+                cp_async_4(&S.pipe_b, p.active + ptk);
+                cp_async_8(&S.pipe_v, p.list_vofs + ptk);
+            } else {
+                ptk = 0xffffffffu;  // the list is exhausted: draw no more tickets
             }
         }
         // S.sbrick[s] is next read at the top of iteration it + GSTAGES, after the
@@ -941,6 +1090,19 @@ __global__ void __launch_bounds__(THREADS, 4) mc_generate_kernel(const __grid_co
     if (S.abort && tid == 0) {
         atomicOr(&p.totals->flags, 1u);
         for (int s = 0; s < GSTAGES; ++s) mbar_wait(&S.bars[s], 0, 100000000ull);
+    }
+    // the last CTA out resets the work counter for the next launch over the
+    // same list and reports the flags to the host copy
+    if (tid == 0) {
+        __threadfence();
+        if (atomicAdd(&p.totals->gen_exit, 1u) == gridDim.x - 1) {
+            p.totals->gen_ticket = 0;
+            p.totals->gen_exit = 0;
+            if (p.host) {
+                p.host->flags = *(volatile unsigned int *)&p.totals->flags;
+                __threadfence_system();
+            }
+        }
     }
 }
 
@@ -1186,61 +1348,83 @@ struct Scratch {
     uint32_t *chunk;  // CHUNK_FIELDS per chunk of CHUNK bricks
     unsigned long long *vofs;
     uint32_t *active;
+    unsigned long long *list_vofs;  // soup offset per active-list entry
     MeshTotals *totals;
+    MeshTotals *host;  // mapped host copy of the totals, or null
 };
 
-template <int VT, bool TMA, int G, int CSTAGES>
-void launch_classify_s(const CUtensorMap &map, const mcg_volume *vol, const Geometry &g, const Scratch &sc, int sms,
-                       cudaStream_t s) {
-    const size_t smem = sizeof(ClsSmemG<VT, G, CSTAGES>);
+template <int VT, bool TMA, int G, int XH, int CSTAGES, int NT>
+void launch_classify_s(const CUtensorMap &map, const CUtensorMap &hmap, const mcg_volume *vol, const Geometry &g,
+                       const Scratch &sc, int sms, cudaStream_t s) {
+    const size_t smem = sizeof(ClsSmemG<VT, G, XH, CSTAGES, NT>);
     static int occ = 0;  // per instantiation; all devices of a run are the same part
-    if (!occ) occ = occupancy(mc_classify_kernel<VT, TMA, G, CSTAGES>, CLS_THREADS, smem);
+    if (!occ) occ = occupancy(mc_classify_kernel<VT, TMA, G, XH, CSTAGES, NT>, NT, smem);
     const int ngx = (g.nbx + G - 1) / G;
     const long long nitems = (long long)ngx * g.nby * g.nbz;
     long long grid = (long long)sms * occ;
     if (grid > nitems) grid = nitems;
-    mc_classify_kernel<VT, TMA, G, CSTAGES><<<(int)grid, CLS_THREADS, smem, s>>>(
-        map, static_cast<const typename Vox<VT>::T *>(vol->data), vol->nx, vol->ny, vol->nz, g.nbx, g.nby, nitems,
-        ngx, g.zbase, g.zlim, sc.tris, sc.chunk, &sc.totals->flags, &sc.totals->cls_ticket);
+    mc_classify_kernel<VT, TMA, G, XH, CSTAGES, NT><<<(int)grid, NT, smem, s>>>(
+        map, hmap, static_cast<const typename Vox<VT>::T *>(vol->data), vol->nx, vol->ny, vol->nz, g.nbx, g.nby,
+        (int)nitems, ngx, g.zbase, g.zlim, sc.tris, sc.chunk, &sc.totals->flags, &sc.totals->cls_ticket);
 }
 
-// pipeline depth of the classify pass (tile stages per CTA); MCG_CLS_STAGES
-// overrides it for tuning
-int classify_stages() {
-    static int st = 0;
-    if (!st) {
-        st = 2;
-        if (const char *e = getenv("MCG_CLS_STAGES")) {
+// classify configuration; MCG_CLS_CFG selects one for tuning:
+//   0: 2 bricks, in-box halo (68-voxel box), 2 stages x 256 threads
+//   1: 4 bricks, halo box, 2 stages x 256 threads
+//   2: 4 bricks, halo box, 4 stages x 512 threads
+//   3: 4 bricks, in-box halo (132-voxel box), 2 stages x 256 threads
+//   4: 4 bricks, in-box halo (132-voxel box), 1 stage x 256 threads
+//   5: 2 bricks, in-box halo (68-voxel box), 1 stage x 256 threads
+int classify_cfg() {
+    static int c = -1;
+    if (c < 0) {
+        c = 4;
+        if (const char *e = getenv("MCG_CLS_CFG")) {
             const int v = atoi(e);
-            if (v == 2 || v == 3) st = v;
+            if (v >= 0 && v <= 5) c = v;
         }
     }
-    return st;
+    return c;
 }
 
-// bricks per classify work item: 2 (a 68-voxel box; measured fastest at 512^3
-// against 1 and 4) when the volume is wide enough for that box, else 1;
-// MCG_CLS_GROUP (1, 2 or 4) overrides it for tuning
-int classify_group(int nx) {
-    static int pref = 0;
-    if (!pref) {
-        pref = 2;
-        if (const char *e = getenv("MCG_CLS_GROUP")) {
-            const int v = atoi(e);
-            if (v == 1 || v == 2 || v == 4) pref = v;
-        }
-    }
-    if (pref == 4 && nx >= ClsGeom<4>::TXW) return 4;
-    if (pref >= 2 && nx >= ClsGeom<2>::TXW) return 2;
-    return 1;
+// bricks per work item and in-box halo of the configuration, narrowed to
+// what the volume's width allows
+void classify_shape(int nx, int eb, int &G, int &XH) {
+    const int c = classify_cfg();
+    XH = (c == 1 || c == 2) ? 0 : 4;
+    const int pref = (c == 0 || c == 5) ? 2 : 512 / (BX * eb);
+    G = 1;
+    if (pref >= 4 && nx >= BX * 4 + XH) G = 4;
+    else if (pref >= 2 && nx >= BX * 2 + XH) G = 2;
 }
 
-template <int VT, bool TMA, int G>
-void launch_classify_g(const CUtensorMap &map, const mcg_volume *vol, const Geometry &g, const Scratch &sc, int sms,
-                       cudaStream_t s) {
+template <int VT, bool TMA, int G, int XH>
+void launch_classify_g(const CUtensorMap &map, const CUtensorMap &hmap, const mcg_volume *vol, const Geometry &g,
+                       const Scratch &sc, int sms, cudaStream_t s) {
     // without TMA only one stage is ever used
-    if (TMA && classify_stages() == 3) launch_classify_s<VT, TMA, G, 3>(map, vol, g, sc, sms, s);
-    else launch_classify_s<VT, TMA, G, 2>(map, vol, g, sc, sms, s);
+    if constexpr (!TMA) {
+        launch_classify_s<VT, TMA, G, XH, 1, 256>(map, hmap, vol, g, sc, sms, s);
+    } else {
+        const int c = classify_cfg();
+        if (c == 2) launch_classify_s<VT, TMA, G, XH, 4, 512>(map, hmap, vol, g, sc, sms, s);
+        else if (c >= 4) launch_classify_s<VT, TMA, G, XH, 1, 256>(map, hmap, vol, g, sc, sms, s);
+        else launch_classify_s<VT, TMA, G, XH, 2, 256>(map, hmap, vol, g, sc, sms, s);
+    }
+}
+
+template <int VT, int XH>
+void launch_classify_x(bool tma, int G, const CUtensorMap &map, const CUtensorMap &hmap, const mcg_volume *vol,
+                       const Geometry &g, const Scratch &sc, int sms, cudaStream_t s) {
+    if (G == 4) {
+        if (tma) launch_classify_g<VT, true, 4, XH>(map, hmap, vol, g, sc, sms, s);
+        else launch_classify_g<VT, false, 4, XH>(map, hmap, vol, g, sc, sms, s);
+    } else if (G == 2) {
+        if (tma) launch_classify_g<VT, true, 2, XH>(map, hmap, vol, g, sc, sms, s);
+        else launch_classify_g<VT, false, 2, XH>(map, hmap, vol, g, sc, sms, s);
+    } else {
+        if (tma) launch_classify_g<VT, true, 1, XH>(map, hmap, vol, g, sc, sms, s);
+        else launch_classify_g<VT, false, 1, XH>(map, hmap, vol, g, sc, sms, s);
+    }
 }
 
 template <int VT, bool TMA, int MODE = 0>
@@ -1257,40 +1441,32 @@ void launch_generate_t(const CUtensorMap &map, const GenParams &p, const Geometr
 long long num_chunks(long long nbricks) { return (nbricks + CHUNK - 1) / CHUNK; }
 
 cudaError_t launch_count_phase(const mcg_volume *vol, const Geometry &g, const Scratch &sc, int sms, cudaStream_t s) {
-    // flags and both work counters
+    // flags and both work counters; the chunk sums are zero already (the
+    // previous scan cleared them)
     cudaError_t e = cudaMemsetAsync(&sc.totals->flags, 0, 3 * sizeof(unsigned int), s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(sc.chunk, 0, sizeof(uint32_t) * CHUNK_FIELDS * num_chunks(g.nbricks), s);
     if (e != cudaSuccess) return e;
-    CUtensorMap map;
+    CUtensorMap map, hmap;
     const int eb = vol->voxel_type == MCG_VOXEL_SHORT2 ? 4 : 8;
-    const int G = classify_group(vol->nx);
-    const bool tma = encode_volume_map(&map, vol->data, vol->nx, vol->ny, vol->nz, eb, G * BX + 4, CTY, CTZ);
-    if (!tma) memset(&map, 0, sizeof(map));
-    if (vol->voxel_type == MCG_VOXEL_SHORT2) {
-        if (G == 4) {
-            if (tma) launch_classify_g<MCG_VOXEL_SHORT2, true, 4>(map, vol, g, sc, sms, s);
-            else launch_classify_g<MCG_VOXEL_SHORT2, false, 4>(map, vol, g, sc, sms, s);
-        } else if (G == 2) {
-            if (tma) launch_classify_g<MCG_VOXEL_SHORT2, true, 2>(map, vol, g, sc, sms, s);
-            else launch_classify_g<MCG_VOXEL_SHORT2, false, 2>(map, vol, g, sc, sms, s);
-        } else {
-            if (tma) launch_classify_g<MCG_VOXEL_SHORT2, true, 1>(map, vol, g, sc, sms, s);
-            else launch_classify_g<MCG_VOXEL_SHORT2, false, 1>(map, vol, g, sc, sms, s);
-        }
+    int G, XH;
+    classify_shape(vol->nx, eb, G, XH);
+    if ((long long)((g.nbx + G - 1) / G) * g.nby * g.nbz > 0x7fffffffll) return cudaErrorInvalidValue;
+    bool tma = encode_volume_map(&map, vol->data, vol->nx, vol->ny, vol->nz, eb, G * BX + XH, CTY, CTZ);
+    if (tma && XH == 0) tma = encode_volume_map(&hmap, vol->data, vol->nx, vol->ny, vol->nz, eb, 16 / eb, CTY, CTZ);
+    else memset(&hmap, 0, sizeof(hmap));
+    if (!tma) {
+        memset(&map, 0, sizeof(map));
+        memset(&hmap, 0, sizeof(hmap));
+    }
+    const bool s2 = vol->voxel_type == MCG_VOXEL_SHORT2;
+    if (XH) {
+        if (s2) launch_classify_x<MCG_VOXEL_SHORT2, 4>(tma, G, map, hmap, vol, g, sc, sms, s);
+        else launch_classify_x<MCG_VOXEL_FLOAT2, 4>(tma, G, map, hmap, vol, g, sc, sms, s);
     } else {
-        if (G == 4) {
-            if (tma) launch_classify_g<MCG_VOXEL_FLOAT2, true, 4>(map, vol, g, sc, sms, s);
-            else launch_classify_g<MCG_VOXEL_FLOAT2, false, 4>(map, vol, g, sc, sms, s);
-        } else if (G == 2) {
-            if (tma) launch_classify_g<MCG_VOXEL_FLOAT2, true, 2>(map, vol, g, sc, sms, s);
-            else launch_classify_g<MCG_VOXEL_FLOAT2, false, 2>(map, vol, g, sc, sms, s);
-        } else {
-            if (tma) launch_classify_g<MCG_VOXEL_FLOAT2, true, 1>(map, vol, g, sc, sms, s);
-            else launch_classify_g<MCG_VOXEL_FLOAT2, false, 1>(map, vol, g, sc, sms, s);
-        }
+        if (s2) launch_classify_x<MCG_VOXEL_SHORT2, 0>(tma, G, map, hmap, vol, g, sc, sms, s);
+        else launch_classify_x<MCG_VOXEL_FLOAT2, 0>(tma, G, map, hmap, vol, g, sc, sms, s);
     }
     mc_scan_kernel<<<(unsigned int)num_chunks(g.nbricks), CHUNK, 0, s>>>(sc.tris, sc.chunk, g.nbricks, sc.vofs,
-                                                                        sc.active, sc.totals);
+                                                                        sc.active, sc.list_vofs, sc.totals, sc.host);
     return cudaGetLastError();
 }
 
@@ -1300,10 +1476,7 @@ cudaError_t launch_generate_phase(const mcg_volume *vol, const Geometry &g, cons
         cudaError_t e = cudaMemsetAsync(out->ver_voxel, 0, sizeof(int16_t) * (size_t)vol->nx * vol->ny * vol->nz, s);
         if (e != cudaSuccess) return e;
     }
-    {
-        const cudaError_t e = cudaMemsetAsync(&sc.totals->gen_ticket, 0, sizeof(unsigned int), s);
-        if (e != cudaSuccess) return e;
-    }
+    // gen_ticket is zero: cleared by the count phase and by every generate launch at its end
     GenParams p;
     p.vol = vol->data;
     p.nx = vol->nx;
@@ -1316,6 +1489,8 @@ cudaError_t launch_generate_phase(const mcg_volume *vol, const Geometry &g, cons
     p.zlim = g.zlim;
     p.active = sc.active;
     p.brick_vofs = sc.vofs;
+    p.list_vofs = sc.list_vofs;
+    p.host = sc.host;
     p.totals = sc.totals;
     p.soup = out->soup;
     p.normals = out->soup_normals;
@@ -1341,7 +1516,8 @@ cudaError_t launch_generate_phase(const mcg_volume *vol, const Geometry &g, cons
 }
 
 Scratch ctx_scratch(mcg_context *ctx) {
-    return Scratch{ctx->brick_tris, ctx->brick_occ, ctx->brick_vofs, ctx->active, ctx->d_totals};
+    return Scratch{ctx->brick_tris, ctx->brick_occ, ctx->brick_vofs, ctx->active, ctx->list_vofs, ctx->d_totals,
+                   ctx->h_totals_dev};
 }
 
 }  // namespace
@@ -1360,10 +1536,17 @@ static mcg_status classify_impl(mcg_context *ctx, const mcg_volume *vol, int32_t
     if (!ensure(&ctx->brick_tris, &ctx->brick_tris_cap, (size_t)g.nbricks) ||
         !ensure(&ctx->brick_occ, &ctx->brick_occ_cap, (size_t)(CHUNK_FIELDS * num_chunks(g.nbricks))) ||
         !ensure(&ctx->brick_vofs, &ctx->brick_vofs_cap, (size_t)g.nbricks) ||
-        !ensure(&ctx->active, &ctx->active_cap, (size_t)g.nbricks))
+        !ensure(&ctx->active, &ctx->active_cap, (size_t)g.nbricks) ||
+        !ensure(&ctx->list_vofs, &ctx->list_vofs_cap, (size_t)g.nbricks))
         return mcg_cuda_fail(ctx, cudaErrorMemoryAllocation);
+    // chunk sums: zeroed once per allocation, then by each scan after use
+    if (ctx->chunk_clean_cap != ctx->brick_occ_cap) {
+        e = cudaMemsetAsync(ctx->brick_occ, 0, sizeof(uint32_t) * ctx->brick_occ_cap, s);
+        if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
+        ctx->chunk_clean_cap = ctx->brick_occ_cap;
+    }
     e = launch_count_phase(vol, g, ctx_scratch(ctx), ctx->num_sms, s);
-    if (e == cudaSuccess)
+    if (e == cudaSuccess && !ctx->h_totals_dev)
         e = cudaMemcpyAsync(ctx->h_totals, ctx->d_totals, sizeof(MeshTotals), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = mcg_counts_event(ctx, s);
     if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
@@ -1432,8 +1615,9 @@ mcg_status mcg_mc_generate(mcg_context *ctx, const mcg_volume *vol, const mcg_me
     if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
     const Geometry g = geometry_slab(vol->nx, vol->ny, ctx->cls_z0, ctx->cls_z1);
     e = launch_generate_phase(vol, g, ctx_scratch(ctx), out, ctx->num_sms, s);
-    // the totals are re-read so a timeout flagged by generate is reported
-    if (e == cudaSuccess)
+    // the totals are re-read so a timeout flagged by generate is reported (the
+    // launch writes the flags to the mapped host copy itself)
+    if (e == cudaSuccess && !ctx->h_totals_dev)
         e = cudaMemcpyAsync(ctx->h_totals, ctx->d_totals, sizeof(MeshTotals), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = mcg_counts_event(ctx, s);
     if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
@@ -1502,6 +1686,7 @@ mcg_status mcg_mc_backward(mcg_context *ctx, const mcg_volume *vol, const float 
     p.zlim = g.zlim;
     p.active = ctx->active;
     p.brick_vofs = ctx->brick_vofs;
+    p.list_vofs = ctx->list_vofs;
     p.totals = ctx->d_totals;
     p.grad_pos = grad_pos;
     p.grad_f = grad_f;
@@ -1675,7 +1860,8 @@ mcg_status mcg_mc_classify_batched(mcg_context *ctx, const mcg_volume *vols, int
     if (vols[0].voxel_type == MCG_VOXEL_SHORT2) launch_classify_multi<MCG_VOXEL_SHORT2>(ctx, nvol, nbricks, s);
     else launch_classify_multi<MCG_VOXEL_FLOAT2>(ctx, nvol, nbricks, s);
     mc_scan_kernel<<<(unsigned int)num_chunks(nbricks), CHUNK, 0, s>>>(ctx->brick_tris, ctx->brick_occ, nbricks,
-                                                                      ctx->brick_vofs, ctx->active, ctx->d_totals);
+                                                                      ctx->brick_vofs, ctx->active, nullptr,
+                                                                      ctx->d_totals, nullptr);
     e = cudaGetLastError();
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(ctx->h_totals, ctx->d_totals, sizeof(MeshTotals), cudaMemcpyDeviceToHost, s);
@@ -1775,9 +1961,11 @@ constexpr size_t kNoAllocOccOff = kNoAllocTrisOff + sizeof(uint32_t) * kNoAllocB
 static_assert(CHUNK_FIELDS * ((kNoAllocBricks + CHUNK - 1) / CHUNK) <= kNoAllocBricks, "chunk sums fit their region");
 constexpr size_t kNoAllocVofsOff = kNoAllocOccOff + sizeof(uint32_t) * kNoAllocBricks;
 constexpr size_t kNoAllocActiveOff = kNoAllocVofsOff + sizeof(unsigned long long) * kNoAllocBricks;
-constexpr size_t kNoAllocTotalsOff = kNoAllocActiveOff + sizeof(uint32_t) * kNoAllocBricks;
+constexpr size_t kNoAllocListVofsOff = kNoAllocActiveOff + sizeof(uint32_t) * kNoAllocBricks;
+constexpr size_t kNoAllocTotalsOff = kNoAllocListVofsOff + sizeof(unsigned long long) * kNoAllocBricks;
 constexpr size_t kNoAllocBytes = kNoAllocTotalsOff + 256;
-static_assert(kNoAllocVofsOff % 8 == 0 && kNoAllocTotalsOff % 8 == 0, "scratch alignment");
+static_assert(kNoAllocVofsOff % 8 == 0 && kNoAllocListVofsOff % 8 == 0 && kNoAllocTotalsOff % 8 == 0,
+              "scratch alignment");
 static_assert(kNoAllocBytes == MCG_NOALLOC_SCRATCH_BYTES, "scratch size stated in mcg.h");
 
 // brick counts, soup offsets, active-brick list and totals of one call
@@ -1814,6 +2002,8 @@ extern "C" mcg_status mcg_mc_extract_noalloc(const mcg_volume *vol, const mcg_me
     sc.chunk = reinterpret_cast<uint32_t *>(base + kNoAllocOccOff);  // CHUNK_FIELDS * 256 chunk sums at most
     sc.vofs = reinterpret_cast<unsigned long long *>(base + kNoAllocVofsOff);
     sc.active = reinterpret_cast<uint32_t *>(base + kNoAllocActiveOff);
+    sc.list_vofs = reinterpret_cast<unsigned long long *>(base + kNoAllocListVofsOff);
+    sc.host = nullptr;
     sc.totals = reinterpret_cast<MeshTotals *>(base + kNoAllocTotalsOff);
     int sms = 0;
     e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);

@@ -20,8 +20,10 @@ struct MeshTotals {
     unsigned int active_bricks;
     unsigned int flags;       // bit 0: a bounded device wait expired (set by the kernels, cleared by the host)
     unsigned int cls_ticket;  // work counters of the count, generate and (indexed) triangle launches,
-    unsigned int gen_ticket;  // zeroed before each
+    unsigned int gen_ticket;  // zeroed before each (the generate launch also zeroes its own at exit)
     unsigned int idx_ticket;
+    unsigned int scan_done;   // finished CTAs of the scan / generate launch (the last one resets it)
+    unsigned int gen_exit;
 };
 static_assert(sizeof(MeshTotals) <= 256, "MeshTotals fits the totals region of the fixed scratch");
 
@@ -54,6 +56,8 @@ struct mcg_context {
     size_t brick_vofs_cap = 0;
     uint32_t *active = nullptr;
     size_t active_cap = 0;
+    unsigned long long *list_vofs = nullptr;  // soup offset per active-list entry
+    size_t list_vofs_cap = 0;
     // indexed extraction: owned vertices and their offsets per brick, and
     // the vertex id of every grid edge (3 per voxel, written sparsely)
     uint32_t *brick_uniq = nullptr;
@@ -63,7 +67,9 @@ struct mcg_context {
     uint32_t *edge_map = nullptr;
     size_t edge_map_cap = 0;
     mcg::MeshTotals *d_totals = nullptr;
-    mcg::MeshTotals *h_totals = nullptr;  // pinned
+    mcg::MeshTotals *h_totals = nullptr;  // pinned, mapped
+    mcg::MeshTotals *h_totals_dev = nullptr;  // device address of h_totals; null if it has none
+    size_t chunk_clean_cap = 0;  // brick_occ entries known to be zero (the scan re-zeroes what it used)
     cudaEvent_t counts_ready = nullptr;
     bool counts_pending = false;
 

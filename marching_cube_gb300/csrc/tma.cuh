@@ -63,6 +63,16 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity,
     return true;
 }
 
+// Asynchronous 4- / 8-byte copies from global to shared memory (cp.async,
+// completion by cp_async_wait_all in the issuing thread).
+__device__ __forceinline__ void cp_async_4(void *dst, const void *src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_8(void *dst, const void *src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 // 3-D tiled bulk tensor load of the box at element coordinates (x, y, z)
 // into shared memory; completion is signalled on bar (complete_tx).  The
 // caller guarantees x * element size is a multiple of 16 bytes.
