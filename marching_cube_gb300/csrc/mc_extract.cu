@@ -46,6 +46,8 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <utility>
+
 #include "mc_common.cuh"
 
 namespace mcg {
@@ -338,6 +340,10 @@ __global__ void __launch_bounds__(NT)
     ClsSmemG<VT, G, XH, CSTAGES, NT> &S = *reinterpret_cast<ClsSmemG<VT, G, XH, CSTAGES, NT> *>(smem_raw);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     for (int c = tid; c < 256; c += NT) S.ntri[c] = (c == 0 || c == 255) ? 0 : c_nverts[c] / 3;
+    // everything above touches only shared and constant memory: the launch may
+    // overlap the kernel before it, whose writes (the volume, the counters) are
+    // waited for here
+    pdl_wait();
     // stage st's item (drawn by thread 0, which alone divides): origin into
     // S.sorg[st] and, with TMA, its loads -- the halo box only when column
     // x0 + TXW is inside the volume (its voxel is used by no cube otherwise)
@@ -466,6 +472,7 @@ __global__ void __launch_bounds__(NT)
         // with one stage, the entry read at the top is the one just rewritten
         if (!TMA || CSTAGES == 1) __syncthreads();
     }
+    pdl_trigger();  // no more work: the scan may start its launch
     if (S.abort && tid == 0) {
         atomicOr(flags, 1u);
         // give loads still in flight a bounded chance to land before exit
@@ -498,6 +505,8 @@ __global__ void __launch_bounds__(CHUNK)
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const long long j = blockIdx.x;
     const long long nchunks = (nb + CHUNK - 1) / CHUNK;
+    pdl_wait();     // the count launch's sums and counts
+    pdl_trigger();  // the generate launch may start its prologue
     unsigned long long acc[NACC];
 #pragma unroll
     for (int k = 0; k < NACC; ++k) acc[k] = 0;
@@ -978,6 +987,7 @@ __global__ void __launch_bounds__(THREADS, 4) mc_generate_kernel(const __grid_co
         }
     }
     __syncthreads();
+    pdl_wait();  // the scan's list, offsets and totals
     const unsigned int nactive = p.totals->active_bricks;
     unsigned int *ticket = &p.totals->gen_ticket;
     // stage st <- brick b (soup offset v): thread 0 records the brick, its
@@ -1353,6 +1363,24 @@ struct Scratch {
     MeshTotals *host;  // mapped host copy of the totals, or null
 };
 
+// Launch with programmatic stream serialisation: the kernel may start while
+// the kernel before it on the stream drains (it waits with pdl_wait).
+template <class... P, class... A>
+cudaError_t launch_pdl(void (*kernel)(P...), unsigned int grid, unsigned int block, size_t smem, cudaStream_t s,
+                       A &&...args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, std::forward<A>(args)...);
+}
+
 template <int VT, bool TMA, int G, int XH, int CSTAGES, int NT>
 void launch_classify_s(const CUtensorMap &map, const CUtensorMap &hmap, const mcg_volume *vol, const Geometry &g,
                        const Scratch &sc, int sms, cudaStream_t s) {
@@ -1363,9 +1391,9 @@ void launch_classify_s(const CUtensorMap &map, const CUtensorMap &hmap, const mc
     const long long nitems = (long long)ngx * g.nby * g.nbz;
     long long grid = (long long)sms * occ;
     if (grid > nitems) grid = nitems;
-    mc_classify_kernel<VT, TMA, G, XH, CSTAGES, NT><<<(int)grid, NT, smem, s>>>(
-        map, hmap, static_cast<const typename Vox<VT>::T *>(vol->data), vol->nx, vol->ny, vol->nz, g.nbx, g.nby,
-        (int)nitems, ngx, g.zbase, g.zlim, sc.tris, sc.chunk, &sc.totals->flags, &sc.totals->cls_ticket);
+    launch_pdl(mc_classify_kernel<VT, TMA, G, XH, CSTAGES, NT>, (unsigned int)grid, NT, smem, s, map, hmap,
+               static_cast<const typename Vox<VT>::T *>(vol->data), vol->nx, vol->ny, vol->nz, g.nbx, g.nby,
+               (int)nitems, ngx, g.zbase, g.zlim, sc.tris, sc.chunk, &sc.totals->flags, &sc.totals->cls_ticket);
 }
 
 // classify configuration; MCG_CLS_CFG selects one for tuning:
@@ -1434,7 +1462,9 @@ void launch_generate_t(const CUtensorMap &map, const GenParams &p, const Geometr
     if (!occ) occ = occupancy(mc_generate_kernel<VT, TMA, MODE>, THREADS, smem);
     long long grid = (long long)sms * occ;
     if (grid > g.nbricks) grid = g.nbricks;
-    mc_generate_kernel<VT, TMA, MODE><<<(int)grid, THREADS, smem, s>>>(map, p);
+    // MODE 0 follows the scan directly; other launches follow a memset
+    if (MODE == 0) launch_pdl(mc_generate_kernel<VT, TMA, MODE>, (unsigned int)grid, THREADS, smem, s, map, p);
+    else mc_generate_kernel<VT, TMA, MODE><<<(int)grid, THREADS, smem, s>>>(map, p);
 }
 
 // classify + scan into sc; clears the timeout flag first
@@ -1465,8 +1495,8 @@ cudaError_t launch_count_phase(const mcg_volume *vol, const Geometry &g, const S
         if (s2) launch_classify_x<MCG_VOXEL_SHORT2, 0>(tma, G, map, hmap, vol, g, sc, sms, s);
         else launch_classify_x<MCG_VOXEL_FLOAT2, 0>(tma, G, map, hmap, vol, g, sc, sms, s);
     }
-    mc_scan_kernel<<<(unsigned int)num_chunks(g.nbricks), CHUNK, 0, s>>>(sc.tris, sc.chunk, g.nbricks, sc.vofs,
-                                                                        sc.active, sc.list_vofs, sc.totals, sc.host);
+    launch_pdl(mc_scan_kernel, (unsigned int)num_chunks(g.nbricks), CHUNK, 0, s, (const uint32_t *)sc.tris, sc.chunk,
+               (long long)g.nbricks, sc.vofs, sc.active, sc.list_vofs, sc.totals, sc.host);
     return cudaGetLastError();
 }
 

@@ -73,6 +73,14 @@ __device__ __forceinline__ void cp_async_8(void *dst, const void *src) {
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
+// Programmatic dependent launch: a kernel launched with programmatic stream
+// serialisation may start while the kernel before it drains; pdl_wait blocks
+// until that kernel has completed and its writes are visible (a no-op for a
+// kernel launched without the attribute), pdl_trigger lets the next such
+// kernel start once every CTA of this one has triggered or exited.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 // 3-D tiled bulk tensor load of the box at element coordinates (x, y, z)
 // into shared memory; completion is signalled on bar (complete_tx).  The
 // caller guarantees x * element size is a multiple of 16 bytes.
