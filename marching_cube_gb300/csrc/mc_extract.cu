@@ -645,9 +645,9 @@ struct GenSmem {
     unsigned short occ_cube[BRICK_CUBES];  // local cube index (z*8 + y)*32 + x, in that order
     unsigned short occ_off[BRICK_CUBES];   // exclusive soup-vertex offset inside the brick
     unsigned char occ_ci[BRICK_CUBES];
-    signed char tri[256][16];
+    alignas(16) signed char tri[256][16];  // read a row at a time as 16 bytes
     unsigned char nv[256];
-    unsigned short vmap[BRICK_CUBES];      // soup vertex -> list entry, when the brick has <= 2048
+    unsigned short vmap[BRICK_CUBES];      // soup vertex -> local cube << 4 | edge, when the brick has <= 2048
     long long sbrick[GSTAGES];             // brick id, soup offset and origin of each stage's tile
     unsigned long long svbase[GSTAGES];
     int4 spos[GSTAGES];
@@ -676,7 +676,8 @@ struct GenOut {
 // Called by every thread of the CTA (contains __syncthreads).
 // Occupied-cube list of a brick whose tile is in shared memory: S.occ_cube /
 // occ_ci / occ_off in (z, y, x) order, S.nocc entries, S.total soup
-// vertices, and S.vmap when the brick has at most 2048 of them.  Called by
+// vertices, and S.vmap (each vertex's cube and edge) when the brick has at
+// most 2048 of them.  Called by
 // every thread (contains __syncthreads); the list is valid after return.
 template <int VT>
 __device__ __forceinline__ void occupied_list(GenSmem<VT> &S, const typename Vox<VT>::T *tile, int nx, int ny, int zlim,
@@ -734,13 +735,23 @@ __device__ __forceinline__ void occupied_list(GenSmem<VT> &S, const typename Vox
             }
         }
         __syncthreads();
-        // vertex -> occupied cube map, one occupied cube per thread (a row
-        // per thread would serialise up to 32 x 15 writes)
+        // vertex -> (cube, edge) map, one occupied cube per thread (a row per
+        // thread would serialise up to 32 x 15 writes): entry = local cube
+        // index << 4 | edge, the edge of output slot k of triangle j being
+        // tri[3j + 2 - k] (cu_marching_cubes_v1.cu:322-333); cube offsets are
+        // multiples of 3, so a vertex's slot is its index mod 3
         if (S.total <= BRICK_CUBES) {
             const unsigned int nocc = S.nocc;
             for (unsigned int i = tid; i < nocc; i += THREADS) {
-                const unsigned int off = S.occ_off[i], nvc = S.nv[S.occ_ci[i]];
-                for (unsigned int q = 0; q < nvc; ++q) S.vmap[off + q] = (unsigned short)i;
+                const unsigned int off = S.occ_off[i], ci = S.occ_ci[i], nvc = S.nv[ci];
+                const unsigned int cbits = (unsigned int)S.occ_cube[i] << 4;
+                const uint4 row = *reinterpret_cast<const uint4 *>(S.tri[ci]);
+                for (unsigned int q = 0; q < nvc; ++q) {
+                    const unsigned int j = q / 3, k = q - 3 * j, slot = 3 * j + 2 - k;
+                    const unsigned int word = slot < 4 ? row.x : slot < 8 ? row.y : slot < 12 ? row.z : row.w;
+                    const unsigned int e = (word >> (8 * (slot & 3))) & 0xffu;
+                    S.vmap[off + q] = (unsigned short)(cbits | e);
+                }
             }
             __syncthreads();
         }
@@ -771,28 +782,31 @@ __device__ __forceinline__ void generate_brick(GenSmem<VT> &S, const typename Vo
             long long cube_lin = 0;
             int kslot = 1;
             if (valid) {
-                // owning cube: the map, or the last list entry with off <= v
-                int lo = 0;
+                // owning cube and edge: the map, or the last list entry with off <= v
+                int c, e;
                 if (use_map) {
-                    lo = S.vmap[v];
+                    const unsigned int w = S.vmap[v];
+                    c = (int)(w >> 4);
+                    e = (int)(w & 15u);
+                    kslot = (int)(v % 3u);
                 } else {
-                    int hi = (int)nocc - 1;
+                    int lo = 0, hi = (int)nocc - 1;
                     while (lo < hi) {
                         const int mid = (lo + hi + 1) >> 1;
                         if (S.occ_off[mid] <= v) lo = mid; else hi = mid - 1;
                     }
+                    c = S.occ_cube[lo];
+                    const unsigned int ci = S.occ_ci[lo];
+                    const unsigned int sl = v - S.occ_off[lo];
+                    const unsigned int j = sl / 3, k = sl - 3 * j;
+                    kslot = (int)k;
+                    // output slot k of triangle j takes edge tri[3j+2-k] (:322-333)
+                    e = S.tri[ci][3 * j + 2 - k];
                 }
-                const int c = S.occ_cube[lo];
                 const int lcx = c & (BX - 1), lcy = (c / BX) & (BY - 1), lcz = c / (BX * BY);
-                const unsigned int ci = S.occ_ci[lo];
-                const unsigned int sl = v - S.occ_off[lo];
-                const unsigned int j = sl / 3, k = sl - 3 * j;
-                kslot = (int)k;
-                // output slot k of triangle j takes edge tri[3j+2-k] (:322-333)
-                const int e = S.tri[ci][3 * j + 2 - k];
                 const int a = c_ea(e), bb = c_eb(e);
                 const int gx = x0 + lcx, gy = y0 + lcy, gz = z0 + lcz;
-                cube_lin = lin3(nx, ny, gx, gy, gz);
+                if (o.tri_cube) cube_lin = lin3(nx, ny, gx, gy, gz);
                 const float f0 =
                     V::f(tile[tidx(lcx + TXO + c_cx(a), lcy + TYO + c_cy(a), lcz + TZO + c_cz(a))]);
                 const float f1 =
@@ -819,18 +833,21 @@ __device__ __forceinline__ void generate_brick(GenSmem<VT> &S, const typename Vo
                     vox[d] = (int)floorf(pf[d] - 0.5f);
                     inside &= vox[d] >= 0 && vox[d] < dims[d] && vox[d] - org[d] >= 0 && vox[d] - org[d] < tdim[d];
                 }
-                const long long li = lin3(nx, ny, vox[0], vox[1], vox[2]);
                 if (inside) {
                     const T vv = tile[tidx(vox[0] - org[0], vox[1] - org[1], vox[2] - org[2])];
                     vt = V::tsdf(vv);
                     vw = V::wt(vv);
-                } else if (li >= 0 && li < N) {
-                    const T vv = vol[li];
-                    vt = V::tsdf(vv);
-                    vw = V::wt(vv);
                 }
-                if (o.ver_voxel && li >= 0 && li < N && vbase + v < (unsigned long long)o.cap)
-                    o.ver_voxel[li] = vt;
+                if (!inside || o.ver_voxel) {
+                    const long long li = lin3(nx, ny, vox[0], vox[1], vox[2]);
+                    if (!inside && li >= 0 && li < N) {
+                        const T vv = vol[li];
+                        vt = V::tsdf(vv);
+                        vw = V::wt(vv);
+                    }
+                    if (o.ver_voxel && li >= 0 && li < N && vbase + v < (unsigned long long)o.cap)
+                        o.ver_voxel[li] = vt;
+                }
                 if (o.normals) {
                     const float fx = pf[0], fy = pf[1], fz = pf[2];
                     const int ix = (int)fx, iy = (int)fy, iz = (int)fz;
@@ -930,22 +947,24 @@ __device__ __forceinline__ void backward_brick(GenSmem<VT> &S, const typename Vo
     for (unsigned int v = tid; v < T_brick; v += THREADS) {
         const unsigned long long gv = vbase + v;
         if ((long long)gv >= n_grad) break;
-        int lo = 0;
+        int c, e;
         if (use_map) {
-            lo = S.vmap[v];
+            const unsigned int w = S.vmap[v];
+            c = (int)(w >> 4);
+            e = (int)(w & 15u);
         } else {
-            int hi = (int)nocc - 1;
+            int lo = 0, hi = (int)nocc - 1;
             while (lo < hi) {
                 const int mid = (lo + hi + 1) >> 1;
                 if (S.occ_off[mid] <= v) lo = mid; else hi = mid - 1;
             }
+            c = S.occ_cube[lo];
+            const unsigned int ci = S.occ_ci[lo];
+            const unsigned int sl = v - S.occ_off[lo];
+            const unsigned int j = sl / 3, k = sl - 3 * j;
+            e = S.tri[ci][3 * j + 2 - k];
         }
-        const int c = S.occ_cube[lo];
         const int lcx = c & (BX - 1), lcy = (c / BX) & (BY - 1), lcz = c / (BX * BY);
-        const unsigned int ci = S.occ_ci[lo];
-        const unsigned int sl = v - S.occ_off[lo];
-        const unsigned int j = sl / 3, k = sl - 3 * j;
-        const int e = S.tri[ci][3 * j + 2 - k];
         const int a = c_ea(e), bb = c_eb(e);
         const float f0 = V::f(tile[tidx(lcx + TXO + c_cx(a), lcy + TYO + c_cy(a), lcz + TZO + c_cz(a))]);
         const float f1 = V::f(tile[tidx(lcx + TXO + c_cx(bb), lcy + TYO + c_cy(bb), lcz + TZO + c_cz(bb))]);
