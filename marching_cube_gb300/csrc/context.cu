@@ -53,7 +53,8 @@ mcg_status mcg_create(mcg_context **out, int device) {
         ctx->h_totals_dev = nullptr;
     }
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->counts_ready, cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->btab_copied, cudaEventDisableTiming);
+    for (int k = 0; k < 2 && e == cudaSuccess; ++k)
+        e = cudaEventCreateWithFlags(&ctx->btab_copied[k], cudaEventDisableTiming);
     if (e != cudaSuccess) {
         cudaGetLastError();
         mcg_destroy(ctx);
@@ -73,16 +74,21 @@ mcg_status mcg_destroy(mcg_context *ctx) {
     cudaFree(ctx->brick_vofs);
     cudaFree(ctx->active);
     cudaFree(ctx->list_vofs);
+    cudaFree(ctx->batch_list);
     cudaFree(ctx->brick_uniq);
     cudaFree(ctx->brick_uofs);
     cudaFree(ctx->edge_map);
     cudaFree(ctx->d_totals);
     if (ctx->h_totals) cudaFreeHost(ctx->h_totals);
     if (ctx->counts_ready) cudaEventDestroy(ctx->counts_ready);
-    if (ctx->btab_copied) cudaEventSynchronize(ctx->btab_copied);
+    for (int k = 0; k < 2; ++k)
+        if (ctx->btab_copied[k]) cudaEventSynchronize(ctx->btab_copied[k]);
     cudaFree(ctx->d_btab);
-    if (ctx->h_btab) cudaFreeHost(ctx->h_btab);
-    if (ctx->btab_copied) cudaEventDestroy(ctx->btab_copied);
+    for (int k = 0; k < 2; ++k) {
+        if (ctx->h_btab[k]) cudaFreeHost(ctx->h_btab[k]);
+        if (ctx->btab_copied[k]) cudaEventDestroy(ctx->btab_copied[k]);
+    }
+    free(ctx->batch_tma);
     cudaFree(ctx->d_vol_sums);
     if (ctx->h_vol_sums) cudaFreeHost(ctx->h_vol_sums);
     delete[] ctx->batch_caps;

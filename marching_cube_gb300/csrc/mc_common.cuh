@@ -107,18 +107,30 @@ __device__ __forceinline__ BrickPos slab_pos(long long b, int nbx, int nby, int 
     return p;
 }
 
-// Plain-load fill of a (DX, DY, DZ) tile whose origin is (ox, oy, oz);
-// outside the volume reads as the zero voxel, like the TMA fill.
+// Fill of a (DX, DY, DZ) tile whose origin is (ox, oy, oz) for volumes TMA
+// cannot describe: one asynchronous copy per voxel (cp.async, so all of a
+// thread's loads are in flight at once), zero-filled outside the volume like
+// the TMA fill.  Each thread waits for its own copies; the caller's barrier
+// then publishes the tile.
 template <int VT, int DX, int DY, int DZ>
 __device__ __forceinline__ void fill_tile(typename Vox<VT>::T *tile, const typename Vox<VT>::T *__restrict__ vol,
                                           int nx, int ny, int nz, int ox, int oy, int oz) {
+    constexpr int B = Vox<VT>::bytes;
     for (int i = threadIdx.x; i < DX * DY * DZ; i += blockDim.x) {
         const int lx = i % DX, t = i / DX, ly = t % DY, lz = t / DY;
         const int gx = ox + lx, gy = oy + ly, gz = oz + lz;
-        typename Vox<VT>::T v = Vox<VT>::fill();
-        if (gx >= 0 && gy >= 0 && gz >= 0 && gx < nx && gy < ny && gz < nz) v = vol[lin3(nx, ny, gx, gy, gz)];
-        tile[i] = v;
+        const bool in = gx >= 0 && gy >= 0 && gz >= 0 && gx < nx && gy < ny && gz < nz;
+        // outside: no byte is read (source size 0) and the voxel is zero
+        const typename Vox<VT>::T *src = in ? vol + lin3(nx, ny, gx, gy, gz) : vol;
+        const unsigned int n = in ? B : 0;
+        if (B == 4)
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(smem_u32(tile + i)), "l"(src), "r"(n)
+                         : "memory");
+        else
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(smem_u32(tile + i)), "l"(src), "r"(n)
+                         : "memory");
     }
+    cp_async_wait_all();
 }
 
 // ---- normals (cu_kinect_fusion_v1.cu:3146-3225) -----------------------------------

@@ -1180,17 +1180,36 @@ struct ClsSmemMulti {
     unsigned char ntri[256];
     int svol[2];
     int stma[2];
+    int4 spos[2];  // origin of each stage's brick
     int abort;
 };
 
+// volume of the bricks [base, end) that thread 0 resolved last: a CTA's
+// bricks are a fixed stride apart, so most lie in the same volume as the one
+// before and skip the search
+struct VolCache {
+    int v = -1;
+    long long base = 0, end = 0;
+};
+
+__device__ __forceinline__ int cached_volume(VolCache &c, const VolDesc *__restrict__ vols, int nvol, long long b) {
+    if (c.v < 0 || b < c.base || b >= c.end) {
+        c.v = find_volume(vols, nvol, b);
+        c.base = vols[c.v].brick_base;
+        c.end = c.base + vols[c.v].nbricks;
+    }
+    return c.v;
+}
+
 template <int VT>
 __device__ __forceinline__ void issue_cls_tile(ClsSmemMulti<VT> &S, int s, const VolDesc *__restrict__ vols, int nvol,
-                                               const CUtensorMap *maps, long long b) {
-    const int v = find_volume(vols, nvol, b);
+                                               const CUtensorMap *maps, long long b, VolCache &vc) {
+    const int v = cached_volume(vc, vols, nvol, b);
     S.svol[s] = v;
     S.stma[s] = vols[v].tma;
+    const BrickPos bp = brick_pos(b - vc.base, vols[v].nbx, vols[v].nby);
+    S.spos[s] = make_int4(bp.x0, bp.y0, bp.z0, 0);
     if (vols[v].tma) {
-        const BrickPos bp = brick_pos(b - vols[v].brick_base, vols[v].nbx, vols[v].nby);
         mbar_arrive_expect_tx(&S.bars[s], CTILE * Vox<VT>::bytes);
         tma_load_3d(S.tiles[s], maps + v, &S.bars[s], bp.x0, bp.y0, bp.z0);
     }
@@ -1208,6 +1227,7 @@ __global__ void __launch_bounds__(CTHREADS)
     const int tid = threadIdx.x;
     const long long stride = gridDim.x;
     uint32_t phase[2] = {0, 0};
+    VolCache vc;
     for (int c = tid; c < 256; c += CTHREADS) S.ntri[c] = (c == 0 || c == 255) ? 0 : c_nverts[c] / 3;
     if (tid == 0) {
         S.abort = 0;
@@ -1215,7 +1235,7 @@ __global__ void __launch_bounds__(CTHREADS)
         fence_barrier_init();
         for (int s = 0; s < 2; ++s) {
             const long long b = blockIdx.x + s * stride;
-            if (b < nbricks) issue_cls_tile<VT>(S, s, vols, nvol, maps, b);
+            if (b < nbricks) issue_cls_tile<VT>(S, s, vols, nvol, maps, b, vc);
         }
     }
     __syncthreads();
@@ -1226,7 +1246,11 @@ __global__ void __launch_bounds__(CTHREADS)
         T *tile = reinterpret_cast<T *>(S.tiles[s]);
         const int v = S.svol[s];
         const VolDesc &d = vols[v];
-        const BrickPos bp = brick_pos(b - d.brick_base, d.nbx, d.nby);
+        const int4 sp = S.spos[s];
+        BrickPos bp;
+        bp.x0 = sp.x;
+        bp.y0 = sp.y;
+        bp.z0 = sp.z;
         if (S.stma[s]) {
             if (tid == 0) {
                 if (!mbar_wait(&S.bars[s], phase[s])) S.abort = 1;
@@ -1260,7 +1284,7 @@ __global__ void __launch_bounds__(CTHREADS)
                 atomicAdd(&vol_sums[2 * v + 1], (unsigned long long)o);
             }
             const long long nb = b + 2 * stride;
-            if (nb < nbricks) issue_cls_tile<VT>(S, s, vols, nvol, maps, nb);
+            if (nb < nbricks) issue_cls_tile<VT>(S, s, vols, nvol, maps, nb, vc);
         }
     }
     if (S.abort && tid == 0) {
@@ -1269,33 +1293,67 @@ __global__ void __launch_bounds__(CTHREADS)
     }
 }
 
-template <int VT>
-struct GenSmemMulti : GenSmem<VT> {
-    int svol[2];
-    int stma[2];
+// An active-list entry of a batch resolved for the generate launch: volume,
+// brick origin and soup offset inside the volume's soup.
+struct BatchBrick {
+    unsigned long long vbase;
+    int v, x0, y0, z0;
+    int pad[2];
 };
+static_assert(sizeof(BatchBrick) == 32, "two 16-byte copies");
 
-template <int VT>
-__device__ __forceinline__ void issue_gen_tile(GenSmemMulti<VT> &S, int s, const VolDesc *__restrict__ vols, int nvol,
-                                               const CUtensorMap *maps, const unsigned long long *__restrict__ vofs,
-                                               long long b) {
-    const int v = find_volume(vols, nvol, b);
-    S.svol[s] = v;
-    S.stma[s] = vols[v].tma;
-    S.sbrick[s] = b;
-    S.svbase[s] = vofs[b] - vofs[vols[v].brick_base];
-    if (vols[v].tma) {
-        const BrickPos bp = brick_pos(b - vols[v].brick_base, vols[v].nbx, vols[v].nby);
-        mbar_arrive_expect_tx(&S.bars[s], GTILE * Vox<VT>::bytes);
-        tma_load_3d(S.tiles[s], maps + v, &S.bars[s], bp.x0 - TXO, bp.y0 - TYO, bp.z0 - TZO);
+// One thread per active-list entry: the volume search, the brick origin and
+// the per-volume soup offset, done once here instead of by the thread that
+// stages the brick while its CTA waits.
+__global__ void mc_resolve_multi_kernel(const VolDesc *__restrict__ vols, int nvol, const uint32_t *__restrict__ active,
+                                        const unsigned long long *__restrict__ vofs,
+                                        const MeshTotals *__restrict__ totals, BatchBrick *__restrict__ out) {
+    const unsigned int n = totals->active_bricks;
+    for (unsigned int w = blockIdx.x * blockDim.x + threadIdx.x; w < n; w += gridDim.x * blockDim.x) {
+        const long long b = active[w];
+        const int v = find_volume(vols, nvol, b);
+        const long long base = vols[v].brick_base;
+        const BrickPos bp = brick_pos(b - base, vols[v].nbx, vols[v].nby);
+        BatchBrick r;
+        r.vbase = vofs[b] - vofs[base];
+        r.v = v;
+        r.x0 = bp.x0;
+        r.y0 = bp.y0;
+        r.z0 = bp.z0;
+        r.pad[0] = r.pad[1] = 0;
+        out[w] = r;
     }
 }
 
 template <int VT>
+struct GenSmemMulti : GenSmem<VT> {
+    int svol[2];
+    int stma[2];
+    alignas(16) BatchBrick pipe;  // entry staged at the next refill (thread 0's pipeline)
+};
+
+template <int VT>
+__device__ __forceinline__ void issue_gen_tile(GenSmemMulti<VT> &S, int s, const VolDesc *__restrict__ vols,
+                                               const CUtensorMap *maps, const BatchBrick &r) {
+    S.svol[s] = r.v;
+    S.stma[s] = vols[r.v].tma;
+    S.sbrick[s] = 0;
+    S.svbase[s] = r.vbase;
+    S.spos[s] = make_int4(r.x0, r.y0, r.z0, 0);
+    if (vols[r.v].tma) {
+        mbar_arrive_expect_tx(&S.bars[s], GTILE * Vox<VT>::bytes);
+        tma_load_3d(S.tiles[s], maps + r.v, &S.bars[s], r.x0 - TXO, r.y0 - TYO, r.z0 - TZO);
+    }
+}
+
+// Bricks of every volume of the batch from one active list, scheduled as in
+// the single-volume launch: fixed serpentine first rounds, then entries from
+// the counter, each entry's resolved record copied asynchronously one brick
+// before it is staged.
+template <int VT>
 __global__ void __launch_bounds__(THREADS, 4)
     mc_generate_multi_kernel(const VolDesc *__restrict__ vols, const CUtensorMap *maps, int nvol,
-                             const uint32_t *__restrict__ active, const unsigned long long *__restrict__ vofs,
-                             MeshTotals *totals) {
+                             const BatchBrick *__restrict__ list, MeshTotals *totals) {
     using V = Vox<VT>;
     using T = typename V::T;
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -1305,34 +1363,46 @@ __global__ void __launch_bounds__(THREADS, 4)
     for (int i = tid; i < 256 * 16; i += THREADS) (&S.tri[0][0])[i] = (&c_tri[0][0])[i];
     S.nv[tid] = (tid == 0 || tid == 255) ? 0 : c_nverts[tid];
     const unsigned int nactive = totals->active_bricks;
+    unsigned int *ticket = &totals->gen_ticket;
+    const unsigned int grid = gridDim.x, c = blockIdx.x;
+    const unsigned int tbase = 3 * grid;  // list entry of ticket 0
+    auto entry = [&](unsigned int r) { return r * grid + ((r & 1) ? grid - 1 - c : c); };
+    unsigned int ptk = 0xffffffffu;  // list entry of the ticket drawn at the top of this brick
+    bool have_pipe = false;          // S.pipe holds the entry of the next refill
     if (tid == 0) {
         S.abort = 0;
         for (int s = 0; s < 2; ++s) mbar_init(&S.bars[s], 1);
         fence_barrier_init();
         for (int s = 0; s < 2; ++s) {
-            const unsigned int w = blockIdx.x + s * gridDim.x;
-            if (w < nactive) issue_gen_tile<VT>(S, s, vols, nvol, maps, vofs, active[w]);
+            S.svol[s] = -1;
+            const unsigned int w = entry(s);
+            if (w < nactive) issue_gen_tile<VT>(S, s, vols, maps, list[w]);
         }
+        const unsigned int w = entry(2);
+        if (w < nactive) {
+            cp_async_16(&S.pipe, list + w);
+            cp_async_16(reinterpret_cast<unsigned char *>(&S.pipe) + 16, reinterpret_cast<const unsigned char *>(list + w) + 16);
+            have_pipe = true;
+        }
+        if (tbase < nactive) ptk = 0;  // not ~0u: draw tickets at the tops of the bricks
     }
     __syncthreads();
-    int it = 0;
-    for (unsigned int w = blockIdx.x; w < nactive; w += gridDim.x, ++it) {
+    for (int it = 0;; ++it) {
         const int s = it & 1;
         T *tile = reinterpret_cast<T *>(S.tiles[s]);
-        const long long b = S.sbrick[s];
-        const unsigned long long vbase = S.svbase[s];
         const int v = S.svol[s];
-        const VolDesc &d = vols[v];
-        const BrickPos bp = brick_pos(b - d.brick_base, d.nbx, d.nby);
-        if (S.stma[s]) {
-            if (tid == 0) {
-                if (!mbar_wait(&S.bars[s], phase[s])) S.abort = 1;
-            }
-            phase[s] ^= 1u;
-        } else {
-            fill_tile<VT, TX, TY, TZ>(tile, static_cast<const T *>(d.data), d.nx, d.ny, d.nz, bp.x0 - TXO,
-                                      bp.y0 - TYO, bp.z0 - TZO);
+        if (v < 0) break;  // uniform
+        if (tid == 0) {
+            if (ptk != 0xffffffffu) ptk = tbase + atomicAdd(ticket, 1u);
+            if (S.stma[s] && !mbar_wait(&S.bars[s], phase[s])) S.abort = 1;
         }
+        if (S.stma[s]) phase[s] ^= 1u;
+        const unsigned long long vbase = S.svbase[s];
+        const int4 sp = S.spos[s];
+        const VolDesc &d = vols[v];
+        if (!S.stma[s])
+            fill_tile<VT, TX, TY, TZ>(tile, static_cast<const T *>(d.data), d.nx, d.ny, d.nz, sp.x - TXO, sp.y - TYO,
+                                      sp.z - TZO);
         __syncthreads();
         if (S.abort) break;
         GenOut o;
@@ -1343,13 +1413,26 @@ __global__ void __launch_bounds__(THREADS, 4)
         o.tri_cube = d.tri_cube;
         o.cap = d.cap;
         o.zlim = d.nz - 1;
-        generate_brick<VT>(S, tile, static_cast<const T *>(d.data), d.nx, d.ny, d.nz, d.cell, bp.x0, bp.y0, bp.z0,
+        generate_brick<VT>(S, tile, static_cast<const T *>(d.data), d.nx, d.ny, d.nz, d.cell, sp.x, sp.y, sp.z,
                            vbase, o);
         __syncthreads();  // tile s, the list and the stage are free again
         if (tid == 0) {
-            const unsigned int wn = w + 2 * gridDim.x;
-            if (wn < nactive) issue_gen_tile<VT>(S, s, vols, nvol, maps, vofs, active[wn]);
+            S.svol[s] = -1;
+            if (have_pipe) {
+                cp_async_wait_all();
+                issue_gen_tile<VT>(S, s, vols, maps, S.pipe);
+            }
+            have_pipe = ptk < nactive;
+            if (have_pipe) {
+                cp_async_16(&S.pipe, list + ptk);
+                cp_async_16(reinterpret_cast<unsigned char *>(&S.pipe) + 16,
+                            reinterpret_cast<const unsigned char *>(list + ptk) + 16);
+            } else {
+                ptk = 0xffffffffu;  // the list is exhausted: draw no more tickets
+            }
         }
+        // S.svol[s] is next read at the top of iteration it + 2, after the
+        // barriers of iteration it + 1
     }
     if (S.abort && tid == 0) {
         atomicOr(&totals->flags, 1u);
@@ -1763,16 +1846,19 @@ namespace {
 size_t btab_desc_bytes(int nvol) { return ((sizeof(VolDesc) * (size_t)nvol + 63) / 64) * 64; }
 size_t btab_bytes(int nvol) { return btab_desc_bytes(nvol) + 2 * sizeof(CUtensorMap) * (size_t)nvol; }
 
-mcg_status grow_pinned(mcg_context *ctx, unsigned char **p, size_t *cap, size_t n) {
-    if (*cap >= n && *p) return MCG_OK;
-    if (*p) {
-        if (ctx->btab_pending) cudaEventSynchronize(ctx->btab_copied);
-        cudaFreeHost(*p);
+// staging slot k of at least n bytes; its last copy has completed
+mcg_status grow_pinned(mcg_context *ctx, int k, size_t n) {
+    if (ctx->btab_pending[k]) {
+        const cudaError_t e = cudaEventSynchronize(ctx->btab_copied[k]);
+        if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
+        ctx->btab_pending[k] = false;
     }
-    *p = nullptr;
-    *cap = 0;
-    if (cudaMallocHost((void **)p, n) != cudaSuccess) return mcg_cuda_fail(ctx, cudaErrorMemoryAllocation);
-    *cap = n;
+    if (ctx->h_btab_cap[k] >= n && ctx->h_btab[k]) return MCG_OK;
+    if (ctx->h_btab[k]) cudaFreeHost(ctx->h_btab[k]);
+    ctx->h_btab[k] = nullptr;
+    ctx->h_btab_cap[k] = 0;
+    if (cudaMallocHost((void **)&ctx->h_btab[k], n) != cudaSuccess) return mcg_cuda_fail(ctx, cudaErrorMemoryAllocation);
+    ctx->h_btab_cap[k] = n;
     return MCG_OK;
 }
 
@@ -1790,15 +1876,23 @@ mcg_status upload_btab(mcg_context *ctx, const mcg_volume *vols, const mcg_mesh_
                        bool with_maps, cudaStream_t s, long long *total_bricks) {
     const size_t bytes = btab_bytes(nvol);
     if (!ensure(&ctx->d_btab, &ctx->d_btab_cap, bytes)) return mcg_cuda_fail(ctx, cudaErrorMemoryAllocation);
-    mcg_status st = grow_pinned(ctx, &ctx->h_btab, &ctx->h_btab_cap, bytes);
+    const int k = ctx->btab_slot;
+    mcg_status st = grow_pinned(ctx, k, bytes);
     if (st != MCG_OK) return st;
-    if (ctx->btab_pending) {
-        cudaError_t e = cudaEventSynchronize(ctx->btab_copied);
-        if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
-        ctx->btab_pending = false;
+    ctx->btab_slot ^= 1;
+    if (with_maps) {
+        if (ctx->batch_tma_cap < (size_t)nvol) {
+            unsigned char *t = static_cast<unsigned char *>(realloc(ctx->batch_tma, (size_t)nvol));
+            if (!t) return MCG_ERR_INVALID_ARG;
+            ctx->batch_tma = t;
+            ctx->batch_tma_cap = (size_t)nvol;
+        }
+    } else if (ctx->batch_tma_cap < (size_t)nvol) {
+        return MCG_ERR_STATE;
     }
-    VolDesc *desc = reinterpret_cast<VolDesc *>(ctx->h_btab);
-    CUtensorMap *cmaps = reinterpret_cast<CUtensorMap *>(ctx->h_btab + btab_desc_bytes(nvol));
+    unsigned char *hb = ctx->h_btab[k];
+    VolDesc *desc = reinterpret_cast<VolDesc *>(hb);
+    CUtensorMap *cmaps = reinterpret_cast<CUtensorMap *>(hb + btab_desc_bytes(nvol));
     CUtensorMap *gmaps = cmaps + nvol;
     long long base = 0;
     const int eb = vols[0].voxel_type == MCG_VOXEL_SHORT2 ? 4 : 8;
@@ -1824,24 +1918,30 @@ mcg_status upload_btab(mcg_context *ctx, const mcg_volume *vols, const mcg_mesh_
             d.tri_cube = outs[v].tri_cube;
             d.cap = outs[v].capacity_vertices;
         }
-        // TMA only when both boxes can be described (the flag serves both passes)
-        const bool tc = encode_volume_map(&cmaps[v], vols[v].data, vols[v].nx, vols[v].ny, vols[v].nz, eb, CTX, CTY, CTZ);
-        const bool tg = encode_volume_map(&gmaps[v], vols[v].data, vols[v].nx, vols[v].ny, vols[v].nz, eb, TX, TY, TZ);
-        d.tma = tc && tg ? 1 : 0;
-        if (!d.tma) {
-            memset(&cmaps[v], 0, sizeof(CUtensorMap));
-            memset(&gmaps[v], 0, sizeof(CUtensorMap));
+        // TMA only when both boxes can be described (the flag serves both
+        // passes); the maps are encoded and copied with the count phase's
+        // table, the generate phase's table carries the flags it recorded
+        if (with_maps) {
+            const bool tc =
+                encode_volume_map(&cmaps[v], vols[v].data, vols[v].nx, vols[v].ny, vols[v].nz, eb, CTX, CTY, CTZ);
+            const bool tg = encode_volume_map(&gmaps[v], vols[v].data, vols[v].nx, vols[v].ny, vols[v].nz, eb, TX, TY, TZ);
+            ctx->batch_tma[v] = tc && tg ? 1 : 0;
+            if (!ctx->batch_tma[v]) {
+                memset(&cmaps[v], 0, sizeof(CUtensorMap));
+                memset(&gmaps[v], 0, sizeof(CUtensorMap));
+            }
         }
+        d.tma = ctx->batch_tma[v];
     }
     *total_bricks = base;
     const size_t n = with_maps ? bytes : btab_desc_bytes(nvol);
-    cudaError_t e = cudaMemcpyAsync(ctx->d_btab, ctx->h_btab, n, cudaMemcpyHostToDevice, s);
+    cudaError_t e = cudaMemcpyAsync(ctx->d_btab, hb, n, cudaMemcpyHostToDevice, s);
     // during capture the staging copy becomes a graph node that reads the
-    // staging buffer at every replay: it must then stay untouched
+    // staging slot at every replay: it must then stay untouched
     const bool cap = mcg_capturing(s);
-    if (e == cudaSuccess && !cap) e = cudaEventRecord(ctx->btab_copied, s);
+    if (e == cudaSuccess && !cap) e = cudaEventRecord(ctx->btab_copied[k], s);
     if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
-    ctx->btab_pending = !cap;
+    ctx->btab_pending[k] = !cap;
     return MCG_OK;
 }
 
@@ -1860,16 +1960,25 @@ void launch_classify_multi(mcg_context *ctx, int nvol, long long nbricks, cudaSt
 }
 
 template <int VT>
-void launch_generate_multi(mcg_context *ctx, int nvol, long long nbricks, cudaStream_t s) {
+cudaError_t launch_generate_multi(mcg_context *ctx, int nvol, long long nbricks, cudaStream_t s) {
+    if (!ensure(&ctx->batch_list, &ctx->batch_list_cap, (size_t)nbricks * sizeof(BatchBrick)))
+        return cudaErrorMemoryAllocation;
+    const VolDesc *desc = reinterpret_cast<const VolDesc *>(ctx->d_btab);
+    BatchBrick *list = reinterpret_cast<BatchBrick *>(ctx->batch_list);
+    cudaError_t e = cudaMemsetAsync(&ctx->d_totals->gen_ticket, 0, sizeof(unsigned int), s);
+    if (e != cudaSuccess) return e;
+    long long rgrid = (nbricks + 255) / 256;
+    if (rgrid > 4LL * ctx->num_sms) rgrid = 4LL * ctx->num_sms;
+    mc_resolve_multi_kernel<<<(unsigned int)rgrid, 256, 0, s>>>(desc, nvol, ctx->active, ctx->brick_vofs,
+                                                                 ctx->d_totals, list);
     const size_t smem = sizeof(GenSmemMulti<VT>);
     static int occ = 0;
     if (!occ) occ = occupancy(mc_generate_multi_kernel<VT>, THREADS, smem);
     long long grid = (long long)ctx->num_sms * occ;
     if (grid > nbricks) grid = nbricks;
-    const VolDesc *desc = reinterpret_cast<const VolDesc *>(ctx->d_btab);
     const CUtensorMap *gmaps = reinterpret_cast<const CUtensorMap *>(ctx->d_btab + btab_desc_bytes(nvol)) + nvol;
-    mc_generate_multi_kernel<VT><<<(int)grid, THREADS, smem, s>>>(desc, gmaps, nvol, ctx->active, ctx->brick_vofs,
-                                                                   ctx->d_totals);
+    mc_generate_multi_kernel<VT><<<(int)grid, THREADS, smem, s>>>(desc, gmaps, nvol, list, ctx->d_totals);
+    return cudaGetLastError();
 }
 
 }  // namespace
@@ -1979,9 +2088,8 @@ mcg_status mcg_mc_generate_batched(mcg_context *ctx, const mcg_volume *vols, con
     mcg_status st = upload_btab(ctx, vols, outs, nvol, false, s, &total);
     if (st != MCG_OK) return st;
     if (total != ctx->batch_nbricks) return MCG_ERR_STATE;
-    if (vols[0].voxel_type == MCG_VOXEL_SHORT2) launch_generate_multi<MCG_VOXEL_SHORT2>(ctx, nvol, total, s);
-    else launch_generate_multi<MCG_VOXEL_FLOAT2>(ctx, nvol, total, s);
-    e = cudaGetLastError();
+    if (vols[0].voxel_type == MCG_VOXEL_SHORT2) e = launch_generate_multi<MCG_VOXEL_SHORT2>(ctx, nvol, total, s);
+    else e = launch_generate_multi<MCG_VOXEL_FLOAT2>(ctx, nvol, total, s);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(ctx->h_totals, ctx->d_totals, sizeof(MeshTotals), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = mcg_counts_event(ctx, s);

@@ -58,6 +58,8 @@ struct mcg_context {
     size_t active_cap = 0;
     unsigned long long *list_vofs = nullptr;  // soup offset per active-list entry
     size_t list_vofs_cap = 0;
+    unsigned char *batch_list = nullptr;  // resolved active-list entries of a batch (32 B each)
+    size_t batch_list_cap = 0;
     // indexed extraction: owned vertices and their offsets per brick, and
     // the vertex id of every grid edge (3 per voxel, written sparsely)
     uint32_t *brick_uniq = nullptr;
@@ -86,10 +88,15 @@ struct mcg_context {
     // generate tensor maps), pinned staging for them, per-volume sums
     unsigned char *d_btab = nullptr;
     size_t d_btab_cap = 0;
-    unsigned char *h_btab = nullptr;  // pinned
-    size_t h_btab_cap = 0;
-    cudaEvent_t btab_copied = nullptr;
-    bool btab_pending = false;
+    // pinned staging of the table, two slots used in turn: a call waits only
+    // for the copy out of the slot two calls back
+    unsigned char *h_btab[2] = {nullptr, nullptr};
+    size_t h_btab_cap[2] = {0, 0};
+    cudaEvent_t btab_copied[2] = {nullptr, nullptr};
+    bool btab_pending[2] = {false, false};
+    int btab_slot = 0;
+    unsigned char *batch_tma = nullptr;  // per volume of the classified batch: both boxes encodable
+    size_t batch_tma_cap = 0;
     unsigned long long *d_vol_sums = nullptr;
     size_t d_vol_sums_cap = 0;
     unsigned long long *h_vol_sums = nullptr;  // pinned
