@@ -6,7 +6,10 @@
 #include "mcg_internal.h"
 
 mcg_status mcg_cuda_fail(mcg_context *ctx, cudaError_t e) {
-    if (ctx) ctx->last_cuda_error = (int)e;
+    if (ctx) {
+        ctx->last_cuda_error = (int)e;
+        ctx->counters_clean = false;
+    }
     cudaGetLastError();  // clear a sticky-free error so later calls can proceed
     return MCG_ERR_CUDA;
 }

@@ -533,6 +533,9 @@ __global__ void __launch_bounds__(CHUNK)
     }
     __syncthreads();  // this CTA's reads of the chunk sums are done
     if (tid == 0) {
+        // the count launch's flags, read before this CTA counts itself done
+        // (the last CTA may clear them after that)
+        const unsigned int fl = j == 0 ? *(volatile unsigned int *)&totals->flags : 0u;
         __threadfence();
         s_last = atomicAdd(&totals->scan_done, 1u) == gridDim.x - 1;
         unsigned long long r[NACC];
@@ -558,7 +561,7 @@ __global__ void __launch_bounds__(CHUNK)
                 host->triangles = r[2 + NH];
                 host->vertices = 3ull * r[2 + NH];
                 host->active_bricks = (unsigned int)r[3 + NH];
-                host->flags = *(volatile unsigned int *)&totals->flags;  // the count launch has finished
+                host->flags = fl;
                 __threadfence_system();
             }
         }
@@ -605,9 +608,15 @@ __global__ void __launch_bounds__(CHUNK)
                 if (list_vofs) list_vofs[w] = v;
             }
     }
-    if (s_last) {  // every CTA has read the chunk sums
+    if (s_last) {  // every CTA has read the chunk sums (and CTA 0 the flags)
         for (long long i = tid; i < nchunks * CHUNK_FIELDS; i += CHUNK) chunk[i] = 0;
-        if (tid == 0) totals->scan_done = 0;
+        if (tid == 0) {
+            totals->scan_done = 0;
+            if (host) {  // the flags live on in the host copy
+                totals->flags = 0;
+                totals->cls_ticket = 0;
+            }
+        }
     }
 }
 
@@ -1127,8 +1136,9 @@ __global__ void __launch_bounds__(THREADS, 4) mc_generate_kernel(const __grid_co
         if (atomicAdd(&p.totals->gen_exit, 1u) == gridDim.x - 1) {
             p.totals->gen_ticket = 0;
             p.totals->gen_exit = 0;
-            if (p.host) {
-                p.host->flags = *(volatile unsigned int *)&p.totals->flags;
+            if (p.host) {  // onto the count phase's flags in the host copy
+                p.host->flags |= *(volatile unsigned int *)&p.totals->flags;
+                p.totals->flags = 0;
                 __threadfence_system();
             }
         }
@@ -1572,10 +1582,11 @@ void launch_generate_t(const CUtensorMap &map, const GenParams &p, const Geometr
 // classify + scan into sc; clears the timeout flag first
 long long num_chunks(long long nbricks) { return (nbricks + CHUNK - 1) / CHUNK; }
 
-cudaError_t launch_count_phase(const mcg_volume *vol, const Geometry &g, const Scratch &sc, int sms, cudaStream_t s) {
-    // flags and both work counters; the chunk sums are zero already (the
-    // previous scan cleared them)
-    cudaError_t e = cudaMemsetAsync(&sc.totals->flags, 0, 3 * sizeof(unsigned int), s);
+cudaError_t launch_count_phase(const mcg_volume *vol, const Geometry &g, const Scratch &sc, int sms, cudaStream_t s,
+                               bool clear = true) {
+    // flags and both work counters unless known to be zero; the chunk sums
+    // are zero already (the previous scan cleared them)
+    cudaError_t e = clear ? cudaMemsetAsync(&sc.totals->flags, 0, 3 * sizeof(unsigned int), s) : cudaSuccess;
     if (e != cudaSuccess) return e;
     CUtensorMap map, hmap;
     const int eb = vol->voxel_type == MCG_VOXEL_SHORT2 ? 4 : 8;
@@ -1677,7 +1688,8 @@ static mcg_status classify_impl(mcg_context *ctx, const mcg_volume *vol, int32_t
         if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
         ctx->chunk_clean_cap = ctx->brick_occ_cap;
     }
-    e = launch_count_phase(vol, g, ctx_scratch(ctx), ctx->num_sms, s);
+    e = launch_count_phase(vol, g, ctx_scratch(ctx), ctx->num_sms, s, !ctx->h_totals_dev || !ctx->counters_clean);
+    ctx->counters_clean = e == cudaSuccess && ctx->h_totals_dev != nullptr;
     if (e == cudaSuccess && !ctx->h_totals_dev)
         e = cudaMemcpyAsync(ctx->h_totals, ctx->d_totals, sizeof(MeshTotals), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = mcg_counts_event(ctx, s);
@@ -1805,6 +1817,7 @@ mcg_status mcg_mc_backward(mcg_context *ctx, const mcg_volume *vol, const float 
     const Geometry g = geometry_slab(vol->nx, vol->ny, ctx->cls_z0, ctx->cls_z1);
     e = cudaMemsetAsync(&ctx->d_totals->gen_ticket, 0, sizeof(unsigned int), s);
     if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
+    ctx->counters_clean = false;  // a timeout here leaves the flags set
     GenParams p;
     memset(&p, 0, sizeof(p));
     p.vol = vol->data;
@@ -2011,6 +2024,7 @@ mcg_status mcg_mc_classify_batched(mcg_context *ctx, const mcg_volume *vols, int
     long long total = 0;
     mcg_status st = upload_btab(ctx, vols, nullptr, nvol, true, s, &total);
     if (st != MCG_OK) return st;
+    ctx->counters_clean = false;  // the batched launches leave the counters in use
     e = cudaMemsetAsync(&ctx->d_totals->flags, 0, sizeof(unsigned int), s);
     if (e == cudaSuccess) e = cudaMemsetAsync(ctx->brick_occ, 0, sizeof(uint32_t) * CHUNK_FIELDS * num_chunks(nbricks), s);
     if (e == cudaSuccess) e = cudaMemsetAsync(ctx->d_vol_sums, 0, sizeof(unsigned long long) * 2 * nvol, s);

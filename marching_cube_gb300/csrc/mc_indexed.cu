@@ -758,6 +758,7 @@ mcg_status mcg_mc_classify_indexed(mcg_context *ctx, const mcg_volume *vol, mcg_
     e = cudaMemsetAsync(&ctx->d_totals->flags, 0, 4 * sizeof(unsigned int), s);
     if (e == cudaSuccess) e = cudaMemsetAsync(ctx->brick_occ, 0, sizeof(uint32_t) * 4 * nch, s);
     ctx->chunk_clean_cap = 0;  // these sums stay behind: the next count phase clears the array first
+    ctx->counters_clean = false;
     if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
     const IdxParams p = idx_params(ctx, vol, g);
     launch_idx_pass(0, vol, p, ctx->num_sms, g.nbricks, s);

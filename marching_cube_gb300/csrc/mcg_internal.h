@@ -72,6 +72,10 @@ struct mcg_context {
     mcg::MeshTotals *h_totals = nullptr;  // pinned, mapped
     mcg::MeshTotals *h_totals_dev = nullptr;  // device address of h_totals; null if it has none
     size_t chunk_clean_cap = 0;  // brick_occ entries known to be zero (the scan re-zeroes what it used)
+    // flags and work counters of d_totals known to be zero: the last scan and
+    // generate CTAs reset them when the totals reach the host through
+    // h_totals_dev; any other launch over them, or an error, clears this
+    bool counters_clean = false;
     cudaEvent_t counts_ready = nullptr;
     bool counts_pending = false;
 
