@@ -632,6 +632,7 @@ struct GenParams {
     const unsigned long long *list_vofs;  // soup offset of each active-list entry
     MeshTotals *totals;
     MeshTotals *host;  // mapped host copy of the totals (flags written at exit), or null
+    unsigned int fixed_rounds;  // first bricks of each CTA taken in fixed serpentine rounds
     mcg_vertex_voxel *soup;
     float *normals;
     int32_t *vi2vox;
@@ -1043,21 +1044,30 @@ __global__ void __launch_bounds__(THREADS, 4) mc_generate_kernel(const __grid_co
     // global memory (a wait in warp 0 would hold the whole CTA at its next
     // barrier).
     const unsigned int grid = gridDim.x, c = blockIdx.x;
-    const unsigned int tbase = (GSTAGES + 1) * grid;  // list entry of ticket 0
+    const unsigned int nfix = p.fixed_rounds;
+    const unsigned int tbase = nfix * grid;  // list entry of ticket 0
+    // list entry of this CTA's k-th brick: fixed rounds first, then the counter
+    auto next_entry = [&](unsigned int k) {
+        return k < nfix ? k * grid + ((k & 1) ? grid - 1 - c : c) : tbase + atomicAdd(ticket, 1u);
+    };
     unsigned int ptk = 0xffffffffu;  // list entry of the ticket drawn at the top of this brick
+    unsigned int kdraw = GSTAGES + 1;  // entries assigned so far (thread 0)
     if (TMA && tid == 0) {
+        unsigned int wr[GSTAGES + 1];
+#pragma unroll
+        for (unsigned int r = 0; r <= GSTAGES; ++r) wr[r] = next_entry(r);
 #pragma unroll
         for (int r = 0; r < GSTAGES; ++r) {
-            const unsigned int w = r * grid + ((r & 1) ? grid - 1 - c : c);
+            const unsigned int w = wr[r];
             stage_brick(r, w < nactive ? (long long)p.active[w] : -1ll, w < nactive ? p.list_vofs[w] : 0ull);
         }
-        const unsigned int w = GSTAGES * grid + ((GSTAGES & 1) ? grid - 1 - c : c);
+        const unsigned int w = wr[GSTAGES];
         S.pipe_b = 0xffffffffu;
         if (w < nactive) {
             cp_async_4(&S.pipe_b, p.active + w);
             cp_async_8(&S.pipe_v, p.list_vofs + w);
         }
-        if (tbase < nactive) ptk = 0;  // not ~0u: draw tickets at the tops of the bricks
+        if (w < nactive) ptk = 0;  // not ~0u: draw tickets at the tops of the bricks
     }
     if (TMA) __syncthreads();
     for (int it = 0;; ++it) {
@@ -1071,7 +1081,7 @@ __global__ void __launch_bounds__(THREADS, 4) mc_generate_kernel(const __grid_co
             if (b < 0) break;  // uniform
             if (tid == 0) {
                 // the ticket of the refill after the next one (used at this brick's end)
-                if (ptk != 0xffffffffu) ptk = tbase + atomicAdd(ticket, 1u);
+                if (ptk != 0xffffffffu) ptk = next_entry(kdraw++);
                 if (!mbar_wait(&S.bars[s], (uint32_t)((it / GSTAGES) & 1))) S.abort = 1;
             }
             __syncthreads();
@@ -1475,6 +1485,20 @@ struct Scratch {
     MeshTotals *host;  // mapped host copy of the totals, or null
 };
 
+// fixed serpentine rounds at the start of the generate launch (tuning:
+// MCG_GEN_FIXED)
+unsigned int generate_fixed_rounds() {
+    static int f = -1;
+    if (f < 0) {
+        f = 3;
+        if (const char *e = getenv("MCG_GEN_FIXED")) {
+            const int v = atoi(e);
+            if (v >= 0 && v <= 1000000) f = v;
+        }
+    }
+    return (unsigned int)f;
+}
+
 // Launch with programmatic stream serialisation: the kernel may start while
 // the kernel before it on the stream drains (it waits with pdl_wait).
 template <class... P, class... A>
@@ -1634,6 +1658,7 @@ cudaError_t launch_generate_phase(const mcg_volume *vol, const Geometry &g, cons
     p.brick_vofs = sc.vofs;
     p.list_vofs = sc.list_vofs;
     p.host = sc.host;
+    p.fixed_rounds = generate_fixed_rounds();
     p.totals = sc.totals;
     p.soup = out->soup;
     p.normals = out->soup_normals;
@@ -1833,6 +1858,7 @@ mcg_status mcg_mc_backward(mcg_context *ctx, const mcg_volume *vol, const float 
     p.brick_vofs = ctx->brick_vofs;
     p.list_vofs = ctx->list_vofs;
     p.totals = ctx->d_totals;
+    p.fixed_rounds = generate_fixed_rounds();
     p.grad_pos = grad_pos;
     p.grad_f = grad_f;
     p.n_grad = n_vertices;
