@@ -112,7 +112,7 @@ __device__ __forceinline__ BrickPos slab_pos(long long b, int nbx, int nby, int 
 // thread's loads are in flight at once), zero-filled outside the volume like
 // the TMA fill.  Each thread waits for its own copies; the caller's barrier
 // then publishes the tile.
-template <int VT, int DX, int DY, int DZ>
+template <int VT, int DX, int DY, int DZ, bool WAIT = true>
 __device__ __forceinline__ void fill_tile(typename Vox<VT>::T *tile, const typename Vox<VT>::T *__restrict__ vol,
                                           int nx, int ny, int nz, int ox, int oy, int oz) {
     constexpr int B = Vox<VT>::bytes;
@@ -130,7 +130,7 @@ __device__ __forceinline__ void fill_tile(typename Vox<VT>::T *tile, const typen
             asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(smem_u32(tile + i)), "l"(src), "r"(n)
                          : "memory");
     }
-    cp_async_wait_all();
+    if (WAIT) cp_async_wait_all();
 }
 
 // ---- normals (cu_kinect_fusion_v1.cu:3146-3225) -----------------------------------

@@ -1201,6 +1201,8 @@ struct ClsSmemMulti {
     int svol[2];
     int stma[2];
     int4 spos[2];  // origin of each stage's brick
+    int4 nxt;      // the brick refilled at the end of this iteration: {volume, TMA, origin x, y}
+    int nxt_z;
     int abort;
 };
 
@@ -1235,6 +1237,10 @@ __device__ __forceinline__ void issue_cls_tile(ClsSmemMulti<VT> &S, int s, const
     }
 }
 
+// Count pass over all volumes of a batch, one brick per work item, bricks a
+// fixed stride apart per CTA, 2 tile stages: TMA volumes load by TMA, the
+// others by asynchronous per-voxel copies (one copy group per iteration), so
+// in both cases the next tile loads while the current one is classified.
 template <int VT>
 __global__ void __launch_bounds__(CTHREADS)
     mc_classify_multi_kernel(const VolDesc *__restrict__ vols, const CUtensorMap *maps, int nvol, long long nbricks,
@@ -1259,6 +1265,15 @@ __global__ void __launch_bounds__(CTHREADS)
         }
     }
     __syncthreads();
+    // the plain-copy fills of the first two stages, one copy group each
+    for (int s = 0; s < 2; ++s) {
+        if (blockIdx.x + s * stride < nbricks && !S.stma[s]) {
+            const VolDesc &d = vols[S.svol[s]];
+            fill_tile<VT, CTX, CTY, CTZ, false>(reinterpret_cast<T *>(S.tiles[s]), static_cast<const T *>(d.data),
+                                                d.nx, d.ny, d.nz, S.spos[s].x, S.spos[s].y, S.spos[s].z);
+        }
+        cp_async_commit();
+    }
     for (int i = 0;; ++i) {
         const long long b = blockIdx.x + (long long)i * stride;
         if (b >= nbricks) break;
@@ -1277,15 +1292,40 @@ __global__ void __launch_bounds__(CTHREADS)
             }
             phase[s] ^= 1u;
         } else {
-            fill_tile<VT, CTX, CTY, CTZ>(tile, static_cast<const T *>(d.data), d.nx, d.ny, d.nz, bp.x0, bp.y0, bp.z0);
+            cp_async_wait_group<1>();  // this stage's group (the newest is the other stage's)
         }
         __syncthreads();
         if (S.abort) break;
+        // the brick that refills this stage: resolved by thread 0 now, read by
+        // all after the barrier in tile_mixed
+        const long long nb = b + 2 * stride;
+        if (tid == 0 && nb < nbricks) {
+            const int nv = cached_volume(vc, vols, nvol, nb);
+            const BrickPos np = brick_pos(nb - vc.base, vols[nv].nbx, vols[nv].nby);
+            S.nxt = make_int4(nv, vols[nv].tma, np.x0, np.y0);
+            S.nxt_z = np.z0;
+        }
         const bool mixed = tile_mixed<VT>(S, tile);
         if (mixed) {
             classify_brick<VT>(S, tile, d.nx, d.ny, d.nz, bp);
             __syncthreads();  // tile s consumed, red[] complete
         }
+        // tile s is free: refill it
+        if (nb < nbricks) {
+            const int4 nx4 = S.nxt;
+            const int nz0 = S.nxt_z;
+            if (nx4.y) {
+                if (tid == 0) {
+                    mbar_arrive_expect_tx(&S.bars[s], CTILE * Vox<VT>::bytes);
+                    tma_load_3d(S.tiles[s], maps + nx4.x, &S.bars[s], nx4.z, nx4.w, nz0);
+                }
+            } else {
+                const VolDesc &dn = vols[nx4.x];
+                fill_tile<VT, CTX, CTY, CTZ, false>(tile, static_cast<const T *>(dn.data), dn.nx, dn.ny, dn.nz, nx4.z,
+                                                    nx4.w, nz0);
+            }
+        }
+        cp_async_commit();
         if (tid == 0) {
             unsigned int t = 0, o = 0;
             if (mixed) {
@@ -1303,10 +1343,14 @@ __global__ void __launch_bounds__(CTHREADS)
                 atomicAdd(&vol_sums[2 * v + 0], (unsigned long long)t);
                 atomicAdd(&vol_sums[2 * v + 1], (unsigned long long)o);
             }
-            const long long nb = b + 2 * stride;
-            if (nb < nbricks) issue_cls_tile<VT>(S, s, vols, nvol, maps, nb, vc);
+            if (nb < nbricks) {
+                S.svol[s] = S.nxt.x;
+                S.stma[s] = S.nxt.y;
+                S.spos[s] = make_int4(S.nxt.z, S.nxt.w, S.nxt_z, 0);
+            }
         }
     }
+    cp_async_wait_all();
     if (S.abort && tid == 0) {
         atomicOr(flags, 1u);
         for (int s = 0; s < 2; ++s) mbar_wait(&S.bars[s], phase[s], 100000000ull);

@@ -75,6 +75,11 @@ __device__ __forceinline__ void cp_async_16(void *dst, const void *src) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+// close the group of this thread's copies issued since the last commit; wait
+// until at most N of its groups are still in flight
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait_group() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
 // Programmatic dependent launch: a kernel launched with programmatic stream
 // serialisation may start while the kernel before it drains; pdl_wait blocks
