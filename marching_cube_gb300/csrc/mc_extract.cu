@@ -8,31 +8,33 @@
 //
 // Work is organised in bricks of 32x8x8 cubes.
 //
-// Pass 1 (classify) streams the whole volume once.  Persistent CTAs take work
-// items (groups of 2 bricks adjacent in x) from a counter; each item's voxels
-// (68x9x9: the bricks plus a 1-voxel halo, x padded to 16 bytes) arrive by
+// Pass 1 (classify) streams the whole volume once.  Persistent CTAs, four per
+// SM with one tile stage each, take work items (groups of 4 bricks adjacent
+// in x, 2 for float2) from a counter; each item's voxels (132x9x9: the bricks
+// plus the voxels the last cube column and the y / z halo need) arrive by
 // TMA (cp.async.bulk.tensor.3d, completion on an mbarrier that one thread
-// polls with a time bound) into a 2-stage ring.  A tile whose voxels all have
-// one sign is settled by one OR/AND pass; otherwise threads turn its rows
-// into two bit masks per 33 voxels (tsdf < 0, weight == 0) from 16-byte
-// shared-memory loads, and a cube row of 32 cubes is classified with a
-// handful of 64-bit AND/OR operations on four row masks and __popc, so only
-// occupied cubes (a few per mille of a fusion volume) ever look up a table.
-// Output: triangle counts per brick and per-chunk sums.
+// polls with a time bound).  A tile whose in-volume voxels all have one sign
+// is settled by one OR/AND pass; otherwise threads turn its rows into two bit
+// masks per 33 voxels (tsdf < 0, weight == 0) from 16-byte shared-memory
+// loads, and a cube row of 32 cubes is classified with a handful of 64-bit
+// AND/OR operations on four row masks and __popc, so only occupied cubes (a
+// few per mille of a fusion volume) ever look up a table.  Output: triangle
+// counts per brick and per-chunk sums.
 //
 // A multi-CTA scan (one CTA per chunk of 256 bricks) turns brick counts into
-// 64-bit soup offsets and a list of active bricks in brick order.
+// 64-bit soup offsets and a list of active bricks (heaviest classes first).
 //
-// Pass 2 (generate) visits only active bricks (taken from a counter), with a
-// 2-stage TMA prefetch of the brick + halo (36x10x10 voxels).  The same masks
-// give a compact list of occupied cubes with their vertex offsets; each
-// thread then emits one soup vertex (owning cube through a vertex -> cube map
-// or a binary search over the list), computes the fused normal from the tile,
-// and the 28-byte records go out through a per-warp shared-memory stage as
-// full coalesced lines.
+// Pass 2 (generate) visits only active bricks, with a 2-stage TMA prefetch
+// of the brick + halo (36x10x10 voxels).  The same masks give a compact list
+// of occupied cubes with their vertex offsets; each thread then emits one
+// soup vertex (its cube and edge through a vertex map, or a binary search
+// over the list), computes the fused normal from the tile, and the 28-byte
+// records go out through a per-warp shared-memory stage as full coalesced
+// lines.  The three launches chain with programmatic dependent launch.
 //
 // When TMA cannot describe the volume (x row not a multiple of 16 bytes or an
-// unaligned base) the same kernels fill the tiles with plain loads.
+// unaligned base) the same kernels fill the tiles with per-voxel cp.async
+// copies.
 //
 // Output order is deterministic: bricks in (bz, by, bx) order, cubes in
 // (z, y, x) order inside a brick, then the table slot -- the reference's
