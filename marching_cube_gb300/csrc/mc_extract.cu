@@ -70,6 +70,18 @@ constexpr int TXO = 0, TYO = 0, TZO = 0;
 constexpr int TX = BX + 4, TY = BY + 2, TZ = BZ + 2;
 constexpr int GTILE = TX * TY * TZ;
 constexpr int GSTAGES = 2;
+// tile stages and minimum resident CTAs per SM of the single-volume generate
+// launch.  One stage measured faster than two at 4 CTAs/SM (a brick's work
+// hides most of its next tile's load, and the smaller footprint lets the next
+// launch's count CTAs start beside the drained ones); 5 CTAs/SM spill.
+#ifndef MCG_GEN_STAGES
+#define MCG_GEN_STAGES 1
+#endif
+#ifndef MCG_GEN_MINB
+#define MCG_GEN_MINB 4
+#endif
+constexpr int GEN_STAGES = MCG_GEN_STAGES;
+constexpr int GEN_MINB = MCG_GEN_MINB;
 
 // Row masks: bit k of neg / dead = voxel (x0 + k) of a 33-voxel row is
 // negative / has weight 0, k = 0..32.  One thread builds one row from 16-byte
@@ -647,12 +659,12 @@ struct GenParams {
     long long n_grad;
 };
 
-template <int VT>
+template <int VT, int NST = GSTAGES>
 struct GenSmem {
     static constexpr int STAGE_BYTES = pad128(GTILE * Vox<VT>::bytes);
-    unsigned char tiles[GSTAGES][STAGE_BYTES];
+    unsigned char tiles[NST][STAGE_BYTES];
     unsigned long long neg[ROWS], dead[ROWS];
-    uint64_t bars[GSTAGES];
+    uint64_t bars[NST];
     unsigned int stage[WARPS][32 * 7];
     unsigned short occ_cube[BRICK_CUBES];  // local cube index (z*8 + y)*32 + x, in that order
     unsigned short occ_off[BRICK_CUBES];   // exclusive soup-vertex offset inside the brick
@@ -660,9 +672,9 @@ struct GenSmem {
     alignas(16) signed char tri[256][16];  // read a row at a time as 16 bytes
     unsigned char nv[256];
     unsigned short vmap[BRICK_CUBES];      // soup vertex -> local cube << 4 | edge, when the brick has <= 2048
-    long long sbrick[GSTAGES];             // brick id, soup offset and origin of each stage's tile
-    unsigned long long svbase[GSTAGES];
-    int4 spos[GSTAGES];
+    long long sbrick[NST];                 // brick id, soup offset and origin of each stage's tile
+    unsigned long long svbase[NST];
+    int4 spos[NST];
     unsigned long long pipe_v;  // refill pipeline (thread 0): the brick staged at the next
     unsigned int pipe_b;        // refill and its soup offset; pipe_b ~0u = none
     unsigned int wsum[2][2];
@@ -691,8 +703,8 @@ struct GenOut {
 // vertices, and S.vmap (each vertex's cube and edge) when the brick has at
 // most 2048 of them.  Called by
 // every thread (contains __syncthreads); the list is valid after return.
-template <int VT>
-__device__ __forceinline__ void occupied_list(GenSmem<VT> &S, const typename Vox<VT>::T *tile, int nx, int ny, int zlim,
+template <int VT, class Smem>
+__device__ __forceinline__ void occupied_list(Smem &S, const typename Vox<VT>::T *tile, int nx, int ny, int zlim,
                                               int x0, int y0, int z0) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
         // occupied cubes of the brick, from row masks (voxel rows y0..y0+8, z0..z0+8)
@@ -769,8 +781,8 @@ __device__ __forceinline__ void occupied_list(GenSmem<VT> &S, const typename Vox
         }
 }
 
-template <int VT>
-__device__ __forceinline__ void generate_brick(GenSmem<VT> &S, const typename Vox<VT>::T *tile,
+template <int VT, class Smem>
+__device__ __forceinline__ void generate_brick(Smem &S, const typename Vox<VT>::T *tile,
                                                const typename Vox<VT>::T *__restrict__ vol, int nx, int ny,
                                                int nz, float cell, int x0, int y0, int z0,
                                                unsigned long long vbase, const GenOut &o) {
@@ -945,8 +957,8 @@ __device__ __forceinline__ void generate_brick(GenSmem<VT> &S, const typename Vo
 //   dL/df_b += (dL/dP . (p_b - p_a)) *  f_a / D^2
 // accumulated in FP32 with atomics (a voxel is shared by up to 6 edges).
 // Called by every thread (contains __syncthreads).
-template <int VT>
-__device__ __forceinline__ void backward_brick(GenSmem<VT> &S, const typename Vox<VT>::T *tile, int nx, int ny,
+template <int VT, class Smem>
+__device__ __forceinline__ void backward_brick(Smem &S, const typename Vox<VT>::T *tile, int nx, int ny,
                                                int nz, int zlim, float cell, int x0, int y0, int z0,
                                                unsigned long long vbase,
                                                const float *__restrict__ grad_pos, float *__restrict__ grad_f,
@@ -998,11 +1010,11 @@ __device__ __forceinline__ void backward_brick(GenSmem<VT> &S, const typename Vo
 }
 
 template <int VT, bool TMA, int MODE>
-__global__ void __launch_bounds__(THREADS, 4) mc_generate_kernel(const __grid_constant__ CUtensorMap map, GenParams p) {
+__global__ void __launch_bounds__(THREADS, GEN_MINB) mc_generate_kernel(const __grid_constant__ CUtensorMap map, GenParams p) {
     using V = Vox<VT>;
     using T = typename V::T;
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    GenSmem<VT> &S = *reinterpret_cast<GenSmem<VT> *>(smem_raw);
+    GenSmem<VT, GEN_STAGES> &S = *reinterpret_cast<GenSmem<VT, GEN_STAGES> *>(smem_raw);
     const T *__restrict__ vol = static_cast<const T *>(p.vol);
     const int tid = threadIdx.x;
     const int nx = p.nx, ny = p.ny, nz = p.nz;
@@ -1013,7 +1025,7 @@ __global__ void __launch_bounds__(THREADS, 4) mc_generate_kernel(const __grid_co
     if (tid == 0) {
         S.abort = 0;
         if (TMA) {
-            for (int s = 0; s < GSTAGES; ++s) mbar_init(&S.bars[s], 1);
+            for (int s = 0; s < GEN_STAGES; ++s) mbar_init(&S.bars[s], 1);
             fence_barrier_init();
         }
     }
@@ -1032,7 +1044,7 @@ __global__ void __launch_bounds__(THREADS, 4) mc_generate_kernel(const __grid_co
         mbar_arrive_expect_tx(&S.bars[st], GTILE * V::bytes);
         tma_load_3d(S.tiles[st], &map, &S.bars[st], bp.x0 - TXO, bp.y0 - TYO, bp.z0 - TZO);
     };
-    // The first GSTAGES + 1 bricks of each CTA are fixed: round r gives list
+    // The first GEN_STAGES + 1 bricks of each CTA are fixed: round r gives list
     // entry r * grid + c to CTA c, c counted backwards in odd rounds, so the
     // heaviest bricks at the head of the list spread over all CTAs with the
     // heaviest and lightest of adjacent rounds paired.  Later bricks come from
@@ -1053,17 +1065,17 @@ __global__ void __launch_bounds__(THREADS, 4) mc_generate_kernel(const __grid_co
         return k < nfix ? k * grid + ((k & 1) ? grid - 1 - c : c) : tbase + atomicAdd(ticket, 1u);
     };
     unsigned int ptk = 0xffffffffu;  // list entry of the ticket drawn at the top of this brick
-    unsigned int kdraw = GSTAGES + 1;  // entries assigned so far (thread 0)
+    unsigned int kdraw = GEN_STAGES + 1;  // entries assigned so far (thread 0)
     if (TMA && tid == 0) {
-        unsigned int wr[GSTAGES + 1];
+        unsigned int wr[GEN_STAGES + 1];
 #pragma unroll
-        for (unsigned int r = 0; r <= GSTAGES; ++r) wr[r] = next_entry(r);
+        for (unsigned int r = 0; r <= GEN_STAGES; ++r) wr[r] = next_entry(r);
 #pragma unroll
-        for (int r = 0; r < GSTAGES; ++r) {
+        for (int r = 0; r < GEN_STAGES; ++r) {
             const unsigned int w = wr[r];
             stage_brick(r, w < nactive ? (long long)p.active[w] : -1ll, w < nactive ? p.list_vofs[w] : 0ull);
         }
-        const unsigned int w = wr[GSTAGES];
+        const unsigned int w = wr[GEN_STAGES];
         S.pipe_b = 0xffffffffu;
         if (w < nactive) {
             cp_async_4(&S.pipe_b, p.active + w);
@@ -1073,7 +1085,7 @@ __global__ void __launch_bounds__(THREADS, 4) mc_generate_kernel(const __grid_co
     }
     if (TMA) __syncthreads();
     for (int it = 0;; ++it) {
-        const int s = TMA ? it % GSTAGES : 0;
+        const int s = TMA ? it % GEN_STAGES : 0;
         const T *tile = reinterpret_cast<const T *>(S.tiles[s]);
         long long b;
         unsigned long long vbase;
@@ -1084,7 +1096,7 @@ __global__ void __launch_bounds__(THREADS, 4) mc_generate_kernel(const __grid_co
             if (tid == 0) {
                 // the ticket of the refill after the next one (used at this brick's end)
                 if (ptk != 0xffffffffu) ptk = next_entry(kdraw++);
-                if (!mbar_wait(&S.bars[s], (uint32_t)((it / GSTAGES) & 1))) S.abort = 1;
+                if (!mbar_wait(&S.bars[s], (uint32_t)((it / GEN_STAGES) & 1))) S.abort = 1;
             }
             __syncthreads();
             if (S.abort) break;
@@ -1134,12 +1146,13 @@ __global__ void __launch_bounds__(THREADS, 4) mc_generate_kernel(const __grid_co
                 ptk = 0xffffffffu;  // the list is exhausted: draw no more tickets
             }
         }
-        // S.sbrick[s] is next read at the top of iteration it + GSTAGES, after the
-        // barriers of iteration it + 1
+        // S.sbrick[s] is next read at the top of iteration it + GEN_STAGES, after the
+        // barriers of iteration it + 1 (with one stage: after this barrier)
+        if (GEN_STAGES == 1) __syncthreads();
     }
     if (S.abort && tid == 0) {
         atomicOr(&p.totals->flags, 1u);
-        for (int s = 0; s < GSTAGES; ++s) mbar_wait(&S.bars[s], 0, 100000000ull);
+        for (int s = 0; s < GEN_STAGES; ++s) mbar_wait(&S.bars[s], 0, 100000000ull);
     }
     // the last CTA out resets the work counter for the next launch over the
     // same list and reports the flags to the host copy
@@ -1392,7 +1405,7 @@ __global__ void mc_resolve_multi_kernel(const VolDesc *__restrict__ vols, int nv
 }
 
 template <int VT>
-struct GenSmemMulti : GenSmem<VT> {
+struct GenSmemMulti : GenSmem<VT, 2> {
     int svol[2];
     int stma[2];
     alignas(16) BatchBrick pipe;  // entry staged at the next refill (thread 0's pipeline)
@@ -1639,7 +1652,7 @@ void launch_classify_x(bool tma, int G, const CUtensorMap &map, const CUtensorMa
 
 template <int VT, bool TMA, int MODE = 0>
 void launch_generate_t(const CUtensorMap &map, const GenParams &p, const Geometry &g, int sms, cudaStream_t s) {
-    const size_t smem = sizeof(GenSmem<VT>);
+    const size_t smem = sizeof(GenSmem<VT, GEN_STAGES>);
     static int occ = 0;
     if (!occ) occ = occupancy(mc_generate_kernel<VT, TMA, MODE>, THREADS, smem);
     long long grid = (long long)sms * occ;
