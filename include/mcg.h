@@ -117,6 +117,14 @@ mcg_status mcg_mc_generate(mcg_context *ctx, const mcg_volume *vol, const mcg_me
 /* classify + generate in one call, no host synchronisation */
 mcg_status mcg_mc_extract(mcg_context *ctx, const mcg_volume *vol, const mcg_mesh_out *out,
                           mcg_stream_t stream);
+/* Measurement (no counterpart in the reference).  With enable != 0, every
+ * later count phase on ctx records CUDA events on its stream around the
+ * classify kernel alone (not the scan); mcg_mc_count_kernel_ms waits for the
+ * last such pair and gives its duration in milliseconds (MCG_ERR_STATE when
+ * none was recorded).  The events keep the scan from starting while the
+ * classify kernel drains, so leave this off outside measurement. */
+mcg_status mcg_set_kernel_timing(mcg_context *ctx, int32_t enable);
+mcg_status mcg_mc_count_kernel_ms(mcg_context *ctx, float *ms);
 /* Indexed extraction (no counterpart in the reference, whose OBJ writer
  * merges soup vertices by their printed coordinates, kf.cu:3625-3726): one
  * vertex per grid edge the surface crosses, shared by every triangle using

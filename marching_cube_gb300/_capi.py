@@ -66,6 +66,8 @@ SIGNATURES = {
     "mcg_voxel_init": (c_int, [c_void_p, c_void_p, c_int32, c_int64, c_void_p]),
     "mcg_mc_classify": (c_int, [c_void_p, ctypes.POINTER(Volume), c_void_p]),
     "mcg_mc_counts": (c_int, [c_void_p, ctypes.POINTER(MeshCounts)]),
+    "mcg_set_kernel_timing": (c_int, [c_void_p, c_int32]),
+    "mcg_mc_count_kernel_ms": (c_int, [c_void_p, ctypes.POINTER(ctypes.c_float)]),
     "mcg_mc_generate": (c_int, [c_void_p, ctypes.POINTER(Volume), ctypes.POINTER(MeshOut), c_void_p]),
     "mcg_mc_classify_indexed": (c_int, [c_void_p, ctypes.POINTER(Volume), c_void_p]),
     "mcg_mc_generate_indexed": (c_int, [c_void_p, ctypes.POINTER(Volume), ctypes.POINTER(IndexedOut), c_void_p]),

@@ -84,6 +84,8 @@ mcg_status mcg_destroy(mcg_context *ctx) {
     cudaFree(ctx->d_totals);
     if (ctx->h_totals) cudaFreeHost(ctx->h_totals);
     if (ctx->counts_ready) cudaEventDestroy(ctx->counts_ready);
+    if (ctx->tk0) cudaEventDestroy(ctx->tk0);
+    if (ctx->tk1) cudaEventDestroy(ctx->tk1);
     for (int k = 0; k < 2; ++k)
         if (ctx->btab_copied[k]) cudaEventSynchronize(ctx->btab_copied[k]);
     cudaFree(ctx->d_btab);

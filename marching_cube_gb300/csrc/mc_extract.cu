@@ -1666,7 +1666,7 @@ void launch_generate_t(const CUtensorMap &map, const GenParams &p, const Geometr
 long long num_chunks(long long nbricks) { return (nbricks + CHUNK - 1) / CHUNK; }
 
 cudaError_t launch_count_phase(const mcg_volume *vol, const Geometry &g, const Scratch &sc, int sms, cudaStream_t s,
-                               bool clear = true) {
+                               bool clear = true, cudaEvent_t t0 = nullptr, cudaEvent_t t1 = nullptr) {
     // flags and both work counters unless known to be zero; the chunk sums
     // are zero already (the previous scan cleared them)
     cudaError_t e = clear ? cudaMemsetAsync(&sc.totals->flags, 0, 3 * sizeof(unsigned int), s) : cudaSuccess;
@@ -1684,12 +1684,20 @@ cudaError_t launch_count_phase(const mcg_volume *vol, const Geometry &g, const S
         memset(&hmap, 0, sizeof(hmap));
     }
     const bool s2 = vol->voxel_type == MCG_VOXEL_SHORT2;
+    if (t0) {
+        const cudaError_t et = cudaEventRecord(t0, s);
+        if (et != cudaSuccess) return et;
+    }
     if (XH) {
         if (s2) launch_classify_x<MCG_VOXEL_SHORT2, 4>(tma, G, map, hmap, vol, g, sc, sms, s);
         else launch_classify_x<MCG_VOXEL_FLOAT2, 4>(tma, G, map, hmap, vol, g, sc, sms, s);
     } else {
         if (s2) launch_classify_x<MCG_VOXEL_SHORT2, 0>(tma, G, map, hmap, vol, g, sc, sms, s);
         else launch_classify_x<MCG_VOXEL_FLOAT2, 0>(tma, G, map, hmap, vol, g, sc, sms, s);
+    }
+    if (t1) {
+        const cudaError_t et = cudaEventRecord(t1, s);
+        if (et != cudaSuccess) return et;
     }
     launch_pdl(mc_scan_kernel, (unsigned int)num_chunks(g.nbricks), CHUNK, 0, s, (const uint32_t *)sc.tris, sc.chunk,
                (long long)g.nbricks, sc.vofs, sc.active, sc.list_vofs, sc.totals, sc.host);
@@ -1772,7 +1780,14 @@ static mcg_status classify_impl(mcg_context *ctx, const mcg_volume *vol, int32_t
         if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
         ctx->chunk_clean_cap = ctx->brick_occ_cap;
     }
-    e = launch_count_phase(vol, g, ctx_scratch(ctx), ctx->num_sms, s, !ctx->h_totals_dev || !ctx->counters_clean);
+    if (ctx->time_kernels && !ctx->tk0) {
+        e = cudaEventCreate(&ctx->tk0);
+        if (e == cudaSuccess) e = cudaEventCreate(&ctx->tk1);
+        if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
+    }
+    e = launch_count_phase(vol, g, ctx_scratch(ctx), ctx->num_sms, s, !ctx->h_totals_dev || !ctx->counters_clean,
+                           ctx->time_kernels ? ctx->tk0 : nullptr, ctx->time_kernels ? ctx->tk1 : nullptr);
+    if (e == cudaSuccess && ctx->time_kernels) ctx->timed = true;
     ctx->counters_clean = e == cudaSuccess && ctx->h_totals_dev != nullptr;
     if (e == cudaSuccess && !ctx->h_totals_dev)
         e = cudaMemcpyAsync(ctx->h_totals, ctx->d_totals, sizeof(MeshTotals), cudaMemcpyDeviceToHost, s);
@@ -1790,6 +1805,20 @@ static mcg_status classify_impl(mcg_context *ctx, const mcg_volume *vol, int32_t
     ctx->cls_z1 = z1;
     ctx->last_capacity = -1;
     return MCG_OK;
+}
+
+mcg_status mcg_set_kernel_timing(mcg_context *ctx, int32_t enable) {
+    if (!ctx) return MCG_ERR_INVALID_ARG;
+    ctx->time_kernels = enable != 0;
+    return MCG_OK;
+}
+
+mcg_status mcg_mc_count_kernel_ms(mcg_context *ctx, float *ms) {
+    if (!ctx || !ms) return MCG_ERR_INVALID_ARG;
+    if (!ctx->timed) return MCG_ERR_STATE;
+    cudaError_t e = cudaEventSynchronize(ctx->tk1);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(ms, ctx->tk0, ctx->tk1);
+    return e == cudaSuccess ? MCG_OK : mcg_cuda_fail(ctx, e);
 }
 
 mcg_status mcg_mc_classify(mcg_context *ctx, const mcg_volume *vol, mcg_stream_t stream) {

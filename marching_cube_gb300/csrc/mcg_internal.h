@@ -77,6 +77,9 @@ struct mcg_context {
     // h_totals_dev; any other launch over them, or an error, clears this
     bool counters_clean = false;
     cudaEvent_t counts_ready = nullptr;
+    bool time_kernels = false;  // events around the classify kernel (mcg_set_kernel_timing)
+    bool timed = false;         // a pair has been recorded
+    cudaEvent_t tk0 = nullptr, tk1 = nullptr;
     bool counts_pending = false;
 
     // geometry of the last classify (generate must match it)
