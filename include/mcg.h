@@ -184,17 +184,26 @@ mcg_status mcg_mc_extract_batched(mcg_context *ctx, const mcg_volume *vols, cons
  * reserved at start-up, where a stray cudaMalloc can fail or fragment the
  * budget), or a real-time loop that forbids allocation once running
  * (cudaMalloc/cudaFree may synchronise the device and take unbounded time).
- * It takes no context and allocates nothing: its scratch is one static
- * device array of MCG_NOALLOC_SCRATCH_BYTES (about 1.75 MiB) that every
- * device the library is loaded on holds until the process exits.  Volumes
- * with more than MCG_NOALLOC_MAX_BRICKS bricks of 32x8x8 cubes (e.g. larger
- * than 513^3 voxels) are rejected with MCG_ERR_TOO_LARGE.  The first call on
- * a device looks up the array's device address (cudaGetSymbolAddress) with
- * that device current; make that first call before any stream capture.
+ * It takes no context and allocates nothing itself: its scratch is one
+ * static device array of MCG_NOALLOC_SCRATCH_BYTES (about 1.75 MiB), held on
+ * every device that loads the library's extraction code until the process
+ * exits.  CUDA reserves that array (with the code) when it loads the code
+ * onto a device: under lazy module loading (CUDA_MODULE_LOADING=LAZY, the
+ * default) at the first call on that device that uses the extraction
+ * kernels -- often this function's first call -- and at context creation
+ * with CUDA_MODULE_LOADING=EAGER.  So make one call on each device before
+ * device memory is committed to the other allocator or the real-time loop
+ * starts, and before any stream capture.  Volumes with more than
+ * MCG_NOALLOC_MAX_BRICKS bricks of 32x8x8 cubes (e.g. larger than 513^3
+ * voxels) are rejected with MCG_ERR_TOO_LARGE before anything is launched.
+ * Each call looks up the array's device address on the current device
+ * (cudaGetSymbolAddress) and clears the parts of it that must start at zero,
+ * so a call that failed half-way leaves nothing behind for the next one.
  * Every call shares the one array, so calls whose work overlaps on the GPU
  * (other streams, other host threads) race and corrupt each other's
  * results: serialise them.  The call waits for its stream to finish and
- * fills *counts (status MCG_ERR_CAPACITY if the soup was truncated). */
+ * fills *counts (status MCG_ERR_CAPACITY if the soup was truncated: the
+ * records that fit are written, in the order of mcg_mc_extract). */
 #define MCG_NOALLOC_MAX_BRICKS 65536
 #define MCG_NOALLOC_SCRATCH_BYTES (65536 * 28 + 256)
 mcg_status mcg_mc_extract_noalloc(const mcg_volume *vol, const mcg_mesh_out *out,

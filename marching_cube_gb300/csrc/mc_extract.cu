@@ -2235,8 +2235,12 @@ mcg_status mcg_mc_extract_batched(mcg_context *ctx, const mcg_volume *vols, cons
 
 // ---- extraction without any allocation ------------------------------------------
 // For callers that cannot allocate device memory: the scratch of the three
-// passes lives in one file-scope device array of fixed size, reserved when
-// the library is loaded onto a device and held until the process exits.
+// passes lives in one file-scope device array of fixed size.  The array is
+// part of this library's device code: CUDA reserves it when it loads that
+// code onto a device -- at the first use of any kernel of this file on the
+// device under lazy module loading (CUDA_MODULE_LOADING=LAZY, the default),
+// at context creation with CUDA_MODULE_LOADING=EAGER -- and holds it until
+// the process exits.
 namespace mcg {
 namespace {
 
@@ -2256,9 +2260,6 @@ static_assert(kNoAllocBytes == MCG_NOALLOC_SCRATCH_BYTES, "scratch size stated i
 // brick counts, soup offsets, active-brick list and totals of one call
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
-// device address of g_noalloc_scratch per device, taken once with that device current
-unsigned char *g_noalloc_addr[64] = {nullptr};
-
 }  // namespace
 }  // namespace mcg
 
@@ -2271,17 +2272,16 @@ extern "C" mcg_status mcg_mc_extract_noalloc(const mcg_volume *vol, const mcg_me
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess || dev < 0 || dev >= 64) return MCG_ERR_CUDA;
-    // set-up, once per device: the host-side symbol is only a stand-in, the
-    // kernels need the device address of the array
-    if (!g_noalloc_addr[dev]) {
-        void *p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || !p) { cudaGetLastError(); return MCG_ERR_CUDA; }
-        g_noalloc_addr[dev] = static_cast<unsigned char *>(p);
-    }
+    // the host-side symbol is only a stand-in: the kernels need the array's
+    // device address on the current device.  It is looked up on every call
+    // (no allocation once the module is loaded), so a module reloaded after
+    // cudaDeviceReset is never addressed through a stale pointer.
+    void *addr = nullptr;
+    e = cudaGetSymbolAddress(&addr, g_noalloc_scratch);
+    if (e != cudaSuccess || !addr) { cudaGetLastError(); return MCG_ERR_CUDA; }
     e = upload_tables(dev);
     if (e != cudaSuccess) { cudaGetLastError(); return MCG_ERR_CUDA; }
-    unsigned char *base = g_noalloc_addr[dev];
+    unsigned char *base = static_cast<unsigned char *>(addr);
     Scratch sc;
     sc.tris = reinterpret_cast<uint32_t *>(base + kNoAllocTrisOff);
     sc.chunk = reinterpret_cast<uint32_t *>(base + kNoAllocOccOff);  // CHUNK_FIELDS * 256 chunk sums at most
@@ -2294,9 +2294,16 @@ extern "C" mcg_status mcg_mc_extract_noalloc(const mcg_volume *vol, const mcg_me
     e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) { cudaGetLastError(); return MCG_ERR_CUDA; }
     cudaStream_t s = (cudaStream_t)stream;
-    // the timeout flag is cleared by the count phase; every other scratch
-    // entry read later is written first by these launches
-    e = launch_count_phase(vol, g, sc, sms, s);
+    // The count phase accumulates into the chunk sums and draws from the work
+    // counters in the totals, and a completed scan leaves both clear; a call
+    // that stopped between its launches (an error, or a call that overlapped
+    // another) would leave them dirty for every later call.  So each call
+    // clears them itself (memsets, no allocation); every other scratch entry
+    // read later is written first by the launches below.
+    e = cudaMemsetAsync(sc.chunk, 0, sizeof(uint32_t) * CHUNK_FIELDS * num_chunks(g.nbricks), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(sc.totals, 0, sizeof(MeshTotals), s);
+    if (e != cudaSuccess) { cudaGetLastError(); return MCG_ERR_CUDA; }
+    e = launch_count_phase(vol, g, sc, sms, s, false);
     if (e == cudaSuccess) e = launch_generate_phase(vol, g, sc, out, sms, s);
     if (e != cudaSuccess) { cudaGetLastError(); return MCG_ERR_CUDA; }
     // counts: copy the totals out of the array into a host variable and wait

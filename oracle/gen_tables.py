@@ -16,7 +16,7 @@ Both are committed, because the reference tree is not available where the
 code is built for the GPU.  tests/test_tables.py re-derives the checks
 without the reference.
 
-usage:  python oracle/gen_tables.py [path/to/cu_marching_cubes_v1.cu]
+usage:  python oracle/gen_tables.py path/to/cu_marching_cubes_v1.cu
 """
 import hashlib
 import os
@@ -25,7 +25,6 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(HERE)
-DEFAULT_SRC = "/root/reference/cu_marching_cubes_v1.cu"
 
 # corner pairs of the 12 cube edges, in the reference's vertlist order
 # (cu_marching_cubes_v1.cu:304-315)
@@ -133,7 +132,9 @@ def render(edge, tri, nv, prefix):
 
 
 def main(argv):
-    src = argv[1] if len(argv) > 1 else DEFAULT_SRC
+    if len(argv) != 2:
+        raise SystemExit("usage: python oracle/gen_tables.py path/to/cu_marching_cubes_v1.cu")
+    src = argv[1]
     with open(src, "r", encoding="latin-1") as f:
         text = f.read()
     edge, tri, nv = parse(text)
