@@ -135,16 +135,24 @@ class Clocks:
 # ---------------------------------------------------------------------------
 # workload construction
 # ---------------------------------------------------------------------------
-def build_volume(mcg, synthetic, torch, n, frames, seed=0):
+def fusion_frames(synthetic, frames, seed=0, device="cuda"):
+    """The fusion workload's depth frames: yields (R, t, depth) per frame,
+    R, t the camera -> volume pose of an orbit at 1.5 m around the 3 m
+    cube's centre and depth the [H][W] int16 tensor holding the uint16
+    millimetre image (ray-cast scene + N(0, 2 mm), seeded)."""
     scene = synthetic.FusionScene(seed=seed, extent=EXTENT)
+    for i in range(frames):
+        R, t = scene.pose(i, frames)
+        mm = scene.depth_frame(R, t, w=W, h=H, fx=FX, fy=FY, cx=CX, cy=CY, seed=seed * 1000 + i, device=device)
+        yield R, t, synthetic.mm_to_u16_bits(mm)
+
+
+def build_volume(mcg, synthetic, torch, n, frames, seed=0):
     v = mcg.voxel_new((n, n, n), TRUNC, TRUNC, EXTENT / n)
     k = mcg.intrinsic(FX, FY, CX, CY)
     t_int = 0.0
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    for i in range(frames):
-        R, t = scene.pose(i, frames)
-        mm = scene.depth_frame(R, t, w=W, h=H, fx=FX, fy=FY, cx=CX, cy=CY, seed=seed * 1000 + i, device="cuda")
-        d = synthetic.mm_to_u16_bits(mm)
+    for R, t, d in fusion_frames(synthetic, frames, seed):
         ev0.record()
         m, _, _ = mcg.depth_to_maps(d, k, vertex=False, normal=False)
         mcg.volumetric_integration(v, k, mcg.extrinsic(R, t), m)
@@ -155,25 +163,87 @@ def build_volume(mcg, synthetic, torch, n, frames, seed=0):
                "integrate_ms_per_frame": 1e3 * t_int / max(frames, 1)}
 
 
-def cpu_baseline(orc, vol_np, cell, target_s=8.0):
-    """Oracle (FP32 mirror) extraction of the same volume on all host threads,
-    repeated until about target_s seconds of CPU work; Gvoxels/s."""
-    nthreads = orc.max_threads()
-    vox = vol_np.shape[0] * vol_np.shape[1] * vol_np.shape[2]
+def host_cores():
+    """(cores this process may run on, cores the host reports, machine)."""
+    import platform
+    try:
+        usable = len(os.sched_getaffinity(0))
+    except AttributeError:  # pragma: no cover
+        usable = os.cpu_count() or 1
+    return usable, os.cpu_count() or usable, platform.machine()
+
+
+def _time_cpu_extract(orc, vol_np, cell, nthreads, target_s, max_runs=50):
     times = []
     t_all = time.perf_counter()
     ntri = 0
-    while not times or (time.perf_counter() - t_all < target_s and len(times) < 50):
+    while not times or (time.perf_counter() - t_all < target_s and len(times) < max_runs):
         t0 = time.perf_counter()
         out = orc.mc_extract(vol_np, cell, normals=True, vi2vox=False, ver_voxel=False, tri_cube=False,
                              nthreads=nthreads)
         times.append(time.perf_counter() - t0)
         ntri = len(out["soup"]) // 3
-    dt = float(np.median(times))
+    return float(np.median(times)), len(times), ntri
+
+
+def cpu_baseline(orc, vol_np, cell, target_s=8.0):
+    """Oracle (FP32 mirror) extraction of the same volume on all host threads
+    (OpenMP over z-slabs), repeated for about target_s seconds of CPU work,
+    and on one thread; Gvoxels/s."""
+    nthreads = orc.max_threads()
+    usable, nproc, machine = host_cores()
+    vox = vol_np.shape[0] * vol_np.shape[1] * vol_np.shape[2]
+    dt, runs, ntri = _time_cpu_extract(orc, vol_np, cell, nthreads, target_s)
+    dt1, runs1, _ = _time_cpu_extract(orc, vol_np, cell, 1, target_s / 2, max_runs=5)
+    shape = "x".join(map(str, vol_np.shape[:3]))
     return {"value": vox / dt / 1e9, "unit": UNIT, "cores": nthreads, "kind": "port",
             "sample": "oracle FP32-mirror extraction (classify+scan+generate+normals) of the whole %s volume, "
-                      "%d triangles, median of %d runs (%.3f s each)" % ("x".join(map(str, vol_np.shape[:3])),
-                                                                         ntri, len(times), dt)}
+                      "%d triangles, median of %d runs (%.3f s each) on %d threads" % (shape, ntri, runs, dt,
+                                                                                   nthreads),
+            "single_thread": {"value": vox / dt1 / 1e9, "unit": UNIT, "cores": 1,
+                              "sample": "the same extraction on one thread, median of %d runs (%.3f s each)"
+                                        % (runs1, dt1)},
+            "host": {"nproc": nproc, "usable_cores": usable, "machine": machine}}
+
+
+def bench_full_outputs(mcg, torch, lib, ctx, vol, cell, nvert, stream, steps=50):
+    """One step with every output of the reference's MarchingCubes::run
+    (cu_marching_cubes_v1.cu:416-467): soup, vertexindex_to_voxel (vi2vox)
+    and the volume-sized ver_voxel (cleared, then scattered), plus the
+    normals its driver computes next -- beside the headline step, which
+    writes soup + normals only."""
+    import ctypes
+    from marching_cube_gb300 import _capi
+    nz, ny, nx = (int(x) for x in vol.shape[:3])
+    soup = torch.empty((nvert, 28), dtype=torch.uint8, device="cuda")
+    nrm = torch.empty((nvert, 3), dtype=torch.float32, device="cuda")
+    v2v = torch.empty((nvert, 3), dtype=torch.int32, device="cuda")
+    vv = torch.empty((nz, ny, nx), dtype=torch.int16, device="cuda")
+    cv = _capi.Volume(vol.data_ptr(), nx, ny, nz, 0, float(cell))
+    mo = _capi.MeshOut(soup.data_ptr(), nrm.data_ptr(), v2v.data_ptr(), vv.data_ptr(), None, nvert)
+    s = ctypes.c_void_p(stream.cuda_stream)
+
+    def step():
+        ctx.check(lib.mcg_mc_classify(ctx.handle, ctypes.byref(cv), s), "classify")
+        ctx.check(lib.mcg_mc_generate(ctx.handle, ctypes.byref(cv), ctypes.byref(mo), s), "generate")
+
+    for _ in range(3):
+        step()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    c = mcg.counts(ctx)
+    assert c["status"] == 0 and c["vertices"] == nvert
+    ms = e0.elapsed_time(e1) / steps
+    vox = nx * ny * nz
+    del soup, nrm, v2v, vv
+    return {"outputs": "soup+normals+vi2vox+ver_voxel (the reference run()'s full set)", "steps": steps,
+            "ms_per_step": ms, "gvoxels_per_s": vox / (ms * 1e-3) / 1e9,
+            "bytes_out_per_step": nvert * (28 + 12 + 12) + 2 * vox * 2}
 
 
 def bench_batched(mcg, synthetic, torch, ctx, n=64, reps=10):
@@ -682,43 +752,90 @@ def bench_adjoint(mcg, synthetic, torch, n=256, frames=10, reps=5):
             "precision": "fp32 accumulate (atomics)"}
 
 
+def headline_config(n, frames, **extra):
+    """The config dict both arms print for the headline workload."""
+    cfg = {"workload": "mc_extract_512_fusion", "volume": [n, n, n], "voxel": "short2",
+           "frames_integrated": frames, "outputs": "soup(vertex_voxel)+normals", "l2": "inputs larger than L2"}
+    cfg.update(extra)
+    return cfg
+
+
+def oracle_volume(orc, synthetic, torch, n, frames, seed=0):
+    """The headline volume built without this library: the same depth frames
+    (drawn by torch, on the GPU when there is one, like the GPU arm's), turned
+    into metres and integrated by the oracle on the host cores."""
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    vol = orc.voxel_init(n ** 3).reshape(n, n, n, 2)
+    ko = orc.intrinsic(FX, FY, CX, CY)
+    for R, t, d in fusion_frames(synthetic, frames, seed, device=dev):
+        mo = orc.depth_to_meter(d.cpu().numpy().view(np.uint16))
+        orc.integrate(vol, TRUNC, TRUNC, EXTENT / n, ko, orc.extrinsic(R, t), mo)
+    return vol
+
+
+def summarize(line):
+    """A compact digest of the line's sections (None where a section did not run)."""
+    def get(*path):
+        x = line
+        for k in path:
+            if not isinstance(x, dict) or x.get(k) is None:
+                return None
+            x = x[k]
+        return round(x, 4) if isinstance(x, float) else x
+    return {
+        "headline_gvoxels_per_s": get("value"), "ms_per_step": get("ms_per_step"),
+        "whole_step_frac": get("roofline", "whole_step", "frac"),
+        "e2e_gvoxels_per_s": get("e2e", "value"),
+        "full_outputs_ms": get("full_outputs", "ms_per_step"),
+        "batched_speedup": get("batched", "speedup"), "batched_ms": get("batched", "batched_ms"),
+        "loop_ms": get("batched", "loop_ms"),
+        "adjoint_over_forward": get("adjoint", "path_adjoint_over_forward"),
+        "integrate_ms_per_frame": get("integrate", "integrate_ms_per_frame"),
+        "indexed_ms": get("indexed", "ms"), "stress_gvoxels_per_s": get("stress", "extract_gvoxels_per_s"),
+        "raycast_ms": get("raycast", "ms_per_frame"),
+        "cpu_gvoxels_per_s": get("cpu_baseline", "value"),
+        "cpu_1thread_gvoxels_per_s": get("cpu_baseline", "single_thread", "value"),
+        "cpu_cores": get("cpu_baseline", "cores"),
+    }
+
+
 def run_reference(args):
     """--impl reference: the reference has no CPU marching cubes (MyMarchingCube.h
-    is a declaration only); its algorithm restated in C (oracle/) runs on all
-    host cores over bounded samples of the same workload."""
+    is a declaration only) and its GPU code cannot be built with this CUDA;
+    its algorithm restated in C (oracle/) runs on all host cores, over the
+    same volume (integrated by the oracle from the same frames)."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
     import torch
     import oracle as orc
-    import marching_cube_gb300 as mcg
     from marching_cube_gb300 import synthetic
     orc.build()
-    cfg = {"workload": "mc_extract_512_fusion", "volume": [args.n] * 3, "voxel": "short2",
-           "outputs": "soup+normals", "frames_integrated": args.frames}
-    if torch.cuda.is_available():
-        v, _ = build_volume(mcg, synthetic, torch, args.n, args.frames)
-        vol_np = v.data.cpu().numpy()
-        cell = v.grid_s
-    else:
-        vol_np = synthetic.sphere_volume(args.n, radius=args.n * 0.3, trunc=5.0)
-        cell = EXTENT / args.n
+    vol_np = oracle_volume(orc, synthetic, torch, args.n, args.frames)
+    cell = EXTENT / args.n
     nthreads = orc.max_threads()
+    usable, nproc, machine = host_cores()
     vals = []
     vox = vol_np.shape[0] * vol_np.shape[1] * vol_np.shape[2]
+    ntri = 0
     for i in range(args.warmup + args.steps):
         t0 = time.perf_counter()
-        orc.mc_extract(vol_np, cell, normals=True, vi2vox=False, ver_voxel=False, tri_cube=False, nthreads=nthreads)
+        out = orc.mc_extract(vol_np, cell, normals=True, vi2vox=False, ver_voxel=False, tri_cube=False,
+                             nthreads=nthreads)
         dt = time.perf_counter() - t0
+        ntri = len(out["soup"]) // 3
         if i >= args.warmup:
             vals.append(vox / dt / 1e9)
     value = float(np.median(vals))
+    cfg = headline_config(args.n, args.frames, triangles=ntri, parallelism="single")
     line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": cfg,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": vox / value / 1e6,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int16",
+            "data": "synthetic", "config": cfg,
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
                              "sample": "each step: oracle extraction (classify+scan+generate+normals) of the "
-                                       "whole volume on all host threads"},
+                                       "whole volume on all %d host threads" % nthreads,
+                             "host": {"nproc": nproc, "usable_cores": usable, "machine": machine}},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -812,6 +929,8 @@ def main():
     cls_kernel_ms = float(np.mean(kms))
     c = mcg.counts(ctx)
     assert c["status"] == 0 and c["vertices"] == nvert
+    full_outputs = bench_full_outputs(mcg, torch, lib, ctx, v.data, cell, nvert, stream,
+                                      steps=min(args.steps, 50))
     if world > 1:
         tt = torch.tensor([total_ms], device="cuda")
         torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
@@ -988,13 +1107,13 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int16", "data": "synthetic",
-        "config": {"workload": "mc_extract_512_fusion", "volume": [n, n, n], "voxel": "short2",
-                   "frames_integrated": args.frames, "outputs": "soup(vertex_voxel)+normals",
-                   "triangles": ntri, "occupied_cubes": counts["occupied"], "l2": "inputs larger than L2",
-                   "parallelism": "replicas" if world > 1 else "single"},
+        "config": headline_config(n, args.frames, triangles=ntri,
+                                  parallelism="replicas" if world > 1 else "single"),
+        "occupied_cubes": counts["occupied"],
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
         "clocks": clk.summary(), "gpu_launches": 3 * args.steps,
         "triangles_per_s": ntri * world / (ms_per_step * 1e-3),
+        "full_outputs": full_outputs,
         "integrate": integ,
         "batched": batched,
         "graph": graph,
@@ -1006,6 +1125,9 @@ def main():
         "icp": icp,
         "stress": stress,
     }
+    # the figures of the other workloads again, compact and last, so that a
+    # reader of the end of the line sees them
+    line["summary"] = summarize(line)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

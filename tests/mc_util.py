@@ -10,6 +10,13 @@ def gpu_extract(mcg, vol_np, cell, canonical=True, **kw):
     vol = torch.from_numpy(np.ascontiguousarray(vol_np)).cuda()
     mesh = mcg.extract(vol, cell, soup=True, normals=True, vi2vox=True, ver_voxel=True, tri_cube=True, **kw)
     torch.cuda.synchronize()
+    return mesh_arrays(mesh, canonical)
+
+
+def mesh_arrays(mesh, canonical=True):
+    """A mesh with every output (soup, normals, vi2vox, ver_voxel, tri_cube)
+    as numpy arrays, triangles in the oracle's canonical order (by cube id,
+    stable) when `canonical`."""
     n = mesh.num_vertices
     soup = mesh.soup.cpu().numpy().reshape(-1).view(VERTEX_DTYPE) if n else np.zeros(0, VERTEX_DTYPE)
     nrm = mesh.normals.cpu().numpy() if n else np.zeros((0, 3), np.float32)
