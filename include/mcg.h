@@ -114,15 +114,44 @@ mcg_status mcg_mc_counts(mcg_context *ctx, mcg_mesh_counts *out);
  * mcg_mc_counts reports MCG_ERR_CAPACITY with the full size. */
 mcg_status mcg_mc_generate(mcg_context *ctx, const mcg_volume *vol, const mcg_mesh_out *out,
                            mcg_stream_t stream);
-/* classify + generate in one call, no host synchronisation */
+/* MarchingCubes::run (mc.cu:416-467) in one call, no host synchronisation:
+ * the same soup, side outputs, order and counts as mcg_mc_classify +
+ * mcg_mc_generate.  For short2 volumes of at least 132 x 10 x 10 voxels that
+ * TMA can describe it runs as one fused launch (count, offsets and
+ * generation together, mcg_mc_config.fused); the counts are then readable
+ * through mcg_mc_counts, but the count phase's brick list is not kept, so
+ * mcg_mc_generate / mcg_mc_backward on this ctx need a mcg_mc_classify first
+ * (MCG_ERR_STATE otherwise).  Other volumes take the two launches. */
 mcg_status mcg_mc_extract(mcg_context *ctx, const mcg_volume *vol, const mcg_mesh_out *out,
                           mcg_stream_t stream);
+/* Launch configuration of the marching-cubes kernels on a context (no
+ * counterpart in the reference; the reference's launch shapes are fixed).
+ * Defaults are the measured best on GB300; the autotuner
+ * (marching_cube_gb300.tune) times the choices on a volume and sets them.
+ *   fused            1: mcg_mc_extract uses the fused launch where it applies,
+ *                    0: always the count + generate launches
+ *   classify_shape   count-pass work item, 0..5: 2 bricks in a 68-voxel box,
+ *                    2 stages (0); 4 bricks with a separate halo box, 2
+ *                    stages (1) or 4 stages of 512 threads (2); 4 bricks in a
+ *                    132-voxel box, 2 stages (3) or 1 stage (4); 2 bricks in a
+ *                    68-voxel box, 1 stage (5) -- all 256 threads unless said
+ *   gen_fixed_rounds generate: bricks each CTA takes in fixed serpentine
+ *                    rounds before drawing from the counter, 0..16 */
+typedef struct mcg_mc_config {
+    int32_t fused;
+    int32_t classify_shape;
+    int32_t gen_fixed_rounds;
+    int32_t reserved;
+} mcg_mc_config;
+mcg_status mcg_mc_get_config(const mcg_context *ctx, mcg_mc_config *cfg);
+mcg_status mcg_mc_set_config(mcg_context *ctx, const mcg_mc_config *cfg);
 /* Measurement (no counterpart in the reference).  With enable != 0, every
  * later count phase on ctx records CUDA events on its stream around the
- * classify kernel alone (not the scan); mcg_mc_count_kernel_ms waits for the
- * last such pair and gives its duration in milliseconds (MCG_ERR_STATE when
- * none was recorded).  The events keep the scan from starting while the
- * classify kernel drains, so leave this off outside measurement. */
+ * classify kernel alone (not the scan), and every fused mcg_mc_extract around
+ * its one kernel; mcg_mc_count_kernel_ms waits for the last such pair and
+ * gives its duration in milliseconds (MCG_ERR_STATE when none was recorded).
+ * The events keep the next launch from starting while the kernel drains, so
+ * leave this off outside measurement. */
 mcg_status mcg_set_kernel_timing(mcg_context *ctx, int32_t enable);
 mcg_status mcg_mc_count_kernel_ms(mcg_context *ctx, float *ms);
 /* Indexed extraction (no counterpart in the reference, whose OBJ writer

@@ -96,6 +96,24 @@ class Context:
         if st != MCG_OK:
             raise MCGError(st, what, _lib.mcg_last_cuda_error(self._h))
 
+    @property
+    def config(self):
+        """The marching-cubes launch configuration (mcg_mc_config) as a dict:
+        fused, classify_shape, gen_fixed_rounds."""
+        c = _capi.McConfig()
+        self.check(_lib.mcg_mc_get_config(self._h, ctypes.byref(c)), "mcg_mc_get_config")
+        return {"fused": c.fused, "classify_shape": c.classify_shape, "gen_fixed_rounds": c.gen_fixed_rounds}
+
+    def set_config(self, **kw):
+        """Changes fields of the launch configuration (the others stay)."""
+        cur = self.config
+        unknown = set(kw) - set(cur)
+        if unknown:
+            raise KeyError("unknown configuration fields: %s" % sorted(unknown))
+        cur.update(kw)
+        c = _capi.McConfig(int(cur["fused"]), int(cur["classify_shape"]), int(cur["gen_fixed_rounds"]), 0)
+        self.check(_lib.mcg_mc_set_config(self._h, ctypes.byref(c)), "mcg_mc_set_config")
+
     def close(self):
         if getattr(self, "_h", None):
             _lib.mcg_destroy(self._h)

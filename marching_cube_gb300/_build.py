@@ -25,6 +25,9 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # without contraction, bit-identical to the CPU restatement.
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
                      "-Xcompiler", "-O2", "-I" + INCLUDE, "-I" + CSRC]
+# build-time tuning macros (e.g. "-DMCG_GEN_MINB=3"), for measuring other
+# configurations of the kernels than the defaults
+NVCC_FLAGS += os.environ.get("MCG_NVCC_DEFINES", "").split()
 
 
 def nvcc():

@@ -37,6 +37,11 @@ class MeshCounts(ctypes.Structure):
                 ("active_bricks", c_int64), ("status", c_int32), ("reserved", c_int32)]
 
 
+class McConfig(ctypes.Structure):
+    _fields_ = [("fused", c_int32), ("classify_shape", c_int32), ("gen_fixed_rounds", c_int32),
+                ("reserved", c_int32)]
+
+
 class TextInfo(ctypes.Structure):
     _fields_ = [("bytes", c_int64), ("numbers", c_int64), ("records", c_int64), ("stored", c_int64),
                 ("fail_offset", c_int64), ("filled_rest", c_int32), ("reserved", c_int32)]
@@ -73,6 +78,8 @@ SIGNATURES = {
     "mcg_mc_generate_indexed": (c_int, [c_void_p, ctypes.POINTER(Volume), ctypes.POINTER(IndexedOut), c_void_p]),
     "mcg_mc_extract_indexed": (c_int, [c_void_p, ctypes.POINTER(Volume), ctypes.POINTER(IndexedOut), c_void_p]),
     "mcg_mc_classify_slab": (c_int, [c_void_p, ctypes.POINTER(Volume), c_int32, c_int32, c_void_p]),
+    "mcg_mc_get_config": (c_int, [c_void_p, ctypes.POINTER(McConfig)]),
+    "mcg_mc_set_config": (c_int, [c_void_p, ctypes.POINTER(McConfig)]),
     "mcg_mc_extract_slab": (c_int, [c_void_p, ctypes.POINTER(Volume), c_int32, c_int32, ctypes.POINTER(MeshOut),
                                     c_void_p]),
     "mcg_mc_extract": (c_int, [c_void_p, ctypes.POINTER(Volume), ctypes.POINTER(MeshOut), c_void_p]),

@@ -81,6 +81,8 @@ mcg_status mcg_destroy(mcg_context *ctx) {
     cudaFree(ctx->brick_uniq);
     cudaFree(ctx->brick_uofs);
     cudaFree(ctx->edge_map);
+    cudaFree(ctx->fx_item);
+    cudaFree(ctx->fx_group);
     cudaFree(ctx->d_totals);
     if (ctx->h_totals) cudaFreeHost(ctx->h_totals);
     if (ctx->counts_ready) cudaEventDestroy(ctx->counts_ready);

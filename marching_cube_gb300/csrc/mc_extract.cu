@@ -1171,6 +1171,542 @@ __global__ void __launch_bounds__(THREADS, GEN_MINB) mc_generate_kernel(const __
 }
 
 
+// ---- fused extraction: count, offsets and generation in one persistent launch ----
+// The count pass already holds every brick's voxels in shared memory and has
+// classified its cubes; the fused kernel generates a work item's triangles
+// right there, instead of a scan launch and a generate launch that fetch the
+// active bricks again and rebuild their occupied-cube lists.  A work item is
+// FG bricks adjacent in x; its tile holds their voxels plus one voxel column
+// and one row / plane of y / z halo beyond what the cubes need, because the
+// normals sample one voxel further (cu_kinect_fusion_v1.cu:3152-3194).
+//
+// Soup offsets come from a decoupled look-back over the items in ticket
+// order, at two levels.  An item publishes its triangle count as soon as it
+// is classified.  Items form groups of FGROUP; the last item of a group sums
+// the group's counts and publishes that aggregate, then looks back over the
+// groups before it and publishes the group's inclusive prefix.  An item that
+// emits triangles sums the counts before it in its own group and looks back
+// over the groups before: a warp reads the states of 32 groups at once, the
+// nearest inclusive prefix ends the walk and the aggregates after it are
+// added.  Items are drawn in order by running CTAs, and neither a count nor
+// an aggregate waits for anything but earlier items, so every wait ends
+// (each is bounded by %globaltimer all the same).  The output order is the
+// one of the two-launch path: bricks in (bz, by, bx) order, cubes in (z, y, x)
+// order inside a brick, table slot order inside a cube.
+constexpr int FG = 4;                        // bricks per item
+constexpr int FTX = BX * FG + 4;             // 132 voxels in x
+constexpr int FTY = BY + 2, FTZ = BZ + 2;    // 10 x 10 rows
+constexpr int FTILE = FTX * FTY * FTZ;
+constexpr int FROWS = FG * CUBE_ROWS;        // 256 cube rows per item, one per thread
+constexpr int FGROUP = 32;                   // items per look-back group
+static_assert(FROWS == THREADS, "one thread per cube row of an item");
+
+template <int VT>
+struct FusedSmem {
+    static constexpr int TILE_BYTES = pad128(FTILE * Vox<VT>::bytes);
+    unsigned char tile[TILE_BYTES];
+    unsigned long long neg[FG * ROWS];           // row masks of the item's bricks, [brick][row]
+    union {
+        unsigned long long dead[FG * ROWS];      // classification only
+        unsigned int stage[WARPS][32 * 7];       // emission only: per-warp store staging
+    };
+    unsigned int rowocc[FROWS];                  // occupied cubes of each cube row (bit x)
+    unsigned int rownib[FROWS][4];               // soup vertices of each cube of the row, 4 bits each
+    unsigned int rowoff[FROWS + 1];              // exclusive vertex offset of each row in the item; [FROWS]: total
+    alignas(16) signed char tri[256][16];
+    unsigned char nv[256];
+    uint64_t bar;
+    int4 sorg;                                   // item origin {x0, y0, z0, first brick x}; x0 < 0: none
+    int sitem;                                   // item number
+    unsigned long long base;                     // soup offset (vertices) of the item
+    unsigned int wsum[WARPS];
+    unsigned int red[WARPS];
+    unsigned int mix[WARPS];
+    int abort;
+};
+
+struct FusedParams {
+    const void *vol;
+    int nx, ny, nz;
+    float cell;
+    int nbx, nby;
+    int nitems, ngx, zlim;
+    unsigned long long *item;   // per item: epoch << 32 | (triangles + 1)
+    unsigned long long *group;  // per group of FGROUP items: group_word(epoch, kind, value)
+    unsigned int epoch;         // 1 .. 2^22 - 1
+    MeshTotals *totals;
+    MeshTotals *host;           // mapped host copy, or null
+    GenOut out;
+};
+
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long *p) {
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_relaxed_u64(unsigned long long *p, unsigned long long v) {
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+// Triangle count of item j of this launch, waiting (bounded) until it is
+// published; false on timeout.
+__device__ __forceinline__ bool item_count(const FusedParams &p, int j, unsigned int &tris) {
+    const unsigned long long *q = p.item + j;
+    unsigned long long v = ld_relaxed_u64(q);
+    if ((unsigned int)(v >> 32) != p.epoch) {
+        const unsigned long long t0 = globaltimer_ns();
+        do {
+            if (globaltimer_ns() - t0 > kWaitLimitNs) return false;
+            v = ld_relaxed_u64(q);
+        } while ((unsigned int)(v >> 32) != p.epoch);
+    }
+    tris = (unsigned int)v - 1u;
+    return true;
+}
+
+// Group state word: epoch << 42 | kind << 40 | value, kind 1 = the group's
+// triangle total (aggregate), 2 = the inclusive prefix through the group.
+constexpr int FX_EPOCH_BITS = 22;
+constexpr unsigned long long FX_VALUE_MASK = (1ull << 40) - 1ull;
+__device__ __forceinline__ unsigned long long group_word(unsigned int epoch, unsigned int kind,
+                                                         unsigned long long value) {
+    return ((unsigned long long)epoch << 42) | ((unsigned long long)kind << 40) | (value & FX_VALUE_MASK);
+}
+
+// State of group h once it holds at least its aggregate (bounded wait);
+// false on timeout.
+__device__ __forceinline__ bool group_state(const FusedParams &p, int h, unsigned int &kind,
+                                            unsigned long long &value) {
+    const unsigned long long *q = p.group + h;
+    unsigned long long v = ld_relaxed_u64(q);
+    if ((unsigned int)(v >> 42) != p.epoch) {
+        const unsigned long long t0 = globaltimer_ns();
+        do {
+            if (globaltimer_ns() - t0 > kWaitLimitNs) return false;
+            v = ld_relaxed_u64(q);
+        } while ((unsigned int)(v >> 42) != p.epoch);
+    }
+    kind = (unsigned int)(v >> 40) & 3u;
+    value = v & FX_VALUE_MASK;
+    return true;
+}
+
+// Triangles of all groups before group g (called by one whole warp): windows
+// of 32 groups, one per lane; the nearest group holding an inclusive prefix
+// ends the walk, the aggregates of the groups after it are added.  False on
+// a timeout.
+__device__ bool groups_before(const FusedParams &p, int g, unsigned long long &sum) {
+    const int lane = threadIdx.x & 31;
+    bool ok = true;
+    sum = 0;
+    for (int h = g - 1; h >= 0; h -= 32) {
+        const int hh = h - lane;
+        unsigned int kind = 2;  // before group 0: an inclusive prefix of 0
+        unsigned long long val = 0;
+        if (hh >= 0) ok = group_state(p, hh, kind, val) && ok;
+        const unsigned int pref = __ballot_sync(0xffffffffu, kind == 2u || !ok);
+        unsigned long long a = (pref == 0u || lane <= __ffs(pref) - 1) ? val : 0ull;
+#pragma unroll
+        for (int o = 16; o; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+        sum += a;
+        if (pref) break;
+    }
+    return __all_sync(0xffffffffu, ok);
+}
+
+// Triangles of the items of `it`'s group that come before it (one whole warp).
+__device__ bool items_before(const FusedParams &p, int it, unsigned long long &sum) {
+    const int lane = threadIdx.x & 31;
+    const int first = (it / FGROUP) * FGROUP;
+    bool ok = true;
+    unsigned long long v = 0;
+    if (lane < it - first) {
+        unsigned int t = 0;
+        ok = item_count(p, first + lane, t);
+        v = t;
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    sum = v;
+    return __all_sync(0xffffffffu, ok);
+}
+
+// 16-byte words of the item's classification region (voxel rows y0 .. y0+8,
+// z0 .. z0+8) that lie inside the volume hold both signs; contains a barrier.
+template <int VT, class Smem>
+__device__ __forceinline__ bool fused_mixed(Smem &S, const typename Vox<VT>::T *tile, int nx, int ny, int nz,
+                                            int x0, int y0, int z0) {
+    using V = Vox<VT>;
+    constexpr int WPR = FTX * V::bytes / 16;  // 16-byte words per row
+    constexpr int VPW = 16 / V::bytes;
+    const uint4 *q = reinterpret_cast<const uint4 *>(tile);
+    const int ry = ny - y0, rz = nz - z0, rx = nx - x0;
+    unsigned int neg_any = 0, pos_any = 0;
+    for (int i = threadIdx.x; i < WPR * ROWS; i += THREADS) {
+        const int r = i / WPR, w = i - r * WPR, lx = w * VPW;
+        const int lz = r / CTY, ly = r - lz * CTY;  // rows 0..8 of planes 0..8
+        if (ly >= ry || lz >= rz || lx >= rx) continue;
+        const uint4 v = q[(lz * FTY + ly) * WPR + w];
+        if (VT == MCG_VOXEL_SHORT2) {
+            neg_any |= v.x | v.y | v.z | v.w;
+            pos_any |= ~(v.x & v.y & v.z & v.w);
+        } else {
+            const bool n0 = __uint_as_float(v.x) < 0.f, n1 = __uint_as_float(v.z) < 0.f;
+            neg_any |= (unsigned int)(n0 | n1) << 15;
+            pos_any |= (unsigned int)(!n0 | !n1) << 15;
+        }
+    }
+    neg_any = __reduce_or_sync(0xffffffffu, neg_any & 0x8000u);
+    pos_any = __reduce_or_sync(0xffffffffu, pos_any & 0x8000u);
+    if ((threadIdx.x & 31) == 0) S.mix[threadIdx.x >> 5] = (neg_any ? 1u : 0u) | (pos_any ? 2u : 0u);
+    __syncthreads();
+    unsigned int m = 0;
+#pragma unroll
+    for (int w = 0; w < WARPS; ++w) m |= S.mix[w];
+    return m == 3u;
+}
+
+__device__ __forceinline__ int ftidx(int lx, int ly, int lz) { return (lz * FTY + ly) * FTX + lx; }
+
+template <int VT>
+__global__ void __launch_bounds__(THREADS, 3) mc_fused_kernel(const __grid_constant__ CUtensorMap map, FusedParams p) {
+    using V = Vox<VT>;
+    using T = typename V::T;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    FusedSmem<VT> &S = *reinterpret_cast<FusedSmem<VT> *>(smem_raw);
+    const T *__restrict__ vol = static_cast<const T *>(p.vol);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nx = p.nx, ny = p.ny, nz = p.nz;
+    const float cell = p.cell;
+    const GenOut &o = p.out;
+    const long long N = (long long)nx * ny * nz;
+    for (int i = tid; i < 256 * 16; i += THREADS) (&S.tri[0][0])[i] = (&c_tri[0][0])[i];
+    S.nv[tid] = (tid == 0 || tid == 255) ? 0 : c_nverts[tid];
+    pdl_wait();  // the launch before (a writer of the volume or of the counters)
+    unsigned int *ticket = &p.totals->cls_ticket;
+    // thread 0: item -> origin and TMA load of its tile
+    auto stage_item = [&](int it) {
+        S.sitem = it;
+        if (it < 0) {
+            S.sorg = make_int4(-1, 0, 0, 0);
+            return;
+        }
+        const unsigned int r = (unsigned int)it / (unsigned int)p.ngx;
+        const int bx0 = (int)((unsigned int)it - r * (unsigned int)p.ngx) * FG;
+        const int y0 = (int)(r % (unsigned int)p.nby) * BY, z0 = (int)(r / (unsigned int)p.nby) * BZ;
+        const int x0 = bx0 * BX;
+        S.sorg = make_int4(x0, y0, z0, bx0);
+        mbar_arrive_expect_tx(&S.bar, FTILE * V::bytes);
+        tma_load_3d(S.tile, &map, &S.bar, x0, y0, z0);
+    };
+    // the next item's ticket, drawn one item ahead (thread 0)
+    unsigned int ptk = 0xffffffffu;
+    auto refill = [&]() {
+        const int nxt = ptk < (unsigned int)p.nitems ? (int)ptk : -1;
+        stage_item(nxt);
+        if (nxt >= 0) ptk = atomicAdd(ticket, 1u);
+    };
+    if (tid == 0) {
+        S.abort = 0;
+        mbar_init(&S.bar, 1);
+        fence_barrier_init();
+        const unsigned int t0 = atomicAdd(ticket, 1u);
+        stage_item(t0 < (unsigned int)p.nitems ? (int)t0 : -1);
+        if (t0 < (unsigned int)p.nitems) ptk = atomicAdd(ticket, 1u);
+    }
+    __syncthreads();
+    const T *tile = reinterpret_cast<const T *>(S.tile);
+    // thread 0: this CTA's contributions to the totals
+    unsigned long long my_occ = 0, my_tris = 0;
+    unsigned int my_active = 0;
+    for (int i = 0;; ++i) {
+        const int4 org = S.sorg;
+        const int it = S.sitem;
+        if (org.x < 0) break;  // uniform
+        const int x0 = org.x, y0 = org.y, z0 = org.z, bx0 = org.w;
+        if (tid == 0 && !mbar_wait(&S.bar, (uint32_t)(i & 1))) S.abort = 1;
+        __syncthreads();
+        if (S.abort) break;
+        const bool mixed = fused_mixed<VT>(S, tile, nx, ny, nz, x0, y0, z0);
+        unsigned int item_v = 0;  // soup vertices of the item
+        if (mixed) {
+            // row masks of the FG bricks (voxel rows y0..y0+8, z0..z0+8)
+            for (int m = tid; m < FG * ROWS; m += THREADS) {
+                const int h = m / ROWS, r = m - h * ROWS, rz = r / CTY, ry = r - rz * CTY;
+                const T *row = tile + ftidx(h * BX, ry, rz);
+                RowMask<VT>::build(row, row[BX], S.neg[m], S.dead[m]);
+            }
+            __syncthreads();
+            // one cube row per thread: occupancy, vertices per cube, row total
+            const int h = tid / CUBE_ROWS, c = tid - h * CUBE_ROWS, cy = c & (BY - 1), cz = c / BY;
+            unsigned int occ = 0, rv = 0, nib[4] = {0u, 0u, 0u, 0u};
+            if (bx0 + h < p.nbx && y0 + cy < ny - 1 && z0 + cz < p.zlim) {
+                const CubeRow cr =
+                    cube_row(S.neg + h * ROWS, S.dead + h * ROWS, cy, cz, valid_mask(x0 + h * BX, nx));
+                occ = cr.occ;
+                unsigned int mm = occ;
+                while (mm) {
+                    const int x = __ffs(mm) - 1;
+                    mm &= mm - 1;
+                    const unsigned int n = S.nv[cube_index(cr, x)];
+                    nib[x >> 3] |= n << ((x & 7) * 4);
+                    rv += n;
+                }
+            }
+            S.rowocc[tid] = occ;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) S.rownib[tid][k] = nib[k];
+            // exclusive scan of the row totals over the item (rows in soup order)
+            unsigned int incl = rv;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const unsigned int u = __shfl_up_sync(0xffffffffu, incl, d);
+                if (lane >= d) incl += u;
+            }
+            const unsigned int wocc = __reduce_add_sync(0xffffffffu, (unsigned int)__popc(occ));
+            if (lane == 31) S.wsum[warp] = incl;
+            if (lane == 0) S.red[warp] = wocc;
+            __syncthreads();
+            unsigned int before = 0;
+            for (int w = 0; w < warp; ++w) before += S.wsum[w];
+            S.rowoff[tid] = before + incl - rv;
+#pragma unroll
+            for (int w = 0; w < WARPS; ++w) item_v += S.wsum[w];
+            if (tid == 0) {
+                // totals: occupied cubes, triangles, bricks with triangles (two warps per brick)
+                unsigned int o8 = 0, act = 0;
+                for (int w = 0; w < WARPS; ++w) o8 += S.red[w];
+                for (int b = 0; b < FG; ++b) act += (S.wsum[2 * b] + S.wsum[2 * b + 1]) ? 1u : 0u;
+                my_occ += o8;
+                my_tris += item_v / 3u;
+                my_active += act;
+            }
+        }
+        const bool emit = item_v != 0;
+        // publish the item's count; the last item of each group also publishes
+        // the group's aggregate and, once it has looked back, its inclusive
+        // prefix; items that emit look back for their soup offset
+        if (warp == 0) {
+            const unsigned int tris = item_v / 3u;
+            if (lane == 0)
+                st_relaxed_u64(p.item + it, ((unsigned long long)p.epoch << 32) | (unsigned long long)(tris + 1u));
+            const int g = it / FGROUP;
+            const bool last = (it % FGROUP == FGROUP - 1) || it == p.nitems - 1;
+            if (emit || last) {
+                unsigned long long in_group = 0, before = 0;
+                bool ok = items_before(p, it, in_group);
+                if (last && lane == 0) st_relaxed_u64(p.group + g, group_word(p.epoch, 1u, in_group + tris));
+                ok = groups_before(p, g, before) && ok;
+                if (lane == 0) {
+                    if (!ok) S.abort = 1;
+                    S.base = 3ull * (before + in_group);
+                    if (ok && last) st_relaxed_u64(p.group + g, group_word(p.epoch, 2u, before + in_group + tris));
+                }
+            }
+        }
+        if (!emit) {
+            // nothing to generate: no thread reads the tile any more, refill it now
+            if (tid == 0) refill();
+            __syncthreads();  // the next item is staged
+            continue;
+        }
+        __syncthreads();  // S.base, the row tables and S.abort
+        if (S.abort) break;
+        // ---- emission: warps take 32 consecutive soup vertices of the item ----
+        const unsigned long long vbase = S.base;
+        for (unsigned int v0 = warp * 32; v0 < item_v; v0 += THREADS) {
+            const unsigned int v = v0 + lane;
+            const bool valid = v < item_v;
+            float P[3] = {0.f, 0.f, 0.f};
+            int vox[3] = {0, 0, 0};
+            short vt = 0, vw = 0;
+            float3 nrm = make_float3(0.f, 0.f, 0.f);
+            long long cube_lin = 0;
+            int kslot = 1;
+            if (valid) {
+                // the cube row holding vertex v: the last row starting at or before it
+                int lo = 0, hi = FROWS - 1;
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (S.rowoff[mid] <= v) lo = mid; else hi = mid - 1;
+                }
+                const int r = lo;
+                unsigned int j = v - S.rowoff[r];
+                // the cube of the row and the vertex's slot in it
+                unsigned int mm = S.rowocc[r];
+                int x = 0;
+                for (;;) {
+                    x = __ffs(mm) - 1;
+                    const unsigned int n = (S.rownib[r][x >> 3] >> ((x & 7) * 4)) & 15u;
+                    if (j < n) break;
+                    j -= n;
+                    mm &= mm - 1;
+                }
+                const int h = r / CUBE_ROWS, c = r - h * CUBE_ROWS, cy = c & (BY - 1), cz = c / BY;
+                // sign masks only (the weight masks share their storage with the stage)
+                const CubeRow cr = cube_row(S.neg + h * ROWS, S.neg + h * ROWS, cy, cz, 0xffffffffu);
+                const unsigned int ci = cube_index(cr, x);
+                const unsigned int tj = j / 3, k = j - 3 * tj;
+                kslot = (int)k;
+                // output slot k of triangle tj takes edge tri[3 tj + 2 - k] (:322-333)
+                const int e = S.tri[ci][3 * tj + 2 - k];
+                const int lcx = h * BX + x, lcy = cy, lcz = cz;  // cube in tile coordinates
+                const int a = c_ea(e), bb = c_eb(e);
+                const int gx = x0 + lcx, gy = y0 + lcy, gz = z0 + lcz;
+                if (o.tri_cube) cube_lin = lin3(nx, ny, gx, gy, gz);
+                const float f0 = V::f(tile[ftidx(lcx + c_cx(a), lcy + c_cy(a), lcz + c_cz(a))]);
+                const float f1 = V::f(tile[ftidx(lcx + c_cx(bb), lcy + c_cy(bb), lcz + c_cz(bb))]);
+                // getNodeCoo (:243-254) and vertex_interp (:256-264)
+                const float t = (0.0f - f0) / (f1 - f0 + 1e-15f);
+                const int ga[3] = {gx + c_cx(a), gy + c_cy(a), gz + c_cz(a)};
+                const int gb[3] = {gx + c_cx(bb), gy + c_cy(bb), gz + c_cz(bb)};
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    const float p0 = ((float)ga[d] + 0.5f) * cell;
+                    const float p1 = ((float)gb[d] + 0.5f) * cell;
+                    P[d] = p0 + t * (p1 - p0);
+                }
+                // store_point (:336-367): voxel of the vertex, its tsdf / w
+                const int dims[3] = {nx, ny, nz};
+                const int orgv[3] = {x0, y0, z0};
+                const int tdim[3] = {FTX, FTY, FTZ};
+                const float pf[3] = {P[0] / cell, P[1] / cell, P[2] / cell};
+                bool inside = true;
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    vox[d] = (int)floorf(pf[d] - 0.5f);
+                    inside &= vox[d] >= 0 && vox[d] < dims[d] && vox[d] - orgv[d] >= 0 && vox[d] - orgv[d] < tdim[d];
+                }
+                if (inside) {
+                    const T vv = tile[ftidx(vox[0] - x0, vox[1] - y0, vox[2] - z0)];
+                    vt = V::tsdf(vv);
+                    vw = V::wt(vv);
+                }
+                if (!inside || o.ver_voxel) {
+                    const long long li = lin3(nx, ny, vox[0], vox[1], vox[2]);
+                    if (!inside && li >= 0 && li < N) {
+                        const T vv = vol[li];
+                        vt = V::tsdf(vv);
+                        vw = V::wt(vv);
+                    }
+                    if (o.ver_voxel && li >= 0 && li < N && vbase + v < (unsigned long long)o.cap)
+                        o.ver_voxel[li] = vt;
+                }
+                if (o.normals) {
+                    const float fx = pf[0], fy = pf[1], fz = pf[2];
+                    const int ix = (int)fx, iy = (int)fy, iz = (int)fz;
+                    const int lx = ix - x0, ly = iy - y0, lz = iz - z0;
+                    if (ix + 1 < nx && iy + 1 < ny && iz + 1 < nz && lx >= 0 && ly >= 0 && lz >= 0 &&
+                        lx + 1 < FTX && ly + 1 < FTY && lz + 1 < FTZ) {
+                        const T smp[8] = {tile[ftidx(lx, ly, lz)],         tile[ftidx(lx + 1, ly, lz)],
+                                          tile[ftidx(lx + 1, ly + 1, lz)], tile[ftidx(lx, ly + 1, lz)],
+                                          tile[ftidx(lx, ly, lz + 1)],     tile[ftidx(lx + 1, ly, lz + 1)],
+                                          tile[ftidx(lx + 1, ly + 1, lz + 1)], tile[ftidx(lx, ly + 1, lz + 1)]};
+                        bool sent = false;
+                        float sd[8];
+#pragma unroll
+                        for (int q = 0; q < 8; ++q) {
+                            sent |= V::sentinel(smp[q]);
+                            put_slot(sd, q, V::f(smp[q]));
+                        }
+                        if (!sent) nrm = normal_from_samples(sd, fx - (float)ix, fy - (float)iy, fz - (float)iz);
+                    } else {
+                        nrm = normal_global<VT>(vol, nx, ny, nz, cell, P[0], P[1], P[2]);
+                    }
+                }
+            }
+            // ---- coalesced stores through the warp stage ----
+            const unsigned long long g0 = vbase + v0;
+            const long long room = o.cap - (long long)g0;
+            const int nrec = (int)min((long long)min(32u, item_v - v0), room > 0 ? room : 0ll);
+            unsigned int *st = S.stage[warp];
+            if (o.soup) {
+                st[lane * 7 + 0] = __float_as_uint(P[0]);
+                st[lane * 7 + 1] = __float_as_uint(P[1]);
+                st[lane * 7 + 2] = __float_as_uint(P[2]);
+                st[lane * 7 + 3] = (unsigned int)vox[0];
+                st[lane * 7 + 4] = (unsigned int)vox[1];
+                st[lane * 7 + 5] = (unsigned int)vox[2];
+                st[lane * 7 + 6] = (unsigned int)(unsigned short)vt | ((unsigned int)(unsigned short)vw << 16);
+                __syncwarp();
+                unsigned int *dst = reinterpret_cast<unsigned int *>(o.soup) + g0 * 7;
+#pragma unroll
+                for (int q = 0; q < 7; ++q) {
+                    const int word = q * 32 + lane;
+                    if (word < nrec * 7) dst[word] = st[word];
+                }
+                __syncwarp();
+            }
+            if (o.normals) {
+                st[lane * 3 + 0] = __float_as_uint(nrm.x);
+                st[lane * 3 + 1] = __float_as_uint(nrm.y);
+                st[lane * 3 + 2] = __float_as_uint(nrm.z);
+                __syncwarp();
+                unsigned int *dst = reinterpret_cast<unsigned int *>(o.normals) + g0 * 3;
+#pragma unroll
+                for (int q = 0; q < 3; ++q) {
+                    const int word = q * 32 + lane;
+                    if (word < nrec * 3) dst[word] = st[word];
+                }
+                __syncwarp();
+            }
+            if (o.vi2vox) {
+                st[lane * 3 + 0] = (unsigned int)vox[0];
+                st[lane * 3 + 1] = (unsigned int)vox[1];
+                st[lane * 3 + 2] = (unsigned int)vox[2];
+                __syncwarp();
+                unsigned int *dst = reinterpret_cast<unsigned int *>(o.vi2vox) + g0 * 3;
+#pragma unroll
+                for (int q = 0; q < 3; ++q) {
+                    const int word = q * 32 + lane;
+                    if (word < nrec * 3) dst[word] = st[word];
+                }
+                __syncwarp();
+            }
+            // a triangle's cube id is written only when the whole triangle fits
+            if (o.tri_cube && valid && kslot == 0 && (long long)(g0 + lane) + 2 < o.cap)
+                o.tri_cube[(g0 + lane) / 3] = cube_lin;
+        }
+        __syncthreads();  // the tile, the row tables and the stages are free again
+        if (tid == 0) refill();
+        __syncthreads();  // the next item is staged
+    }
+    pdl_trigger();
+    if (tid == 0) {
+        if (S.abort) {
+            atomicOr(&p.totals->flags, 1u);
+            mbar_wait(&S.bar, 0, 100000000ull);  // give a load still in flight a bounded chance to land
+        }
+        if (my_tris) atomicAdd(&p.totals->triangles, my_tris);
+        if (my_occ) atomicAdd(&p.totals->occupied, my_occ);
+        if (my_active) atomicAdd(&p.totals->active_bricks, my_active);
+        __threadfence();
+        // the last CTA out completes the totals, hands them (and the flags) to
+        // the mapped host copy, and leaves the counters clear for the next launch
+        if (atomicAdd(&p.totals->gen_exit, 1u) == gridDim.x - 1) {
+            MeshTotals *t = p.totals;
+            volatile MeshTotals *vt = t;
+            const unsigned long long tris = vt->triangles;
+            t->vertices = 3ull * tris;
+            t->cls_ticket = 0;
+            t->gen_exit = 0;
+            if (p.host) {
+                p.host->occupied = vt->occupied;
+                p.host->triangles = tris;
+                p.host->vertices = 3ull * tris;
+                p.host->active_bricks = vt->active_bricks;
+                p.host->flags = vt->flags;
+                __threadfence_system();
+                t->occupied = 0;
+                t->triangles = 0;
+                t->vertices = 0;
+                t->active_bricks = 0;
+                t->flags = 0;
+            }
+        }
+    }
+}
+
 // ---- batched extraction: many volumes, one launch per pass ------------------------
 // Bricks of all volumes form one index space: volume v owns bricks
 // [brick_base, brick_base + nbricks).  A brick's volume is found by binary
@@ -1544,19 +2080,9 @@ struct Scratch {
     MeshTotals *host;  // mapped host copy of the totals, or null
 };
 
-// fixed serpentine rounds at the start of the generate launch (tuning:
-// MCG_GEN_FIXED)
-unsigned int generate_fixed_rounds() {
-    static int f = -1;
-    if (f < 0) {
-        f = 3;
-        if (const char *e = getenv("MCG_GEN_FIXED")) {
-            const int v = atoi(e);
-            if (v >= 0 && v <= 1000000) f = v;
-        }
-    }
-    return (unsigned int)f;
-}
+// default launch configuration (the measured best on GB300; a context can
+// choose another through mcg_mc_set_config, e.g. from the autotuner)
+constexpr mcg_mc_config kDefaultMcConfig = {1, 4, 3, 0};
 
 // Launch with programmatic stream serialisation: the kernel may start while
 // the kernel before it on the stream drains (it waits with pdl_wait).
@@ -1591,29 +2117,16 @@ void launch_classify_s(const CUtensorMap &map, const CUtensorMap &hmap, const mc
                (int)nitems, ngx, g.zbase, g.zlim, sc.tris, sc.chunk, &sc.totals->flags, &sc.totals->cls_ticket);
 }
 
-// classify configuration; MCG_CLS_CFG selects one for tuning:
+// classify configurations (mcg_mc_config.classify_shape):
 //   0: 2 bricks, in-box halo (68-voxel box), 2 stages x 256 threads
 //   1: 4 bricks, halo box, 2 stages x 256 threads
 //   2: 4 bricks, halo box, 4 stages x 512 threads
 //   3: 4 bricks, in-box halo (132-voxel box), 2 stages x 256 threads
 //   4: 4 bricks, in-box halo (132-voxel box), 1 stage x 256 threads
 //   5: 2 bricks, in-box halo (68-voxel box), 1 stage x 256 threads
-int classify_cfg() {
-    static int c = -1;
-    if (c < 0) {
-        c = 4;
-        if (const char *e = getenv("MCG_CLS_CFG")) {
-            const int v = atoi(e);
-            if (v >= 0 && v <= 5) c = v;
-        }
-    }
-    return c;
-}
-
 // bricks per work item and in-box halo of the configuration, narrowed to
 // what the volume's width allows
-void classify_shape(int nx, int eb, int &G, int &XH) {
-    const int c = classify_cfg();
+void classify_shape(int nx, int eb, int c, int &G, int &XH) {
     XH = (c == 1 || c == 2) ? 0 : 4;
     const int pref = (c == 0 || c == 5) ? 2 : 512 / (BX * eb);
     G = 1;
@@ -1623,12 +2136,11 @@ void classify_shape(int nx, int eb, int &G, int &XH) {
 
 template <int VT, bool TMA, int G, int XH>
 void launch_classify_g(const CUtensorMap &map, const CUtensorMap &hmap, const mcg_volume *vol, const Geometry &g,
-                       const Scratch &sc, int sms, cudaStream_t s) {
+                       const Scratch &sc, int sms, cudaStream_t s, int c) {
     // without TMA only one stage is ever used
     if constexpr (!TMA) {
         launch_classify_s<VT, TMA, G, XH, 1, 256>(map, hmap, vol, g, sc, sms, s);
     } else {
-        const int c = classify_cfg();
         if (c == 2) launch_classify_s<VT, TMA, G, XH, 4, 512>(map, hmap, vol, g, sc, sms, s);
         else if (c >= 4) launch_classify_s<VT, TMA, G, XH, 1, 256>(map, hmap, vol, g, sc, sms, s);
         else launch_classify_s<VT, TMA, G, XH, 2, 256>(map, hmap, vol, g, sc, sms, s);
@@ -1637,16 +2149,16 @@ void launch_classify_g(const CUtensorMap &map, const CUtensorMap &hmap, const mc
 
 template <int VT, int XH>
 void launch_classify_x(bool tma, int G, const CUtensorMap &map, const CUtensorMap &hmap, const mcg_volume *vol,
-                       const Geometry &g, const Scratch &sc, int sms, cudaStream_t s) {
+                       const Geometry &g, const Scratch &sc, int sms, cudaStream_t s, int c) {
     if (G == 4) {
-        if (tma) launch_classify_g<VT, true, 4, XH>(map, hmap, vol, g, sc, sms, s);
-        else launch_classify_g<VT, false, 4, XH>(map, hmap, vol, g, sc, sms, s);
+        if (tma) launch_classify_g<VT, true, 4, XH>(map, hmap, vol, g, sc, sms, s, c);
+        else launch_classify_g<VT, false, 4, XH>(map, hmap, vol, g, sc, sms, s, c);
     } else if (G == 2) {
-        if (tma) launch_classify_g<VT, true, 2, XH>(map, hmap, vol, g, sc, sms, s);
-        else launch_classify_g<VT, false, 2, XH>(map, hmap, vol, g, sc, sms, s);
+        if (tma) launch_classify_g<VT, true, 2, XH>(map, hmap, vol, g, sc, sms, s, c);
+        else launch_classify_g<VT, false, 2, XH>(map, hmap, vol, g, sc, sms, s, c);
     } else {
-        if (tma) launch_classify_g<VT, true, 1, XH>(map, hmap, vol, g, sc, sms, s);
-        else launch_classify_g<VT, false, 1, XH>(map, hmap, vol, g, sc, sms, s);
+        if (tma) launch_classify_g<VT, true, 1, XH>(map, hmap, vol, g, sc, sms, s, c);
+        else launch_classify_g<VT, false, 1, XH>(map, hmap, vol, g, sc, sms, s, c);
     }
 }
 
@@ -1666,7 +2178,8 @@ void launch_generate_t(const CUtensorMap &map, const GenParams &p, const Geometr
 long long num_chunks(long long nbricks) { return (nbricks + CHUNK - 1) / CHUNK; }
 
 cudaError_t launch_count_phase(const mcg_volume *vol, const Geometry &g, const Scratch &sc, int sms, cudaStream_t s,
-                               bool clear = true, cudaEvent_t t0 = nullptr, cudaEvent_t t1 = nullptr) {
+                               const mcg_mc_config &cfg, bool clear = true, cudaEvent_t t0 = nullptr,
+                               cudaEvent_t t1 = nullptr) {
     // flags and both work counters unless known to be zero; the chunk sums
     // are zero already (the previous scan cleared them)
     cudaError_t e = clear ? cudaMemsetAsync(&sc.totals->flags, 0, 3 * sizeof(unsigned int), s) : cudaSuccess;
@@ -1674,7 +2187,7 @@ cudaError_t launch_count_phase(const mcg_volume *vol, const Geometry &g, const S
     CUtensorMap map, hmap;
     const int eb = vol->voxel_type == MCG_VOXEL_SHORT2 ? 4 : 8;
     int G, XH;
-    classify_shape(vol->nx, eb, G, XH);
+    classify_shape(vol->nx, eb, cfg.classify_shape, G, XH);
     if ((long long)((g.nbx + G - 1) / G) * g.nby * g.nbz > 0x7fffffffll) return cudaErrorInvalidValue;
     bool tma = encode_volume_map(&map, vol->data, vol->nx, vol->ny, vol->nz, eb, G * BX + XH, CTY, CTZ);
     if (tma && XH == 0) tma = encode_volume_map(&hmap, vol->data, vol->nx, vol->ny, vol->nz, eb, 16 / eb, CTY, CTZ);
@@ -1688,12 +2201,13 @@ cudaError_t launch_count_phase(const mcg_volume *vol, const Geometry &g, const S
         const cudaError_t et = cudaEventRecord(t0, s);
         if (et != cudaSuccess) return et;
     }
+    const int c = cfg.classify_shape;
     if (XH) {
-        if (s2) launch_classify_x<MCG_VOXEL_SHORT2, 4>(tma, G, map, hmap, vol, g, sc, sms, s);
-        else launch_classify_x<MCG_VOXEL_FLOAT2, 4>(tma, G, map, hmap, vol, g, sc, sms, s);
+        if (s2) launch_classify_x<MCG_VOXEL_SHORT2, 4>(tma, G, map, hmap, vol, g, sc, sms, s, c);
+        else launch_classify_x<MCG_VOXEL_FLOAT2, 4>(tma, G, map, hmap, vol, g, sc, sms, s, c);
     } else {
-        if (s2) launch_classify_x<MCG_VOXEL_SHORT2, 0>(tma, G, map, hmap, vol, g, sc, sms, s);
-        else launch_classify_x<MCG_VOXEL_FLOAT2, 0>(tma, G, map, hmap, vol, g, sc, sms, s);
+        if (s2) launch_classify_x<MCG_VOXEL_SHORT2, 0>(tma, G, map, hmap, vol, g, sc, sms, s, c);
+        else launch_classify_x<MCG_VOXEL_FLOAT2, 0>(tma, G, map, hmap, vol, g, sc, sms, s, c);
     }
     if (t1) {
         const cudaError_t et = cudaEventRecord(t1, s);
@@ -1705,7 +2219,7 @@ cudaError_t launch_count_phase(const mcg_volume *vol, const Geometry &g, const S
 }
 
 cudaError_t launch_generate_phase(const mcg_volume *vol, const Geometry &g, const Scratch &sc,
-                                  const mcg_mesh_out *out, int sms, cudaStream_t s) {
+                                  const mcg_mesh_out *out, int sms, cudaStream_t s, const mcg_mc_config &cfg) {
     if (out->ver_voxel) {
         cudaError_t e = cudaMemsetAsync(out->ver_voxel, 0, sizeof(int16_t) * (size_t)vol->nx * vol->ny * vol->nz, s);
         if (e != cudaSuccess) return e;
@@ -1725,7 +2239,7 @@ cudaError_t launch_generate_phase(const mcg_volume *vol, const Geometry &g, cons
     p.brick_vofs = sc.vofs;
     p.list_vofs = sc.list_vofs;
     p.host = sc.host;
-    p.fixed_rounds = generate_fixed_rounds();
+    p.fixed_rounds = (unsigned int)cfg.gen_fixed_rounds;
     p.totals = sc.totals;
     p.soup = out->soup;
     p.normals = out->soup_normals;
@@ -1753,6 +2267,88 @@ cudaError_t launch_generate_phase(const mcg_volume *vol, const Geometry &g, cons
 Scratch ctx_scratch(mcg_context *ctx) {
     return Scratch{ctx->brick_tris, ctx->brick_occ, ctx->brick_vofs, ctx->active, ctx->list_vofs, ctx->d_totals,
                    ctx->h_totals_dev};
+}
+
+// The fused extraction applies to short2 volumes of at least one item box
+// (132 x 10 x 10) that TMA can describe; `map` receives the tensor map.
+bool fused_applies(const mcg_volume *vol, CUtensorMap *map) {
+    if (vol->voxel_type != MCG_VOXEL_SHORT2) return false;
+    if (vol->nx < FTX || vol->ny < FTY || vol->nz < FTZ) return false;
+    return encode_volume_map(map, vol->data, vol->nx, vol->ny, vol->nz, 4, FTX, FTY, FTZ);
+}
+
+// One fused launch over the whole volume.
+cudaError_t launch_fused(mcg_context *ctx, const CUtensorMap &map, const mcg_volume *vol, const mcg_mesh_out *out,
+                         cudaStream_t s) {
+    const Geometry g = geometry(vol->nx, vol->ny, vol->nz);
+    const int ngx = (g.nbx + FG - 1) / FG;
+    const long long nitems = (long long)ngx * g.nby * g.nbz;
+    if (nitems > 0x7fffffffll) return cudaErrorInvalidValue;
+    const long long ngroups = (nitems + FGROUP - 1) / FGROUP;
+    const size_t icap = ctx->fx_item_cap, gcap = ctx->fx_group_cap;
+    if (!ensure(&ctx->fx_item, &ctx->fx_item_cap, (size_t)nitems) ||
+        !ensure(&ctx->fx_group, &ctx->fx_group_cap, (size_t)ngroups))
+        return cudaErrorMemoryAllocation;
+    cudaError_t e = cudaSuccess;
+    // fresh allocations, and the wrap of the 22-bit epoch, start from entries
+    // of epoch 0: every entry then belongs to an older launch of this cycle
+    if (ctx->fx_item_cap != icap || ctx->fx_group_cap != gcap || ctx->fx_epoch + 1 >= (1u << FX_EPOCH_BITS)) {
+        e = cudaMemsetAsync(ctx->fx_item, 0, sizeof(unsigned long long) * ctx->fx_item_cap, s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(ctx->fx_group, 0, sizeof(unsigned long long) * ctx->fx_group_cap, s);
+        if (e != cudaSuccess) return e;
+        ctx->fx_epoch = 0;
+    }
+    // The launch accumulates the totals, so they must start at zero: the
+    // previous fused launch on ctx leaves them so when the totals reached the
+    // host through the mapped copy; every other count phase leaves its own
+    // totals behind.
+    if (!ctx->h_totals_dev || !ctx->counters_clean || !ctx->cls_fused) {
+        e = cudaMemsetAsync(ctx->d_totals, 0, sizeof(MeshTotals), s);
+        if (e != cudaSuccess) return e;
+    }
+    if (out->ver_voxel) {
+        e = cudaMemsetAsync(out->ver_voxel, 0, sizeof(int16_t) * (size_t)vol->nx * vol->ny * vol->nz, s);
+        if (e != cudaSuccess) return e;
+    }
+    FusedParams p;
+    p.vol = vol->data;
+    p.nx = vol->nx;
+    p.ny = vol->ny;
+    p.nz = vol->nz;
+    p.cell = vol->cell;
+    p.nbx = g.nbx;
+    p.nby = g.nby;
+    p.nitems = (int)nitems;
+    p.ngx = ngx;
+    p.zlim = g.zlim;
+    p.item = ctx->fx_item;
+    p.group = ctx->fx_group;
+    p.epoch = ++ctx->fx_epoch;
+    p.totals = ctx->d_totals;
+    p.host = ctx->h_totals_dev;
+    p.out.soup = out->soup;
+    p.out.normals = out->soup_normals;
+    p.out.vi2vox = out->vi2vox;
+    p.out.ver_voxel = out->ver_voxel;
+    p.out.tri_cube = out->tri_cube;
+    p.out.cap = out->capacity_vertices;
+    p.out.zlim = g.zlim;
+    const size_t smem = sizeof(FusedSmem<MCG_VOXEL_SHORT2>);
+    static int occ = 0;
+    if (!occ) occ = occupancy(mc_fused_kernel<MCG_VOXEL_SHORT2>, THREADS, smem);
+    long long grid = (long long)ctx->num_sms * occ;
+    if (grid > nitems) grid = nitems;
+    if (ctx->time_kernels) {
+        e = cudaEventRecord(ctx->tk0, s);
+        if (e != cudaSuccess) return e;
+    }
+    e = launch_pdl(mc_fused_kernel<MCG_VOXEL_SHORT2>, (unsigned int)grid, THREADS, smem, s, map, p);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e == cudaSuccess && ctx->time_kernels) {
+        e = cudaEventRecord(ctx->tk1, s);
+        if (e == cudaSuccess) ctx->timed = true;
+    }
+    return e;
 }
 
 }  // namespace
@@ -1785,7 +2381,8 @@ static mcg_status classify_impl(mcg_context *ctx, const mcg_volume *vol, int32_t
         if (e == cudaSuccess) e = cudaEventCreate(&ctx->tk1);
         if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
     }
-    e = launch_count_phase(vol, g, ctx_scratch(ctx), ctx->num_sms, s, !ctx->h_totals_dev || !ctx->counters_clean,
+    e = launch_count_phase(vol, g, ctx_scratch(ctx), ctx->num_sms, s, ctx->mc_cfg,
+                           !ctx->h_totals_dev || !ctx->counters_clean,
                            ctx->time_kernels ? ctx->tk0 : nullptr, ctx->time_kernels ? ctx->tk1 : nullptr);
     if (e == cudaSuccess && ctx->time_kernels) ctx->timed = true;
     ctx->counters_clean = e == cudaSuccess && ctx->h_totals_dev != nullptr;
@@ -1795,6 +2392,7 @@ static mcg_status classify_impl(mcg_context *ctx, const mcg_volume *vol, int32_t
     if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
     ctx->classified = true;
     ctx->cls_indexed = false;
+    ctx->cls_fused = false;
     ctx->batch_classified = false;
     ctx->cls_data = vol->data;
     ctx->cls_nx = vol->nx;
@@ -1857,8 +2455,8 @@ mcg_status mcg_mc_counts(mcg_context *ctx, mcg_mesh_counts *out) {
 mcg_status mcg_mc_generate(mcg_context *ctx, const mcg_volume *vol, const mcg_mesh_out *out,
                            mcg_stream_t stream) {
     if (!ctx || !vol_ok(vol) || !out || out->capacity_vertices < 0) return MCG_ERR_INVALID_ARG;
-    if (!ctx->classified || ctx->cls_indexed || ctx->cls_data != vol->data || ctx->cls_nx != vol->nx ||
-        ctx->cls_ny != vol->ny || ctx->cls_nz != vol->nz || ctx->cls_vtype != vol->voxel_type)
+    if (!ctx->classified || ctx->cls_indexed || ctx->cls_fused || ctx->cls_data != vol->data ||
+        ctx->cls_nx != vol->nx || ctx->cls_ny != vol->ny || ctx->cls_nz != vol->nz || ctx->cls_vtype != vol->voxel_type)
         return MCG_ERR_STATE;
     if (out->capacity_vertices > 0 && !out->soup && !out->soup_normals && !out->vi2vox &&
         !out->ver_voxel && !out->tri_cube)
@@ -1871,7 +2469,7 @@ mcg_status mcg_mc_generate(mcg_context *ctx, const mcg_volume *vol, const mcg_me
     cudaError_t e = cudaSetDevice(ctx->device);
     if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
     const Geometry g = geometry_slab(vol->nx, vol->ny, ctx->cls_z0, ctx->cls_z1);
-    e = launch_generate_phase(vol, g, ctx_scratch(ctx), out, ctx->num_sms, s);
+    e = launch_generate_phase(vol, g, ctx_scratch(ctx), out, ctx->num_sms, s, ctx->mc_cfg);
     // the totals are re-read so a timeout flagged by generate is reported (the
     // launch writes the flags to the mapped host copy itself)
     if (e == cudaSuccess && !ctx->h_totals_dev)
@@ -1884,9 +2482,61 @@ mcg_status mcg_mc_generate(mcg_context *ctx, const mcg_volume *vol, const mcg_me
 
 mcg_status mcg_mc_extract(mcg_context *ctx, const mcg_volume *vol, const mcg_mesh_out *out,
                           mcg_stream_t stream) {
+    if (!ctx || !vol_ok(vol) || !out || out->capacity_vertices < 0) return MCG_ERR_INVALID_ARG;
+    if (out->capacity_vertices > 0 && !out->soup && !out->soup_normals && !out->vi2vox && !out->ver_voxel &&
+        !out->tri_cube)
+        return MCG_ERR_INVALID_ARG;
+    CUtensorMap map;
+    if (ctx->mc_cfg.fused && fused_applies(vol, &map)) {
+        cudaStream_t s = (cudaStream_t)stream;
+        cudaError_t e = cudaSetDevice(ctx->device);
+        if (e == cudaSuccess) e = upload_tables(ctx->device);
+        if (e == cudaSuccess && ctx->time_kernels && !ctx->tk0) {
+            e = cudaEventCreate(&ctx->tk0);
+            if (e == cudaSuccess) e = cudaEventCreate(&ctx->tk1);
+        }
+        if (e == cudaSuccess) e = launch_fused(ctx, map, vol, out, s);
+        ctx->counters_clean = e == cudaSuccess && ctx->h_totals_dev != nullptr;
+        if (e == cudaSuccess && !ctx->h_totals_dev)
+            e = cudaMemcpyAsync(ctx->h_totals, ctx->d_totals, sizeof(MeshTotals), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = mcg_counts_event(ctx, s);
+        if (e != cudaSuccess) {
+            ctx->classified = false;
+            ctx->cls_fused = false;
+            return mcg_cuda_fail(ctx, e);
+        }
+        ctx->classified = true;
+        ctx->cls_indexed = false;
+        ctx->cls_fused = true;
+        ctx->batch_classified = false;
+        ctx->cls_data = vol->data;
+        ctx->cls_nx = vol->nx;
+        ctx->cls_ny = vol->ny;
+        ctx->cls_nz = vol->nz;
+        ctx->cls_vtype = vol->voxel_type;
+        ctx->cls_z0 = 0;
+        ctx->cls_z1 = vol->nz - 1;
+        ctx->last_capacity = out->capacity_vertices;
+        return MCG_OK;
+    }
     mcg_status st = mcg_mc_classify(ctx, vol, stream);
     if (st != MCG_OK) return st;
     return mcg_mc_generate(ctx, vol, out, stream);
+}
+
+mcg_status mcg_mc_get_config(const mcg_context *ctx, mcg_mc_config *cfg) {
+    if (!ctx || !cfg) return MCG_ERR_INVALID_ARG;
+    *cfg = ctx->mc_cfg;
+    return MCG_OK;
+}
+
+mcg_status mcg_mc_set_config(mcg_context *ctx, const mcg_mc_config *cfg) {
+    if (!ctx || !cfg) return MCG_ERR_INVALID_ARG;
+    if ((cfg->fused != 0 && cfg->fused != 1) || cfg->classify_shape < 0 || cfg->classify_shape > 5 ||
+        cfg->gen_fixed_rounds < 0 || cfg->gen_fixed_rounds > 16 || cfg->reserved != 0)
+        return MCG_ERR_INVALID_ARG;
+    ctx->mc_cfg = *cfg;
+    return MCG_OK;
 }
 
 mcg_status mcg_mc_extract_slab(mcg_context *ctx, const mcg_volume *vol, int32_t z0, int32_t z1,
@@ -1920,8 +2570,8 @@ mcg_status mcg_mc_backward(mcg_context *ctx, const mcg_volume *vol, const float 
                            float *grad_f, mcg_stream_t stream) {
     if (!ctx || !vol_ok(vol) || n_vertices < 0 || !grad_f || (n_vertices > 0 && !grad_pos))
         return MCG_ERR_INVALID_ARG;
-    if (!ctx->classified || ctx->cls_indexed || ctx->cls_data != vol->data || ctx->cls_nx != vol->nx ||
-        ctx->cls_ny != vol->ny || ctx->cls_nz != vol->nz || ctx->cls_vtype != vol->voxel_type)
+    if (!ctx->classified || ctx->cls_indexed || ctx->cls_fused || ctx->cls_data != vol->data ||
+        ctx->cls_nx != vol->nx || ctx->cls_ny != vol->ny || ctx->cls_nz != vol->nz || ctx->cls_vtype != vol->voxel_type)
         return MCG_ERR_STATE;
     if (n_vertices == 0) return MCG_OK;
     cudaStream_t s = (cudaStream_t)stream;
@@ -1946,7 +2596,7 @@ mcg_status mcg_mc_backward(mcg_context *ctx, const mcg_volume *vol, const float 
     p.brick_vofs = ctx->brick_vofs;
     p.list_vofs = ctx->list_vofs;
     p.totals = ctx->d_totals;
-    p.fixed_rounds = generate_fixed_rounds();
+    p.fixed_rounds = (unsigned int)ctx->mc_cfg.gen_fixed_rounds;
     p.grad_pos = grad_pos;
     p.grad_f = grad_f;
     p.n_grad = n_vertices;
@@ -2157,6 +2807,7 @@ mcg_status mcg_mc_classify_batched(mcg_context *ctx, const mcg_volume *vols, int
     if (e == cudaSuccess) e = mcg_counts_event(ctx, s);
     if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
     ctx->batch_classified = true;
+    ctx->cls_fused = false;  // the batch's scan wrote the totals
     ctx->batch_nvol = nvol;
     ctx->batch_nbricks = nbricks;
     ctx->batch_vtype = vols[0].voxel_type;
@@ -2303,8 +2954,8 @@ extern "C" mcg_status mcg_mc_extract_noalloc(const mcg_volume *vol, const mcg_me
     e = cudaMemsetAsync(sc.chunk, 0, sizeof(uint32_t) * CHUNK_FIELDS * num_chunks(g.nbricks), s);
     if (e == cudaSuccess) e = cudaMemsetAsync(sc.totals, 0, sizeof(MeshTotals), s);
     if (e != cudaSuccess) { cudaGetLastError(); return MCG_ERR_CUDA; }
-    e = launch_count_phase(vol, g, sc, sms, s, false);
-    if (e == cudaSuccess) e = launch_generate_phase(vol, g, sc, out, sms, s);
+    e = launch_count_phase(vol, g, sc, sms, s, kDefaultMcConfig, false);
+    if (e == cudaSuccess) e = launch_generate_phase(vol, g, sc, out, sms, s, kDefaultMcConfig);
     if (e != cudaSuccess) { cudaGetLastError(); return MCG_ERR_CUDA; }
     // counts: copy the totals out of the array into a host variable and wait
     MeshTotals t;

@@ -772,6 +772,7 @@ mcg_status mcg_mc_classify_indexed(mcg_context *ctx, const mcg_volume *vol, mcg_
     if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
     ctx->classified = true;
     ctx->cls_indexed = true;
+    ctx->cls_fused = false;  // the indexed scan wrote the totals
     ctx->batch_classified = false;
     ctx->cls_data = vol->data;
     ctx->cls_nx = vol->nx;

@@ -68,6 +68,15 @@ struct mcg_context {
     size_t brick_uofs_cap = 0;
     uint32_t *edge_map = nullptr;
     size_t edge_map_cap = 0;
+    // fused extraction: per work item its triangle count and per group of
+    // items its aggregate / inclusive prefix, each tagged with the launch's
+    // epoch (entries of older launches read as unpublished), zeroed at
+    // allocation and when the epoch wraps
+    unsigned long long *fx_item = nullptr;
+    size_t fx_item_cap = 0;
+    unsigned long long *fx_group = nullptr;
+    size_t fx_group_cap = 0;
+    unsigned int fx_epoch = 0;
     mcg::MeshTotals *d_totals = nullptr;
     mcg::MeshTotals *h_totals = nullptr;  // pinned, mapped
     mcg::MeshTotals *h_totals_dev = nullptr;  // device address of h_totals; null if it has none
@@ -89,6 +98,8 @@ struct mcg_context {
     int cls_z0 = 0, cls_z1 = 0;  // cube layers z0 <= z < z1 of the last count phase
     int64_t last_capacity = -1;
     bool cls_indexed = false;        // the last classify was mcg_mc_classify_indexed
+    bool cls_fused = false;          // the last count phase was a fused extraction (counts only, no brick list)
+    mcg_mc_config mc_cfg = {1, 4, 3, 0};  // launch configuration (mcg_mc_set_config)
     int64_t last_capacity_tris = -1;  // indexed: triangle capacity of the last generate
 
     // batched extraction: device tables (volume descriptors, classify and
