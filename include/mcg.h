@@ -116,9 +116,10 @@ mcg_status mcg_mc_generate(mcg_context *ctx, const mcg_volume *vol, const mcg_me
                            mcg_stream_t stream);
 /* MarchingCubes::run (mc.cu:416-467) in one call, no host synchronisation:
  * the same soup, side outputs, order and counts as mcg_mc_classify +
- * mcg_mc_generate.  For short2 volumes of at least 132 x 10 x 10 voxels that
- * TMA can describe it runs as one fused launch (count, offsets and
- * generation together, mcg_mc_config.fused); the counts are then readable
+ * mcg_mc_generate.  With mcg_mc_config.fused set, short2 volumes of at
+ * least 132 x 10 x 10 voxels (68 x 10 x 10 with 2-brick items) that TMA can
+ * describe run as one fused launch (count, offsets and generation
+ * together); the counts are then readable
  * through mcg_mc_counts, but the count phase's brick list is not kept, so
  * mcg_mc_generate / mcg_mc_backward on this ctx need a mcg_mc_classify first
  * (MCG_ERR_STATE otherwise).  Other volumes take the two launches. */
@@ -126,10 +127,13 @@ mcg_status mcg_mc_extract(mcg_context *ctx, const mcg_volume *vol, const mcg_mes
                           mcg_stream_t stream);
 /* Launch configuration of the marching-cubes kernels on a context (no
  * counterpart in the reference; the reference's launch shapes are fixed).
- * Defaults are the measured best on GB300; the autotuner
+ * Defaults are the measured best on GB300 for the 512^3 fusion volume
+ * (fused 0, classify_shape 4, gen_fixed_rounds 3); the autotuner
  * (marching_cube_gb300.tune) times the choices on a volume and sets them.
- *   fused            1: mcg_mc_extract uses the fused launch where it applies,
- *                    0: always the count + generate launches
+ *   fused            mcg_mc_extract: 0 always the count + generate launches;
+ *                    1 the fused launch where it applies, work items of 4
+ *                    bricks (132-voxel tiles, 256 threads); 2 the same with
+ *                    items of 2 bricks (68-voxel tiles, 128 threads)
  *   classify_shape   count-pass work item, 0..5: 2 bricks in a 68-voxel box,
  *                    2 stages (0); 4 bricks with a separate halo box, 2
  *                    stages (1) or 4 stages of 512 threads (2); 4 bricks in a

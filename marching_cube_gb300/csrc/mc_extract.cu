@@ -1193,17 +1193,22 @@ __global__ void __launch_bounds__(THREADS, GEN_MINB) mc_generate_kernel(const __
 // (each is bounded by %globaltimer all the same).  The output order is the
 // one of the two-launch path: bricks in (bz, by, bx) order, cubes in (z, y, x)
 // order inside a brick, table slot order inside a cube.
-constexpr int FG = 4;                        // bricks per item
-constexpr int FTX = BX * FG + 4;             // 132 voxels in x
+// Item geometry for FG bricks per item (4: 132-voxel tiles, 256 threads;
+// 2: 68-voxel tiles, 128 threads): one thread per cube row of the item.
 constexpr int FTY = BY + 2, FTZ = BZ + 2;    // 10 x 10 rows
-constexpr int FTILE = FTX * FTY * FTZ;
-constexpr int FROWS = FG * CUBE_ROWS;        // 256 cube rows per item, one per thread
 constexpr int FGROUP = 32;                   // items per look-back group
-static_assert(FROWS == THREADS, "one thread per cube row of an item");
+template <int FG>
+struct FGeo {
+    static constexpr int TX = BX * FG + 4;   // voxels in x
+    static constexpr int TILE = TX * FTY * FTZ;
+    static constexpr int NT = FG * CUBE_ROWS; // threads = cube rows per item
+    static constexpr int NWARP = NT / 32;
+};
 
-template <int VT>
+template <int VT, int FG>
 struct FusedSmem {
-    static constexpr int TILE_BYTES = pad128(FTILE * Vox<VT>::bytes);
+    static constexpr int NT = FGeo<FG>::NT, WARPS = FGeo<FG>::NWARP, FROWS = NT;
+    static constexpr int TILE_BYTES = pad128(FGeo<FG>::TILE * Vox<VT>::bytes);
     unsigned char tile[TILE_BYTES];
     unsigned long long neg[FG * ROWS];           // row masks of the item's bricks, [brick][row]
     union {
@@ -1331,29 +1336,51 @@ __device__ bool items_before(const FusedParams &p, int it, unsigned long long &s
     return __all_sync(0xffffffffu, ok);
 }
 
-// 16-byte words of the item's classification region (voxel rows y0 .. y0+8,
-// z0 .. z0+8) that lie inside the volume hold both signs; contains a barrier.
-template <int VT, class Smem>
+// True when the item's voxels hold both signs; contains a barrier.  An item
+// whose classification region (voxel rows y0 .. y0+8 of planes z0 .. z0+8,
+// all 132 columns) lies inside the volume tests every 16-byte word of its
+// tile in one contiguous sweep -- the extra row and plane the normals need
+// can only turn a one-signed item into a "mixed" one, which costs the full
+// classification but changes no count.  Items at the volume's end test only
+// their words inside the volume (rows and columns beyond it arrive
+// zero-filled and would make an all-negative border item mixed).
+template <int VT, int FG, class Smem>
 __device__ __forceinline__ bool fused_mixed(Smem &S, const typename Vox<VT>::T *tile, int nx, int ny, int nz,
                                             int x0, int y0, int z0) {
     using V = Vox<VT>;
+    constexpr int FTX = FGeo<FG>::TX, THREADS = FGeo<FG>::NT, WARPS = FGeo<FG>::NWARP;
     constexpr int WPR = FTX * V::bytes / 16;  // 16-byte words per row
     constexpr int VPW = 16 / V::bytes;
+    constexpr int NW = FGeo<FG>::TILE * V::bytes / 16;
     const uint4 *q = reinterpret_cast<const uint4 *>(tile);
-    const int ry = ny - y0, rz = nz - z0, rx = nx - x0;
     unsigned int neg_any = 0, pos_any = 0;
-    for (int i = threadIdx.x; i < WPR * ROWS; i += THREADS) {
-        const int r = i / WPR, w = i - r * WPR, lx = w * VPW;
-        const int lz = r / CTY, ly = r - lz * CTY;  // rows 0..8 of planes 0..8
-        if (ly >= ry || lz >= rz || lx >= rx) continue;
-        const uint4 v = q[(lz * FTY + ly) * WPR + w];
+    auto acc = [&](const uint4 v) {
         if (VT == MCG_VOXEL_SHORT2) {
+            // bit 15 of each word is the tsdf sign
             neg_any |= v.x | v.y | v.z | v.w;
             pos_any |= ~(v.x & v.y & v.z & v.w);
         } else {
+            // x and z are the tsdf of two voxels; -0.0f is not negative
             const bool n0 = __uint_as_float(v.x) < 0.f, n1 = __uint_as_float(v.z) < 0.f;
             neg_any |= (unsigned int)(n0 | n1) << 15;
             pos_any |= (unsigned int)(!n0 | !n1) << 15;
+        }
+    };
+    if (x0 + FTX <= nx && y0 + CTY <= ny && z0 + CTZ <= nz) {
+        int i = threadIdx.x;
+        for (; i + THREADS < NW; i += 2 * THREADS) {
+            const uint4 a = q[i], b = q[i + THREADS];
+            acc(a);
+            acc(b);
+        }
+        if (i < NW) acc(q[i]);
+    } else {
+        const int ry = ny - y0, rz = nz - z0, rx = nx - x0;
+        for (int i = threadIdx.x; i < WPR * ROWS; i += THREADS) {
+            const int r = i / WPR, w = i - r * WPR, lx = w * VPW;
+            const int lz = r / CTY, ly = r - lz * CTY;  // rows 0..8 of planes 0..8
+            if (ly >= ry || lz >= rz || lx >= rx) continue;
+            acc(q[(lz * FTY + ly) * WPR + w]);
         }
     }
     neg_any = __reduce_or_sync(0xffffffffu, neg_any & 0x8000u);
@@ -1366,14 +1393,18 @@ __device__ __forceinline__ bool fused_mixed(Smem &S, const typename Vox<VT>::T *
     return m == 3u;
 }
 
-__device__ __forceinline__ int ftidx(int lx, int ly, int lz) { return (lz * FTY + ly) * FTX + lx; }
+template <int FG>
+__device__ __forceinline__ int ftidx(int lx, int ly, int lz) { return (lz * FTY + ly) * FGeo<FG>::TX + lx; }
 
-template <int VT>
-__global__ void __launch_bounds__(THREADS, 3) mc_fused_kernel(const __grid_constant__ CUtensorMap map, FusedParams p) {
+template <int VT, int FG, int MINB>
+__global__ void __launch_bounds__(FGeo<FG>::NT, MINB) mc_fused_kernel(const __grid_constant__ CUtensorMap map,
+                                                                        FusedParams p) {
     using V = Vox<VT>;
     using T = typename V::T;
+    constexpr int FTX = FGeo<FG>::TX, FTILE = FGeo<FG>::TILE, THREADS = FGeo<FG>::NT, WARPS = FGeo<FG>::NWARP;
+    constexpr int FROWS = THREADS;
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    FusedSmem<VT> &S = *reinterpret_cast<FusedSmem<VT> *>(smem_raw);
+    FusedSmem<VT, FG> &S = *reinterpret_cast<FusedSmem<VT, FG> *>(smem_raw);
     const T *__restrict__ vol = static_cast<const T *>(p.vol);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int nx = p.nx, ny = p.ny, nz = p.nz;
@@ -1381,7 +1412,7 @@ __global__ void __launch_bounds__(THREADS, 3) mc_fused_kernel(const __grid_const
     const GenOut &o = p.out;
     const long long N = (long long)nx * ny * nz;
     for (int i = tid; i < 256 * 16; i += THREADS) (&S.tri[0][0])[i] = (&c_tri[0][0])[i];
-    S.nv[tid] = (tid == 0 || tid == 255) ? 0 : c_nverts[tid];
+    for (int c = tid; c < 256; c += THREADS) S.nv[c] = (c == 0 || c == 255) ? 0 : c_nverts[c];
     pdl_wait();  // the launch before (a writer of the volume or of the counters)
     unsigned int *ticket = &p.totals->cls_ticket;
     // thread 0: item -> origin and TMA load of its tile
@@ -1399,20 +1430,20 @@ __global__ void __launch_bounds__(THREADS, 3) mc_fused_kernel(const __grid_const
         mbar_arrive_expect_tx(&S.bar, FTILE * V::bytes);
         tma_load_3d(S.tile, &map, &S.bar, x0, y0, z0);
     };
-    // the next item's ticket, drawn one item ahead (thread 0)
-    unsigned int ptk = 0xffffffffu;
+    // Thread 0 draws the next item only when its tile can be loaded: a CTA
+    // never holds an item it has not started, so an item's count is
+    // published a tile load and a classification after it was drawn, never
+    // after another item's look-back or emission (which could chain waits
+    // across CTAs).
     auto refill = [&]() {
-        const int nxt = ptk < (unsigned int)p.nitems ? (int)ptk : -1;
-        stage_item(nxt);
-        if (nxt >= 0) ptk = atomicAdd(ticket, 1u);
+        const unsigned int t = atomicAdd(ticket, 1u);
+        stage_item(t < (unsigned int)p.nitems ? (int)t : -1);
     };
     if (tid == 0) {
         S.abort = 0;
         mbar_init(&S.bar, 1);
         fence_barrier_init();
-        const unsigned int t0 = atomicAdd(ticket, 1u);
-        stage_item(t0 < (unsigned int)p.nitems ? (int)t0 : -1);
-        if (t0 < (unsigned int)p.nitems) ptk = atomicAdd(ticket, 1u);
+        refill();
     }
     __syncthreads();
     const T *tile = reinterpret_cast<const T *>(S.tile);
@@ -1427,13 +1458,13 @@ __global__ void __launch_bounds__(THREADS, 3) mc_fused_kernel(const __grid_const
         if (tid == 0 && !mbar_wait(&S.bar, (uint32_t)(i & 1))) S.abort = 1;
         __syncthreads();
         if (S.abort) break;
-        const bool mixed = fused_mixed<VT>(S, tile, nx, ny, nz, x0, y0, z0);
+        const bool mixed = fused_mixed<VT, FG>(S, tile, nx, ny, nz, x0, y0, z0);
         unsigned int item_v = 0;  // soup vertices of the item
         if (mixed) {
             // row masks of the FG bricks (voxel rows y0..y0+8, z0..z0+8)
             for (int m = tid; m < FG * ROWS; m += THREADS) {
                 const int h = m / ROWS, r = m - h * ROWS, rz = r / CTY, ry = r - rz * CTY;
-                const T *row = tile + ftidx(h * BX, ry, rz);
+                const T *row = tile + ftidx<FG>(h * BX, ry, rz);
                 RowMask<VT>::build(row, row[BX], S.neg[m], S.dead[m]);
             }
             __syncthreads();
@@ -1517,6 +1548,15 @@ __global__ void __launch_bounds__(THREADS, 3) mc_fused_kernel(const __grid_const
         for (unsigned int v0 = warp * 32; v0 < item_v; v0 += THREADS) {
             const unsigned int v = v0 + lane;
             const bool valid = v < item_v;
+            // row of the chunk's first vertex (the same search in every lane)
+            int r0 = 0;
+            {
+                int hi = FROWS - 1;
+                while (r0 < hi) {
+                    const int mid = (r0 + hi + 1) >> 1;
+                    if (S.rowoff[mid] <= v0) r0 = mid; else hi = mid - 1;
+                }
+            }
             float P[3] = {0.f, 0.f, 0.f};
             int vox[3] = {0, 0, 0};
             short vt = 0, vw = 0;
@@ -1524,13 +1564,11 @@ __global__ void __launch_bounds__(THREADS, 3) mc_fused_kernel(const __grid_const
             long long cube_lin = 0;
             int kslot = 1;
             if (valid) {
-                // the cube row holding vertex v: the last row starting at or before it
-                int lo = 0, hi = FROWS - 1;
-                while (lo < hi) {
-                    const int mid = (lo + hi + 1) >> 1;
-                    if (S.rowoff[mid] <= v) lo = mid; else hi = mid - 1;
-                }
-                const int r = lo;
+                // the cube row holding vertex v: the last row starting at or
+                // before it, scanned forward from the row of the chunk's first
+                // vertex (32 consecutive vertices span a few rows)
+                int r = r0;
+                while (r + 1 < FROWS && S.rowoff[r + 1] <= v) ++r;
                 unsigned int j = v - S.rowoff[r];
                 // the cube of the row and the vertex's slot in it
                 unsigned int mm = S.rowocc[r];
@@ -1554,8 +1592,8 @@ __global__ void __launch_bounds__(THREADS, 3) mc_fused_kernel(const __grid_const
                 const int a = c_ea(e), bb = c_eb(e);
                 const int gx = x0 + lcx, gy = y0 + lcy, gz = z0 + lcz;
                 if (o.tri_cube) cube_lin = lin3(nx, ny, gx, gy, gz);
-                const float f0 = V::f(tile[ftidx(lcx + c_cx(a), lcy + c_cy(a), lcz + c_cz(a))]);
-                const float f1 = V::f(tile[ftidx(lcx + c_cx(bb), lcy + c_cy(bb), lcz + c_cz(bb))]);
+                const float f0 = V::f(tile[ftidx<FG>(lcx + c_cx(a), lcy + c_cy(a), lcz + c_cz(a))]);
+                const float f1 = V::f(tile[ftidx<FG>(lcx + c_cx(bb), lcy + c_cy(bb), lcz + c_cz(bb))]);
                 // getNodeCoo (:243-254) and vertex_interp (:256-264)
                 const float t = (0.0f - f0) / (f1 - f0 + 1e-15f);
                 const int ga[3] = {gx + c_cx(a), gy + c_cy(a), gz + c_cz(a)};
@@ -1578,7 +1616,7 @@ __global__ void __launch_bounds__(THREADS, 3) mc_fused_kernel(const __grid_const
                     inside &= vox[d] >= 0 && vox[d] < dims[d] && vox[d] - orgv[d] >= 0 && vox[d] - orgv[d] < tdim[d];
                 }
                 if (inside) {
-                    const T vv = tile[ftidx(vox[0] - x0, vox[1] - y0, vox[2] - z0)];
+                    const T vv = tile[ftidx<FG>(vox[0] - x0, vox[1] - y0, vox[2] - z0)];
                     vt = V::tsdf(vv);
                     vw = V::wt(vv);
                 }
@@ -1598,10 +1636,10 @@ __global__ void __launch_bounds__(THREADS, 3) mc_fused_kernel(const __grid_const
                     const int lx = ix - x0, ly = iy - y0, lz = iz - z0;
                     if (ix + 1 < nx && iy + 1 < ny && iz + 1 < nz && lx >= 0 && ly >= 0 && lz >= 0 &&
                         lx + 1 < FTX && ly + 1 < FTY && lz + 1 < FTZ) {
-                        const T smp[8] = {tile[ftidx(lx, ly, lz)],         tile[ftidx(lx + 1, ly, lz)],
-                                          tile[ftidx(lx + 1, ly + 1, lz)], tile[ftidx(lx, ly + 1, lz)],
-                                          tile[ftidx(lx, ly, lz + 1)],     tile[ftidx(lx + 1, ly, lz + 1)],
-                                          tile[ftidx(lx + 1, ly + 1, lz + 1)], tile[ftidx(lx, ly + 1, lz + 1)]};
+                        const T smp[8] = {tile[ftidx<FG>(lx, ly, lz)],         tile[ftidx<FG>(lx + 1, ly, lz)],
+                                          tile[ftidx<FG>(lx + 1, ly + 1, lz)], tile[ftidx<FG>(lx, ly + 1, lz)],
+                                          tile[ftidx<FG>(lx, ly, lz + 1)],     tile[ftidx<FG>(lx + 1, ly, lz + 1)],
+                                          tile[ftidx<FG>(lx + 1, ly + 1, lz + 1)], tile[ftidx<FG>(lx, ly + 1, lz + 1)]};
                         bool sent = false;
                         float sd[8];
 #pragma unroll
@@ -2082,7 +2120,7 @@ struct Scratch {
 
 // default launch configuration (the measured best on GB300; a context can
 // choose another through mcg_mc_set_config, e.g. from the autotuner)
-constexpr mcg_mc_config kDefaultMcConfig = {1, 4, 3, 0};
+constexpr mcg_mc_config kDefaultMcConfig = {0, 4, 3, 0};
 
 // Launch with programmatic stream serialisation: the kernel may start while
 // the kernel before it on the stream drains (it waits with pdl_wait).
@@ -2269,15 +2307,25 @@ Scratch ctx_scratch(mcg_context *ctx) {
                    ctx->h_totals_dev};
 }
 
-// The fused extraction applies to short2 volumes of at least one item box
-// (132 x 10 x 10) that TMA can describe; `map` receives the tensor map.
+// The fused extraction with FG bricks per item applies to short2 volumes of
+// at least one item box (FGeo<FG>::TX x 10 x 10) that TMA can describe; `map`
+// receives the tensor map.
+template <int FG>
 bool fused_applies(const mcg_volume *vol, CUtensorMap *map) {
+    constexpr int FTX = FGeo<FG>::TX;
     if (vol->voxel_type != MCG_VOXEL_SHORT2) return false;
     if (vol->nx < FTX || vol->ny < FTY || vol->nz < FTZ) return false;
     return encode_volume_map(map, vol->data, vol->nx, vol->ny, vol->nz, 4, FTX, FTY, FTZ);
 }
 
+// minimum resident CTAs per SM of the fused launch (shared memory bound)
+template <int FG>
+struct FMinB {
+    static constexpr int v = FG == 4 ? 3 : 5;
+};
+
 // One fused launch over the whole volume.
+template <int FG>
 cudaError_t launch_fused(mcg_context *ctx, const CUtensorMap &map, const mcg_volume *vol, const mcg_mesh_out *out,
                          cudaStream_t s) {
     const Geometry g = geometry(vol->nx, vol->ny, vol->nz);
@@ -2333,16 +2381,18 @@ cudaError_t launch_fused(mcg_context *ctx, const CUtensorMap &map, const mcg_vol
     p.out.tri_cube = out->tri_cube;
     p.out.cap = out->capacity_vertices;
     p.out.zlim = g.zlim;
-    const size_t smem = sizeof(FusedSmem<MCG_VOXEL_SHORT2>);
+    constexpr int NT = FGeo<FG>::NT;
+    auto kernel = mc_fused_kernel<MCG_VOXEL_SHORT2, FG, FMinB<FG>::v>;
+    const size_t smem = sizeof(FusedSmem<MCG_VOXEL_SHORT2, FG>);
     static int occ = 0;
-    if (!occ) occ = occupancy(mc_fused_kernel<MCG_VOXEL_SHORT2>, THREADS, smem);
+    if (!occ) occ = occupancy(kernel, NT, smem);
     long long grid = (long long)ctx->num_sms * occ;
     if (grid > nitems) grid = nitems;
     if (ctx->time_kernels) {
         e = cudaEventRecord(ctx->tk0, s);
         if (e != cudaSuccess) return e;
     }
-    e = launch_pdl(mc_fused_kernel<MCG_VOXEL_SHORT2>, (unsigned int)grid, THREADS, smem, s, map, p);
+    e = launch_pdl(kernel, (unsigned int)grid, NT, smem, s, map, p);
     if (e == cudaSuccess) e = cudaGetLastError();
     if (e == cudaSuccess && ctx->time_kernels) {
         e = cudaEventRecord(ctx->tk1, s);
@@ -2487,7 +2537,8 @@ mcg_status mcg_mc_extract(mcg_context *ctx, const mcg_volume *vol, const mcg_mes
         !out->tri_cube)
         return MCG_ERR_INVALID_ARG;
     CUtensorMap map;
-    if (ctx->mc_cfg.fused && fused_applies(vol, &map)) {
+    const int fused = ctx->mc_cfg.fused;
+    if ((fused == 1 && fused_applies<4>(vol, &map)) || (fused == 2 && fused_applies<2>(vol, &map))) {
         cudaStream_t s = (cudaStream_t)stream;
         cudaError_t e = cudaSetDevice(ctx->device);
         if (e == cudaSuccess) e = upload_tables(ctx->device);
@@ -2495,7 +2546,7 @@ mcg_status mcg_mc_extract(mcg_context *ctx, const mcg_volume *vol, const mcg_mes
             e = cudaEventCreate(&ctx->tk0);
             if (e == cudaSuccess) e = cudaEventCreate(&ctx->tk1);
         }
-        if (e == cudaSuccess) e = launch_fused(ctx, map, vol, out, s);
+        if (e == cudaSuccess) e = fused == 1 ? launch_fused<4>(ctx, map, vol, out, s) : launch_fused<2>(ctx, map, vol, out, s);
         ctx->counters_clean = e == cudaSuccess && ctx->h_totals_dev != nullptr;
         if (e == cudaSuccess && !ctx->h_totals_dev)
             e = cudaMemcpyAsync(ctx->h_totals, ctx->d_totals, sizeof(MeshTotals), cudaMemcpyDeviceToHost, s);
@@ -2532,7 +2583,7 @@ mcg_status mcg_mc_get_config(const mcg_context *ctx, mcg_mc_config *cfg) {
 
 mcg_status mcg_mc_set_config(mcg_context *ctx, const mcg_mc_config *cfg) {
     if (!ctx || !cfg) return MCG_ERR_INVALID_ARG;
-    if ((cfg->fused != 0 && cfg->fused != 1) || cfg->classify_shape < 0 || cfg->classify_shape > 5 ||
+    if (cfg->fused < 0 || cfg->fused > 2 || cfg->classify_shape < 0 || cfg->classify_shape > 5 ||
         cfg->gen_fixed_rounds < 0 || cfg->gen_fixed_rounds > 16 || cfg->reserved != 0)
         return MCG_ERR_INVALID_ARG;
     ctx->mc_cfg = *cfg;

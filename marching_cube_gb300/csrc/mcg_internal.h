@@ -99,7 +99,7 @@ struct mcg_context {
     int64_t last_capacity = -1;
     bool cls_indexed = false;        // the last classify was mcg_mc_classify_indexed
     bool cls_fused = false;          // the last count phase was a fused extraction (counts only, no brick list)
-    mcg_mc_config mc_cfg = {1, 4, 3, 0};  // launch configuration (mcg_mc_set_config)
+    mcg_mc_config mc_cfg = {0, 4, 3, 0};  // launch configuration (mcg_mc_set_config)
     int64_t last_capacity_tris = -1;  // indexed: triangle capacity of the last generate
 
     // batched extraction: device tables (volume descriptors, classify and

@@ -28,8 +28,8 @@ def _outputs(n, nvox):
             "tri_cube": torch.zeros((n // 3,), dtype=torch.int64, device="cuda")}
 
 
-def _extract(mcg, ctx, vol, cell, n, cap, fused):
-    ctx.set_config(fused=1 if fused else 0)
+def _extract(mcg, ctx, vol, cell, n, cap, mode):
+    ctx.set_config(fused=mode)
     nz, ny, nx, _ = vol.shape
     o = _outputs(n, nx * ny * nz)
     cv = _capi.Volume(vol.data_ptr(), nx, ny, nz, 0, float(cell))
@@ -42,12 +42,14 @@ def _extract(mcg, ctx, vol, cell, n, cap, fused):
     return o, c, st
 
 
-def _same_both(mcg, vol, cell, cap_frac=None):
+def _same_both(mcg, vol, cell, cap_frac=None, mode=1):
+    """The fused launch (mode 1: 4-brick items, 2: 2-brick items) against the
+    two launches, same capacity."""
     a, b = mcg.Context(), mcg.Context()
     n = mcg.extract(vol, cell).num_vertices
     cap = n if cap_frac is None else int(n * cap_frac)
-    o1, c1, s1 = _extract(mcg, a, vol, cell, n, cap, True)
-    o2, c2, s2 = _extract(mcg, b, vol, cell, n, cap, False)
+    o1, c1, s1 = _extract(mcg, a, vol, cell, n, cap, mode)
+    o2, c2, s2 = _extract(mcg, b, vol, cell, n, cap, 0)
     assert s1 == s2 and (c1.occupied, c1.triangles, c1.vertices, c1.active_bricks) == \
         (c2.occupied, c2.triangles, c2.vertices, c2.active_bricks)
     for k in KEYS:
@@ -57,13 +59,14 @@ def _same_both(mcg, vol, cell, cap_frac=None):
     return n, s1
 
 
-def test_fused_matches_two_pass_and_oracle(mcg, orc):
+@pytest.mark.parametrize("mode", [1, 2])
+def test_fused_matches_two_pass_and_oracle(mcg, orc, mode):
     vol = synthetic.sphere_volume(160, radius=50.0, seed=3)
     t = torch.from_numpy(vol).cuda()
-    n, st = _same_both(mcg, t, 0.01)
+    n, st = _same_both(mcg, t, 0.01, mode=mode)
     assert n > 10000 and st == 0
     ctx = mcg.Context()
-    assert ctx.config["fused"] == 1
+    ctx.set_config(fused=mode)
     o = _outputs(n, t.shape[0] * t.shape[1] * t.shape[2])
     mcg.extract_into(t, 0.01, o, n, ctx=ctx)
     torch.cuda.synchronize()
@@ -73,18 +76,20 @@ def test_fused_matches_two_pass_and_oracle(mcg, orc):
     ctx.close()
 
 
-def test_fused_many_groups_and_odd_sizes(mcg):
+@pytest.mark.parametrize("mode", [1, 2])
+def test_fused_many_groups_and_odd_sizes(mcg, mode):
     # more items than one window of look-back groups reaches, edges that are
     # not whole bricks or items, weight-0 holes, sentinel regions
-    for shape, seed in [((70, 90, 300), 1), ((48, 40, 260), 2), ((41, 64, 388), 4)]:
+    for shape, seed in [((70, 90, 300), 1), ((48, 40, 260), 2), ((41, 64, 388), 4), ((20, 12, 100), 6)]:
         v = synthetic.random_volume(shape, seed=seed, p_zero_weight=0.02, sentinel_frac=0.3)
-        _same_both(mcg, torch.from_numpy(v).cuda(), 0.02)
-    _same_both(mcg, synthetic.stress_volume(256, seed=5, n_spheres=40), 1.0 / 256)
+        _same_both(mcg, torch.from_numpy(v).cuda(), 0.02, mode=mode)
+    _same_both(mcg, synthetic.stress_volume(256, seed=5, n_spheres=40), 1.0 / 256, mode=mode)
 
 
-def test_fused_capacity_truncation(mcg):
+@pytest.mark.parametrize("mode", [1, 2])
+def test_fused_capacity_truncation(mcg, mode):
     vol = torch.from_numpy(synthetic.sphere_volume(140, radius=45.0, seed=6)).cuda()
-    n, st = _same_both(mcg, vol, 0.01, cap_frac=0.37)
+    n, st = _same_both(mcg, vol, 0.01, cap_frac=0.37, mode=mode)
     assert st == mcg.MCG_ERR_CAPACITY
 
 
@@ -95,7 +100,7 @@ def test_fused_consecutive_calls_and_state(mcg):
     # fused calls on one context, with a two-launch call between some of them
     for k, (v, ref) in enumerate(zip(vols + vols, refs + refs)):
         n = ref.num_vertices
-        ctx.set_config(fused=0 if k == 3 else 1)
+        ctx.set_config(fused=[1, 2, 1, 0, 2, 1][k])
         o = {"soup": torch.zeros((n, 28), dtype=torch.uint8, device="cuda"),
              "normals": torch.zeros((n, 3), dtype=torch.float32, device="cuda")}
         mcg.extract_into(v, 0.01, o, n, ctx=ctx)
@@ -116,11 +121,13 @@ def test_fused_consecutive_calls_and_state(mcg):
 
 def test_config_round_trip_and_validation(mcg):
     ctx = mcg.Context()
-    assert ctx.config == {"fused": 1, "classify_shape": 4, "gen_fixed_rounds": 3}
+    assert ctx.config == {"fused": 0, "classify_shape": 4, "gen_fixed_rounds": 3}
     ctx.set_config(classify_shape=2, gen_fixed_rounds=0, fused=0)
     assert ctx.config == {"fused": 0, "classify_shape": 2, "gen_fixed_rounds": 0}
     with pytest.raises(mcg.MCGError):
         ctx.set_config(classify_shape=6)
+    with pytest.raises(mcg.MCGError):
+        ctx.set_config(fused=3)
     with pytest.raises(KeyError):
         ctx.set_config(stages=2)
     ctx.close()
