@@ -784,6 +784,7 @@ def summarize(line):
         return round(x, 4) if isinstance(x, float) else x
     return {
         "headline_gvoxels_per_s": get("value"), "ms_per_step": get("ms_per_step"),
+        "launch_config": get("launch_config", "config"),
         "whole_step_frac": get("roofline", "whole_step", "frac"),
         "e2e_gvoxels_per_s": get("e2e", "value"),
         "full_outputs_ms": get("full_outputs", "ms_per_step"),
@@ -880,15 +881,25 @@ def main():
     s = ctypes.c_void_p(stream.cuda_stream)
     lib = mcg._lib
 
+    # the launch configuration: the library's autotuner times the candidates
+    # on this volume and sets the fastest on ctx (not part of the timed steps)
+    from marching_cube_gb300 import tune
+    t_tune = time.perf_counter()
+    tuned = tune.autotune(v.data, cell, ctx=ctx, reps=5, warmup=2, use_cache=False, store=False)
+    t_tune = time.perf_counter() - t_tune
+    fused = ctx.config["fused"] != 0
+
     def step(ev=None):
-        if ev is not None:
-            ev[0].record(stream)
+        """One extraction through mcg_mc_extract (with ev: the count and
+        generate launches called apart, events between them)."""
+        if ev is None:
+            ctx.check(lib.mcg_mc_extract(ctx.handle, ctypes.byref(cv), ctypes.byref(mo), s), "extract")
+            return
+        ev[0].record(stream)
         ctx.check(lib.mcg_mc_classify(ctx.handle, ctypes.byref(cv), s), "classify")
-        if ev is not None:
-            ev[1].record(stream)
+        ev[1].record(stream)
         ctx.check(lib.mcg_mc_generate(ctx.handle, ctypes.byref(cv), ctypes.byref(mo), s), "generate")
-        if ev is not None:
-            ev[2].record(stream)
+        ev[2].record(stream)
 
     for _ in range(max(args.warmup, 3)):
         step()
@@ -918,14 +929,16 @@ def main():
     ctx.check(lib.mcg_set_kernel_timing(ctx.handle, 1), "kernel timing")
     kms = []
     for i in range(nsplit):
-        step(evs[i])
+        # with the fused launch: its one kernel timed alone; otherwise the
+        # count / generate windows and the classify kernel alone
+        step(None if fused else evs[i])
         km = ctypes.c_float(0.0)
         ctx.check(lib.mcg_mc_count_kernel_ms(ctx.handle, ctypes.byref(km)), "count kernel time")
         kms.append(km.value)
     ctx.check(lib.mcg_set_kernel_timing(ctx.handle, 0), "kernel timing")
     torch.cuda.synchronize()
-    cls_ms = float(np.mean([e[0].elapsed_time(e[1]) for e in evs]))
-    gen_ms = float(np.mean([e[1].elapsed_time(e[2]) for e in evs]))
+    cls_ms = None if fused else float(np.mean([e[0].elapsed_time(e[1]) for e in evs]))
+    gen_ms = None if fused else float(np.mean([e[1].elapsed_time(e[2]) for e in evs]))
     cls_kernel_ms = float(np.mean(kms))
     c = mcg.counts(ctx)
     assert c["status"] == 0 and c["vertices"] == nvert
@@ -954,17 +967,24 @@ def main():
     # generate: active bricks' 32x8x8 voxels (4 B) + soup (28 B) + normals (12 B) per vertex
     out_bytes = nvert * (28 + 12)
     gen_bytes = out_bytes + 4 * 2048 * c["active_bricks"]
-    # per kernel: classify from the events around it alone, generate from its
-    # window (the generate call launches that one kernel)
-    cls_ach = cls_bytes / (cls_kernel_ms * 1e-3) / 1e9
-    gen_ach = gen_bytes / (gen_ms * 1e-3) / 1e9
-    per_kernel = {"mc_classify_kernel": {"ms": cls_kernel_ms, "alg_bytes": cls_bytes, "achieved": cls_ach,
-                                         "frac": cls_ach / hbm},
-                  "mc_generate_kernel": {"ms": gen_ms, "alg_bytes": gen_bytes, "achieved": gen_ach,
-                                         "frac": gen_ach / hbm}}
-    dominant = "mc_classify_kernel" if cls_kernel_ms >= gen_ms else "mc_generate_kernel"
-    achieved = per_kernel[dominant]["achieved"]
     alg_bytes = 4 * vox + out_bytes
+    if fused:
+        # the one fused kernel: the volume once + the soup and normals
+        f_ach = alg_bytes / (cls_kernel_ms * 1e-3) / 1e9
+        per_kernel = {"mc_fused_kernel": {"ms": cls_kernel_ms, "alg_bytes": alg_bytes, "achieved": f_ach,
+                                          "frac": f_ach / hbm}}
+        dominant = "mc_fused_kernel"
+    else:
+        # per kernel: classify from the events around it alone, generate from
+        # its window (the generate call launches that one kernel)
+        cls_ach = cls_bytes / (cls_kernel_ms * 1e-3) / 1e9
+        gen_ach = gen_bytes / (gen_ms * 1e-3) / 1e9
+        per_kernel = {"mc_classify_kernel": {"ms": cls_kernel_ms, "alg_bytes": cls_bytes, "achieved": cls_ach,
+                                             "frac": cls_ach / hbm},
+                      "mc_generate_kernel": {"ms": gen_ms, "alg_bytes": gen_bytes, "achieved": gen_ach,
+                                             "frac": gen_ach / hbm}}
+        dominant = "mc_classify_kernel" if cls_kernel_ms >= gen_ms else "mc_generate_kernel"
+    achieved = per_kernel[dominant]["achieved"]
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                 "traffic": None, "kernel": dominant, "peak_source": peak_src, "per_kernel": per_kernel,
                 "whole_step": {"alg_bytes": alg_bytes, "achieved_gbs": alg_bytes / (ms_per_step * 1e-3) / 1e9,
@@ -987,8 +1007,7 @@ def main():
             ta = time.perf_counter()
             for _ in range(reps):
                 d_vol.copy_(h_vol, non_blocking=True)
-                ctx.check(lib.mcg_mc_classify(ctx.handle, ctypes.byref(cv2), s), "classify")
-                ctx.check(lib.mcg_mc_generate(ctx.handle, ctypes.byref(cv2), ctypes.byref(mo), s), "generate")
+                ctx.check(lib.mcg_mc_extract(ctx.handle, ctypes.byref(cv2), ctypes.byref(mo), s), "extract")
                 h_soup.copy_(soup, non_blocking=True)
                 h_nrm.copy_(nrm, non_blocking=True)
                 torch.cuda.synchronize()
@@ -1006,6 +1025,8 @@ def main():
         # the public stream API: volume i+1's copy in overlaps volume i's
         # extraction and copy out (both link directions busy)
         xs = mcg.ExtractStream((n, n, n), float(cell), cap)
+        for xc in xs.ctx:
+            xc.set_config(**tuned["config"])
         outs = [{"soup": h_soup, "normals": h_nrm}]
         xs.run([h_vol] * 3, outs * 3)
         torch.cuda.synchronize()
@@ -1111,7 +1132,9 @@ def main():
                                   parallelism="replicas" if world > 1 else "single"),
         "occupied_cubes": counts["occupied"],
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-        "clocks": clk.summary(), "gpu_launches": 3 * args.steps,
+        "clocks": clk.summary(), "gpu_launches": (1 if fused else 3) * args.steps,
+        "launch_config": {"config": tuned["config"], "chosen_by": "marching_cube_gb300.tune.autotune on this volume",
+                          "tune_s": round(t_tune, 3), "candidates_ms": tuned["timings"]},
         "triangles_per_s": ntri * world / (ms_per_step * 1e-3),
         "full_outputs": full_outputs,
         "integrate": integ,
