@@ -117,6 +117,8 @@ mcg_status mcg_destroy(mcg_context *ctx) {
     cudaFree(ctx->icp_pose);
     cudaFree(ctx->icp_inlier);
     cudaFree(ctx->depth_scaled);
+    cudaFree(ctx->integ_rows);
+    cudaFree(ctx->integ_zmax);
     cudaFree(ctx->ray_x);
     if (ctx->h_ray_x) cudaFreeHost(ctx->h_ray_x);
     cudaFree(ctx->tr_text);

@@ -136,15 +136,24 @@ __global__ void vertex_to_normal_kernel(int w, int h, const float3 *__restrict__
 
 // ---- integrate ------------------------------------------------------------------
 // d_voxel_volumetric_depth_scaling (:416-425): z-depth -> distance along the ray
+// Also the largest ray-length depth of the frame into *zmax (as float bits,
+// atomic max; *zmax is zero before the launch): +inf when any value is not a
+// finite number, so that the row culling below then culls nothing by depth.
 __global__ void depth_scale_kernel(Intr k, int w, int h, const float *__restrict__ depth,
-                                   float *__restrict__ scaled) {
+                                   float *__restrict__ scaled, unsigned int *__restrict__ zmax) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
-    if (x >= w || y >= h) return;
-    const float px = ((float)x - k.cx) / k.fx;
-    const float py = ((float)y - k.cy) / k.fy;
-    const long long i = (long long)y * w + x;
-    scaled[i] = depth[i] * sqrtf(px * px + py * py + 1.0f);
+    unsigned int zb = 0;
+    if (x < w && y < h) {
+        const float px = ((float)x - k.cx) / k.fx;
+        const float py = ((float)y - k.cy) / k.fy;
+        const long long i = (long long)y * w + x;
+        const float d = depth[i] * sqrtf(px * px + py * py + 1.0f);
+        scaled[i] = d;
+        zb = isfinite(d) ? __float_as_uint(fmaxf(d, 0.0f)) : 0x7f800000u;
+    }
+    zb = __reduce_max_sync(0xffffffffu, zb);
+    if ((threadIdx.x + threadIdx.y * blockDim.x) % 32 == 0 && zb) atomicMax(zmax, zb);
 }
 
 struct IntegParams {
@@ -158,6 +167,7 @@ struct IntegParams {
     const float *ray_x;     // accumulated x coordinate per voxel column
     const float *pose_dev;  // if set: r[9], t[3] read from device memory (graph replay)
     int is_dynamic;
+    const int2 *rows;       // per (y, z) row: the voxels x0 .. x1 that can be updated (x1 < x0: none)
 };
 
 // pose from device memory into the block's copy of the parameters
@@ -270,6 +280,73 @@ __device__ __forceinline__ void fuse(const IntegParams &p, float sdf, float weig
     fuse_core(p.is_dynamic, sdf, weight, sdf1, w1, sdf2, w2);
 }
 
+// Row culling.  Along a voxel row (fixed y, z) the camera-frame point is
+// linear in the row's x coordinate X: q(X) = q(0) + X (r0, r3, r6).  A voxel
+// can be updated only if q_z > 0, its pixel lies inside the image (u in
+// [0, w-3], v in [0, h-3] after rounding) and q_z <= |q| <= zmax + min_t
+// (otherwise its sdf is below -min_t for every pixel).  With q_z > 0 each
+// image bound is a linear inequality in X (fx q_x + (cx - u_bound) q_z
+// against 0), so the row's candidates form one interval of X.  The bounds
+// are widened by one pixel and each inequality by an absolute 1e-3, which
+// covers the binary32 error of evaluating them, and the interval by two
+// voxels beyond its ends, which covers the accumulated x coordinates
+// (p.x += grid_s, :434-444); the exact per-voxel tests still decide.
+__global__ void __launch_bounds__(256) integrate_rows_kernel(IntegParams p, const unsigned int *__restrict__ zmax,
+                                                             int2 *__restrict__ rows) {
+    load_pose(p);
+    const long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= (long long)p.ny * p.nz) return;
+    const int y = (int)(row % p.ny), z = (int)(row / p.ny);
+    const float py = (float)y * p.grid_s, pz = (float)z * p.grid_s;
+    const float v1 = py - p.t[1], v2 = pz - p.t[2];
+    float A[3], B[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        A[k] = p.r[3 * k] * (-p.t[0]) + p.r[3 * k + 1] * v1 + p.r[3 * k + 2] * v2;
+        B[k] = p.r[3 * k];
+    }
+    const float zb = __uint_as_float(*zmax);
+    const float zlim = zb + p.min_t;
+    const float m = 1.0f;
+    const float xmax = (float)p.nx * p.grid_s + fabsf(p.grid_s);
+    // constraints a + b X >= -d_c, d_c 1e-5 of the constraint's terms' size
+    // (two orders above the binary32 error of evaluating them) plus 1e-3
+    float a[6], b[6], sz[6];
+    const float ul = p.k.cx + 1.0f + m, uh = (float)p.w - 2.0f + m - p.k.cx;
+    const float vl = p.k.cy + 1.0f + m, vh = (float)p.h - 2.0f + m - p.k.cy;
+    const float s0 = fabsf(p.r[0] * p.t[0]) + fabsf(p.r[1] * v1) + fabsf(p.r[2] * v2) + fabsf(B[0]) * xmax;
+    const float s1 = fabsf(p.r[3] * p.t[0]) + fabsf(p.r[4] * v1) + fabsf(p.r[5] * v2) + fabsf(B[1]) * xmax;
+    const float s2 = fabsf(p.r[6] * p.t[0]) + fabsf(p.r[7] * v1) + fabsf(p.r[8] * v2) + fabsf(B[2]) * xmax;
+    a[0] = A[2]; b[0] = B[2]; sz[0] = s2;                                                    // q_z >= 0
+    a[1] = p.k.fx * A[0] + ul * A[2]; b[1] = p.k.fx * B[0] + ul * B[2];                      // u >= -1 - m
+    sz[1] = fabsf(p.k.fx) * s0 + fabsf(ul) * s2;
+    a[2] = uh * A[2] - p.k.fx * A[0]; b[2] = uh * B[2] - p.k.fx * B[0];                      // u <= w - 2 + m
+    sz[2] = fabsf(uh) * s2 + fabsf(p.k.fx) * s0;
+    a[3] = p.k.fy * A[1] + vl * A[2]; b[3] = p.k.fy * B[1] + vl * B[2];                      // v >= -1 - m
+    sz[3] = fabsf(p.k.fy) * s1 + fabsf(vl) * s2;
+    a[4] = vh * A[2] - p.k.fy * A[1]; b[4] = vh * B[2] - p.k.fy * B[1];                      // v <= h - 2 + m
+    sz[4] = fabsf(vh) * s2 + fabsf(p.k.fy) * s1;
+    const int nc = isfinite(zlim) ? 6 : 5;
+    a[5] = zlim - A[2]; b[5] = -B[2]; sz[5] = fabsf(zlim) + s2;                              // q_z <= zmax + min_t
+    float lo = -INFINITY, hi = INFINITY;
+    bool empty = false;
+    for (int c = 0; c < nc; ++c) {
+        const float d = 1e-5f * sz[c] + 1e-3f;
+        const float t = (-d - a[c]);
+        if (b[c] > 0.0f) lo = fmaxf(lo, t / b[c]);
+        else if (b[c] < 0.0f) hi = fminf(hi, t / b[c]);
+        else if (a[c] < -d) empty = true;
+    }
+    int x0 = 0, x1 = -1;
+    if (!empty && !(lo > hi)) {
+        const float g = p.grid_s;
+        const float fl = floorf(lo / g) - 2.0f, fh = ceilf(hi / g) + 2.0f;
+        x0 = fl <= 0.0f ? 0 : (fl >= (float)p.nx ? p.nx : (int)fl);
+        x1 = fh >= (float)(p.nx - 1) ? p.nx - 1 : (fh < 0.0f ? -1 : (int)fh);
+    }
+    rows[row] = make_int2(x0, x1);
+}
+
 // short2 volume, 4 voxels per thread; vec = 16-byte path usable
 __global__ void __launch_bounds__(256) integrate_short2_kernel(IntegParams p, short2 *__restrict__ vol, int vec) {
     load_pose(p);
@@ -282,6 +359,8 @@ __global__ void __launch_bounds__(256) integrate_short2_kernel(IntegParams p, sh
     const int y = (int)(row % p.ny), z = (int)(row / p.ny);
     const float py = (float)y * p.grid_s, pz = (float)z * p.grid_s;
     const int x0 = g * 4;
+    const int2 span = p.rows[row];
+    if (x0 + 3 < span.x || x0 > span.y) return;
     float sdf[4], wt[4];
     unsigned int upd = 0;
 #pragma unroll
@@ -339,6 +418,8 @@ __global__ void __launch_bounds__(256) integrate_float2_kernel(IntegParams p, fl
     const int y = (int)(row % p.ny), z = (int)(row / p.ny);
     const float py = (float)y * p.grid_s, pz = (float)z * p.grid_s;
     const int x0 = g * 2;
+    const int2 span = p.rows[row];
+    if (x0 + 1 < span.x || x0 > span.y) return;
     float sdf[2], wt[2];
     unsigned int upd = 0;
 #pragma unroll
@@ -640,9 +721,16 @@ static mcg_status integrate_impl(mcg_context *ctx, void *vol, int32_t voxel_type
     p.normals = (const float3 *)normals;
     p.ray_x = ctx->ray_x;
     p.is_dynamic = is_dynamic ? 1 : 0;
-    const dim3 b2(32, 8), g2((w + 31) / 32, (h + 7) / 8);
-    depth_scale_kernel<<<g2, b2, 0, s>>>(p.k, w, h, depth_m, ctx->depth_scaled);
     const long long rows = (long long)ny * nz;
+    if (!ensure(&ctx->integ_rows, &ctx->integ_rows_cap, (size_t)rows) ||
+        !ensure(&ctx->integ_zmax, &ctx->integ_zmax_cap, (size_t)1))
+        return mcg_cuda_fail(ctx, cudaErrorMemoryAllocation);
+    p.rows = ctx->integ_rows;
+    e = cudaMemsetAsync(ctx->integ_zmax, 0, sizeof(unsigned int), s);
+    if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
+    const dim3 b2(32, 8), g2((w + 31) / 32, (h + 7) / 8);
+    depth_scale_kernel<<<g2, b2, 0, s>>>(p.k, w, h, depth_m, ctx->depth_scaled, ctx->integ_zmax);
+    integrate_rows_kernel<<<(unsigned int)((rows + 255) / 256), 256, 0, s>>>(p, ctx->integ_zmax, ctx->integ_rows);
     if (voxel_type == MCG_VOXEL_SHORT2) {
         const int vec = (nx % 4 == 0) && (((uintptr_t)vol & 15) == 0);
         const long long threads = (long long)((nx + 3) / 4) * rows;

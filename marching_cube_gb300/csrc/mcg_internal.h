@@ -174,6 +174,10 @@ struct mcg_context {
     // integrate scratch
     float *depth_scaled = nullptr;
     size_t depth_scaled_cap = 0;
+    int2 *integ_rows = nullptr;  // per voxel row: the candidate x interval of the frame
+    size_t integ_rows_cap = 0;
+    unsigned int *integ_zmax = nullptr;  // the frame's largest ray-length depth (float bits)
+    size_t integ_zmax_cap = 0;
     // x coordinates of the voxel centres as the reference accumulates them
     // (p.x += grid_s per voxel); cached per (nx, grid_s)
     float *ray_x = nullptr;
