@@ -110,18 +110,26 @@ __device__ __forceinline__ BrickPos slab_pos(long long b, int nbx, int nby, int 
 // Fill of a (DX, DY, DZ) tile whose origin is (ox, oy, oz) for volumes TMA
 // cannot describe: one asynchronous copy per voxel (cp.async, so all of a
 // thread's loads are in flight at once), zero-filled outside the volume like
-// the TMA fill.  Each thread waits for its own copies; the caller's barrier
-// then publishes the tile.
+// the TMA fill.  Thread t copies voxels t, t + blockDim.x, ... of the tile
+// in row-major order; its tile coordinates advance by the stride's fixed
+// decomposition with carries instead of a division per voxel.  Each thread
+// waits for its own copies (WAIT); the caller's barrier then publishes the
+// tile.
 template <int VT, int DX, int DY, int DZ, bool WAIT = true>
 __device__ __forceinline__ void fill_tile(typename Vox<VT>::T *tile, const typename Vox<VT>::T *__restrict__ vol,
                                           int nx, int ny, int nz, int ox, int oy, int oz) {
     constexpr int B = Vox<VT>::bytes;
-    for (int i = threadIdx.x; i < DX * DY * DZ; i += blockDim.x) {
-        const int lx = i % DX, t = i / DX, ly = t % DY, lz = t / DY;
+    constexpr int N = DX * DY * DZ;
+    const int S = blockDim.x;
+    // the stride in tile coordinates (S < DX * DY for every tile here)
+    const int sx = S % DX, sr = S / DX, sy = sr % DY, sz = sr / DY;
+    int i = threadIdx.x;
+    int lx = i % DX, t = i / DX, ly = t % DY, lz = t / DY;
+    for (; i < N; i += S) {
         const int gx = ox + lx, gy = oy + ly, gz = oz + lz;
         const bool in = gx >= 0 && gy >= 0 && gz >= 0 && gx < nx && gy < ny && gz < nz;
         // outside: no byte is read (source size 0) and the voxel is zero
-        const typename Vox<VT>::T *src = in ? vol + lin3(nx, ny, gx, gy, gz) : vol;
+        const typename Vox<VT>::T *src = in ? vol + ((long long)gz * ny + gy) * nx + gx : vol;
         const unsigned int n = in ? B : 0;
         if (B == 4)
             asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(smem_u32(tile + i)), "l"(src), "r"(n)
@@ -129,6 +137,17 @@ __device__ __forceinline__ void fill_tile(typename Vox<VT>::T *tile, const typen
         else
             asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(smem_u32(tile + i)), "l"(src), "r"(n)
                          : "memory");
+        lx += sx;
+        ly += sy;
+        lz += sz;
+        if (lx >= DX) {
+            lx -= DX;
+            ++ly;
+        }
+        if (ly >= DY) {
+            ly -= DY;
+            ++lz;
+        }
     }
     if (WAIT) cp_async_wait_all();
 }
