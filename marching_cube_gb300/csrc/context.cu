@@ -95,6 +95,8 @@ mcg_status mcg_destroy(mcg_context *ctx) {
         if (ctx->h_btab[k]) cudaFreeHost(ctx->h_btab[k]);
         if (ctx->btab_copied[k]) cudaEventDestroy(ctx->btab_copied[k]);
     }
+    for (unsigned char *b : ctx->btab_kept) cudaFreeHost(b);
+    for (unsigned char *b : ctx->btab_spare) cudaFreeHost(b);
     free(ctx->batch_tma);
     cudaFree(ctx->d_vol_sums);
     if (ctx->h_vol_sums) cudaFreeHost(ctx->h_vol_sums);
@@ -119,8 +121,7 @@ mcg_status mcg_destroy(mcg_context *ctx) {
     cudaFree(ctx->depth_scaled);
     cudaFree(ctx->integ_rows);
     cudaFree(ctx->integ_zmax);
-    cudaFree(ctx->ray_x);
-    if (ctx->h_ray_x) cudaFreeHost(ctx->h_ray_x);
+    for (const auto &r : ctx->ray_x) cudaFree(r.d);
     cudaFree(ctx->tr_text);
     cudaFree(ctx->tr_tok);
     cudaFree(ctx->tr_seg);

@@ -663,31 +663,39 @@ mcg_status mcg_vertex_to_normal(mcg_context *ctx, int32_t w, int32_t h, const fl
 }
 
 // x coordinate table, accumulated exactly as :434/:444 do
-static mcg_status ensure_ray_x(mcg_context *ctx, int32_t nx, float grid_s, cudaStream_t s) {
-    cudaError_t e;
-    if (ctx->ray_x_n != nx || ctx->ray_x_g != grid_s || !ctx->ray_x) {
-        if (!ensure(&ctx->ray_x, &ctx->ray_x_cap, (size_t)nx)) return mcg_cuda_fail(ctx, cudaErrorMemoryAllocation);
-        if (ctx->h_ray_x_cap < (size_t)nx) {
-            if (ctx->h_ray_x) cudaFreeHost(ctx->h_ray_x);
-            ctx->h_ray_x = nullptr;
-            ctx->h_ray_x_cap = 0;
-            if (cudaMallocHost((void **)&ctx->h_ray_x, sizeof(float) * nx) != cudaSuccess)
-                return mcg_cuda_fail(ctx, cudaErrorMemoryAllocation);
-            ctx->h_ray_x_cap = nx;
-        }
-        // the pinned table may still be in flight from an earlier call
-        e = cudaStreamSynchronize(s);
-        if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
-        volatile float px = -grid_s;
-        for (int x = 0; x < nx; ++x) {
-            px = px + grid_s;
-            ctx->h_ray_x[x] = px;
-        }
-        e = cudaMemcpyAsync(ctx->ray_x, ctx->h_ray_x, sizeof(float) * nx, cudaMemcpyHostToDevice, s);
-        if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
-        ctx->ray_x_n = nx;
-        ctx->ray_x_g = grid_s;
+// x coordinate of voxel column x as kf.cu:434-444 accumulates it: p.x starts
+// at 0 and grows by grid_s per voxel, in FP32, one addition after another
+__global__ void ray_x_kernel(float *__restrict__ out, int nx, float g) {
+    float px = -g;
+    for (int x = 0; x < nx; ++x) {
+        px = __fadd_rn(px, g);
+        out[x] = px;
     }
+}
+
+// the context's table for (nx, grid_s), built by one thread on stream s the
+// first time (and waited for); inside a stream capture a missing table is MCG_ERR_STATE (an
+// earlier call with this volume shape outside the capture builds it)
+static mcg_status ray_x_table(mcg_context *ctx, int32_t nx, float grid_s, cudaStream_t s, const float **out) {
+    for (const auto &r : ctx->ray_x)
+        if (r.nx == nx && __builtin_memcmp(&r.g, &grid_s, sizeof(float)) == 0) {
+            *out = r.d;
+            return MCG_OK;
+        }
+    if (mcg_capturing(s)) return MCG_ERR_STATE;
+    float *d = nullptr;
+    if (cudaMalloc((void **)&d, sizeof(float) * (size_t)nx) != cudaSuccess)
+        return mcg_cuda_fail(ctx, cudaErrorMemoryAllocation);
+    ray_x_kernel<<<1, 1, 0, s>>>(d, nx, grid_s);
+    // once per shape: complete before a call on another stream can use it
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        cudaFree(d);
+        return mcg_cuda_fail(ctx, e);
+    }
+    ctx->ray_x.push_back({nx, grid_s, d});
+    *out = d;
     return MCG_OK;
 }
 
@@ -703,10 +711,17 @@ static mcg_status integrate_impl(mcg_context *ctx, void *vol, int32_t voxel_type
     cudaStream_t s = (cudaStream_t)stream;
     cudaError_t e = cudaSetDevice(ctx->device);
     if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
+    const long long rows = (long long)ny * nz;
+    // inside a stream capture nothing may be allocated: an earlier call of
+    // the same shapes outside the capture has sized every buffer
+    if (mcg_capturing(s) && (ctx->depth_scaled_cap < (size_t)w * h || ctx->integ_rows_cap < (size_t)rows ||
+                             ctx->integ_zmax_cap < 1))
+        return MCG_ERR_STATE;
     if (!ensure(&ctx->depth_scaled, &ctx->depth_scaled_cap, (size_t)w * h))
         return mcg_cuda_fail(ctx, cudaErrorMemoryAllocation);
+    const float *ray_x = nullptr;
     {
-        const mcg_status st = ensure_ray_x(ctx, nx, grid_s, s);
+        const mcg_status st = ray_x_table(ctx, nx, grid_s, s, &ray_x);
         if (st != MCG_OK) return st;
     }
     IntegParams p;
@@ -719,9 +734,8 @@ static mcg_status integrate_impl(mcg_context *ctx, void *vol, int32_t voxel_type
     p.w = w; p.h = h;
     p.ds = ctx->depth_scaled;
     p.normals = (const float3 *)normals;
-    p.ray_x = ctx->ray_x;
+    p.ray_x = ray_x;
     p.is_dynamic = is_dynamic ? 1 : 0;
-    const long long rows = (long long)ny * nz;
     if (!ensure(&ctx->integ_rows, &ctx->integ_rows_cap, (size_t)rows) ||
         !ensure(&ctx->integ_zmax, &ctx->integ_zmax_cap, (size_t)1))
         return mcg_cuda_fail(ctx, cudaErrorMemoryAllocation);
@@ -778,7 +792,8 @@ mcg_status mcg_integrate_backward(mcg_context *ctx, const void *vol0, int32_t nx
     cudaStream_t s = (cudaStream_t)stream;
     cudaError_t e = cudaSetDevice(ctx->device);
     if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
-    const mcg_status st = ensure_ray_x(ctx, nx, grid_s, s);
+    const float *ray_x = nullptr;
+    const mcg_status st = ray_x_table(ctx, nx, grid_s, s, &ray_x);
     if (st != MCG_OK) return st;
     IntegBwParams p;
     p.nx = nx; p.ny = ny; p.nz = nz;
@@ -788,7 +803,7 @@ mcg_status mcg_integrate_backward(mcg_context *ctx, const void *vol0, int32_t nx
     p.poses = poses_dev;
     p.depth = depth_m;
     p.normals = (const float3 *)normals;
-    p.ray_x = ctx->ray_x;
+    p.ray_x = ray_x;
     p.is_dynamic = is_dynamic ? 1 : 0;
     p.vol0 = (const float2 *)vol0;
     p.grad_f = grad_f;

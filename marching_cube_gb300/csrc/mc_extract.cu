@@ -494,6 +494,50 @@ __global__ void __launch_bounds__(NT)
     }
 }
 
+// ---- batched extraction: shared definitions ----------------------------------------
+// Bricks of all volumes of a batch form one index space: volume v owns bricks
+// [brick_base, brick_base + nbricks).  A brick's volume is found by binary
+// search over the descriptor table; tiles come by TMA through the volume's
+// own tensor map (global memory) when TMA can describe it, by asynchronous
+// per-voxel copies otherwise.  Soup offsets come from one scan over all
+// bricks; a volume's soup starts at the offset of its first brick, i.e. 3x
+// the triangles of the volumes before it.
+struct VolDesc {
+    const void *data;
+    int nx, ny, nz;
+    float cell;
+    int nbx, nby;
+    int tma;
+    int pad;
+    long long brick_base;
+    long long nbricks;
+    mcg_vertex_voxel *soup;
+    float *normals;
+    int32_t *vi2vox;
+    int16_t *ver_voxel;
+    int64_t *tri_cube;
+    long long cap;
+};
+
+__device__ __forceinline__ int find_volume(const VolDesc *__restrict__ vols, int nvol, long long b) {
+    int lo = 0, hi = nvol - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (vols[mid].brick_base <= b) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// An active-list entry of a batch as the batch's scan writes it for the
+// generate launch: volume, brick origin and soup offset inside the volume's
+// soup, so the thread that stages the brick does no search.
+struct BatchBrick {
+    unsigned long long vbase;
+    int v, x0, y0, z0;
+    int pad[2];
+};
+static_assert(sizeof(BatchBrick) == 32, "two 16-byte copies");
+
 // ---- scan: brick counts -> soup offsets + active brick list ---------------------
 // One CTA per chunk of CHUNK consecutive bricks.  Classify has accumulated
 // each chunk's triangles, active bricks, occupied cubes and heavy bricks by
@@ -503,12 +547,22 @@ __global__ void __launch_bounds__(NT)
 // brick order, with each entry's soup offset beside it (list_vofs, when
 // given).  CTA 0 also writes the totals, to `host` as well when given (a
 // mapped host copy).  The last CTA to have read the chunk sums zeroes them for
-// the next count phase.
+// the next count phase.  Over a batch (BATCH) it also writes each active
+// entry's BatchBrick: the brick's volume, origin and offset in that volume's
+// soup, from the per-volume triangle sums of the count launch.
+struct ScanBatch {
+    const VolDesc *vols;
+    int nvol;
+    const unsigned long long *vol_sums;  // {triangles, occupied cubes} per volume
+    BatchBrick *list;                    // one entry per active-list entry
+};
+
+template <bool BATCH>
 __global__ void __launch_bounds__(CHUNK)
     mc_scan_kernel(const uint32_t *__restrict__ brick_tris, uint32_t *__restrict__ chunk, long long nb,
                    unsigned long long *__restrict__ brick_vofs, uint32_t *__restrict__ active,
                    unsigned long long *__restrict__ list_vofs, MeshTotals *__restrict__ totals,
-                   MeshTotals *__restrict__ host) {
+                   MeshTotals *__restrict__ host, ScanBatch bt) {
     // acc: [0] base tris, [1] base active, [2, 2+NH) base heavy per class,
     // [2+NH] all tris, [3+NH] all active, [4+NH] all occupied, [5+NH, 5+2NH) all heavy
     constexpr int NH = NHEAVY, NACC = 5 + 2 * NH, NF = NH + 2;  // scanned per brick: tris, classes, light
@@ -581,6 +635,31 @@ __global__ void __launch_bounds__(CHUNK)
         }
     }
     __syncthreads();
+    // BATCH: the soup start of each volume this chunk's bricks lie in (at
+    // most CHUNK volumes, each owning at least one brick): 3x the triangles
+    // of the volumes before it
+    __shared__ unsigned long long s_vpre[BATCH ? CHUNK : 1];
+    int vmin = 0;
+    if (BATCH) {
+        const long long first = j * CHUNK, last = (first + CHUNK < nb ? first + CHUNK : nb) - 1;
+        vmin = find_volume(bt.vols, bt.nvol, first);
+        const int vmax = find_volume(bt.vols, bt.nvol, last);
+        unsigned long long pre = 0;
+        for (int u = tid; u < vmin; u += CHUNK) pre += bt.vol_sums[2 * u];
+#pragma unroll
+        for (int o = 16; o; o >>= 1) pre += __shfl_xor_sync(0xffffffffu, pre, o);
+        if (lane == 0) s_part[0][warp] = pre;  // thread 0 read s_part before the barrier above
+        __syncthreads();
+        if (tid == 0) {
+            unsigned long long r = 0;
+            for (int w = 0; w < CHUNK / 32; ++w) r += s_part[0][w];
+            for (int v = vmin; v <= vmax; ++v) {
+                s_vpre[v - vmin] = 3ull * r;
+                r += bt.vol_sums[2 * v];
+            }
+        }
+        __syncthreads();
+    }
     const unsigned long long base_v = s_base_v;
     const long long b = j * CHUNK + tid;
     const unsigned int t = b < nb ? brick_tris[b] : 0u;
@@ -620,6 +699,19 @@ __global__ void __launch_bounds__(CHUNK)
                 const unsigned int w = s_base[k] + wp[1 + k] + x[1 + k] - 1;
                 active[w] = (uint32_t)b;
                 if (list_vofs) list_vofs[w] = v;
+                if (BATCH) {
+                    const int vb = find_volume(bt.vols, bt.nvol, b);
+                    const VolDesc &d = bt.vols[vb];
+                    const BrickPos bp = brick_pos(b - d.brick_base, d.nbx, d.nby);
+                    BatchBrick r;
+                    r.vbase = v - s_vpre[vb - vmin];
+                    r.v = vb;
+                    r.x0 = bp.x0;
+                    r.y0 = bp.y0;
+                    r.z0 = bp.z0;
+                    r.pad[0] = r.pad[1] = 0;
+                    bt.list[w] = r;
+                }
             }
     }
     if (s_last) {  // every CTA has read the chunk sums (and CTA 0 the flags)
@@ -1745,39 +1837,7 @@ __global__ void __launch_bounds__(FGeo<FG>::NT, MINB) mc_fused_kernel(const __gr
     }
 }
 
-// ---- batched extraction: many volumes, one launch per pass ------------------------
-// Bricks of all volumes form one index space: volume v owns bricks
-// [brick_base, brick_base + nbricks).  A brick's volume is found by binary
-// search over the descriptor table; tiles come by TMA through the volume's
-// own tensor map (global memory) when TMA can describe it, by plain loads
-// otherwise.  Soup offsets come from one scan over all bricks; each volume's
-// offsets start at its first brick's offset.
-struct VolDesc {
-    const void *data;
-    int nx, ny, nz;
-    float cell;
-    int nbx, nby;
-    int tma;
-    int pad;
-    long long brick_base;
-    long long nbricks;
-    mcg_vertex_voxel *soup;
-    float *normals;
-    int32_t *vi2vox;
-    int16_t *ver_voxel;
-    int64_t *tri_cube;
-    long long cap;
-};
-
-__device__ __forceinline__ int find_volume(const VolDesc *__restrict__ vols, int nvol, long long b) {
-    int lo = 0, hi = nvol - 1;
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (vols[mid].brick_base <= b) lo = mid; else hi = mid - 1;
-    }
-    return lo;
-}
-
+// ---- batched extraction: count and generate launches -------------------------------
 template <int VT>
 struct ClsSmemMulti {
     static constexpr int STAGE_BYTES = pad128(CTILE * Vox<VT>::bytes);
@@ -1943,38 +2003,6 @@ __global__ void __launch_bounds__(CTHREADS)
     if (S.abort && tid == 0) {
         atomicOr(flags, 1u);
         for (int s = 0; s < 2; ++s) mbar_wait(&S.bars[s], phase[s], 100000000ull);
-    }
-}
-
-// An active-list entry of a batch resolved for the generate launch: volume,
-// brick origin and soup offset inside the volume's soup.
-struct BatchBrick {
-    unsigned long long vbase;
-    int v, x0, y0, z0;
-    int pad[2];
-};
-static_assert(sizeof(BatchBrick) == 32, "two 16-byte copies");
-
-// One thread per active-list entry: the volume search, the brick origin and
-// the per-volume soup offset, done once here instead of by the thread that
-// stages the brick while its CTA waits.
-__global__ void mc_resolve_multi_kernel(const VolDesc *__restrict__ vols, int nvol, const uint32_t *__restrict__ active,
-                                        const unsigned long long *__restrict__ vofs,
-                                        const MeshTotals *__restrict__ totals, BatchBrick *__restrict__ out) {
-    const unsigned int n = totals->active_bricks;
-    for (unsigned int w = blockIdx.x * blockDim.x + threadIdx.x; w < n; w += gridDim.x * blockDim.x) {
-        const long long b = active[w];
-        const int v = find_volume(vols, nvol, b);
-        const long long base = vols[v].brick_base;
-        const BrickPos bp = brick_pos(b - base, vols[v].nbx, vols[v].nby);
-        BatchBrick r;
-        r.vbase = vofs[b] - vofs[base];
-        r.v = v;
-        r.x0 = bp.x0;
-        r.y0 = bp.y0;
-        r.z0 = bp.z0;
-        r.pad[0] = r.pad[1] = 0;
-        out[w] = r;
     }
 }
 
@@ -2251,8 +2279,8 @@ cudaError_t launch_count_phase(const mcg_volume *vol, const Geometry &g, const S
         const cudaError_t et = cudaEventRecord(t1, s);
         if (et != cudaSuccess) return et;
     }
-    launch_pdl(mc_scan_kernel, (unsigned int)num_chunks(g.nbricks), CHUNK, 0, s, (const uint32_t *)sc.tris, sc.chunk,
-               (long long)g.nbricks, sc.vofs, sc.active, sc.list_vofs, sc.totals, sc.host);
+    launch_pdl(mc_scan_kernel<false>, (unsigned int)num_chunks(g.nbricks), CHUNK, 0, s, (const uint32_t *)sc.tris,
+               sc.chunk, (long long)g.nbricks, sc.vofs, sc.active, sc.list_vofs, sc.totals, sc.host, ScanBatch{});
     return cudaGetLastError();
 }
 
@@ -2690,6 +2718,23 @@ mcg_status grow_pinned(mcg_context *ctx, int k, size_t n) {
     return MCG_OK;
 }
 
+// Two spare stagings of at least n bytes for a later capture of this batch
+// (its count and generate phases take one each); called outside captures.
+mcg_status top_up_spares(mcg_context *ctx, size_t n) {
+    if (ctx->btab_spare_cap < n) {
+        for (unsigned char *b : ctx->btab_spare) cudaFreeHost(b);
+        ctx->btab_spare.clear();
+        ctx->btab_spare_cap = n;
+    }
+    while (ctx->btab_spare.size() < 2) {
+        unsigned char *b = nullptr;
+        if (cudaMallocHost((void **)&b, ctx->btab_spare_cap) != cudaSuccess)
+            return mcg_cuda_fail(ctx, cudaErrorMemoryAllocation);
+        ctx->btab_spare.push_back(b);
+    }
+    return MCG_OK;
+}
+
 bool batch_ok(const mcg_volume *vols, int32_t nvol) {
     if (!vols || nvol < 1) return false;
     for (int v = 0; v < nvol; ++v) {
@@ -2703,11 +2748,29 @@ bool batch_ok(const mcg_volume *vols, int32_t nvol) {
 mcg_status upload_btab(mcg_context *ctx, const mcg_volume *vols, const mcg_mesh_out *outs, int32_t nvol,
                        bool with_maps, cudaStream_t s, long long *total_bricks) {
     const size_t bytes = btab_bytes(nvol);
-    if (!ensure(&ctx->d_btab, &ctx->d_btab_cap, bytes)) return mcg_cuda_fail(ctx, cudaErrorMemoryAllocation);
-    const int k = ctx->btab_slot;
-    mcg_status st = grow_pinned(ctx, k, bytes);
-    if (st != MCG_OK) return st;
-    ctx->btab_slot ^= 1;
+    // Outside a capture the table goes through the two pinned slots used in
+    // turn.  Inside one, the copy becomes a graph node that reads its source
+    // at every replay, so the table is staged in a spare that no other call
+    // writes again (kept until mcg_destroy); nothing may be allocated or
+    // waited for then, so an earlier call of the batch outside the capture
+    // has made the spares and sized the device table.
+    const bool cap = mcg_capturing(s);
+    unsigned char *hb = nullptr;
+    int k = -1;
+    if (cap) {
+        if (ctx->d_btab_cap < bytes || ctx->btab_spare.empty() || ctx->btab_spare_cap < bytes) return MCG_ERR_STATE;
+        hb = ctx->btab_spare.back();
+        ctx->btab_spare.pop_back();
+        ctx->btab_kept.push_back(hb);
+    } else {
+        if (!ensure(&ctx->d_btab, &ctx->d_btab_cap, bytes)) return mcg_cuda_fail(ctx, cudaErrorMemoryAllocation);
+        k = ctx->btab_slot;
+        mcg_status st = grow_pinned(ctx, k, bytes);
+        if (st == MCG_OK) st = top_up_spares(ctx, bytes);
+        if (st != MCG_OK) return st;
+        ctx->btab_slot ^= 1;
+        hb = ctx->h_btab[k];
+    }
     if (with_maps) {
         if (ctx->batch_tma_cap < (size_t)nvol) {
             unsigned char *t = static_cast<unsigned char *>(realloc(ctx->batch_tma, (size_t)nvol));
@@ -2718,7 +2781,6 @@ mcg_status upload_btab(mcg_context *ctx, const mcg_volume *vols, const mcg_mesh_
     } else if (ctx->batch_tma_cap < (size_t)nvol) {
         return MCG_ERR_STATE;
     }
-    unsigned char *hb = ctx->h_btab[k];
     VolDesc *desc = reinterpret_cast<VolDesc *>(hb);
     CUtensorMap *cmaps = reinterpret_cast<CUtensorMap *>(hb + btab_desc_bytes(nvol));
     CUtensorMap *gmaps = cmaps + nvol;
@@ -2764,12 +2826,9 @@ mcg_status upload_btab(mcg_context *ctx, const mcg_volume *vols, const mcg_mesh_
     *total_bricks = base;
     const size_t n = with_maps ? bytes : btab_desc_bytes(nvol);
     cudaError_t e = cudaMemcpyAsync(ctx->d_btab, hb, n, cudaMemcpyHostToDevice, s);
-    // during capture the staging copy becomes a graph node that reads the
-    // staging slot at every replay: it must then stay untouched
-    const bool cap = mcg_capturing(s);
     if (e == cudaSuccess && !cap) e = cudaEventRecord(ctx->btab_copied[k], s);
     if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
-    ctx->btab_pending[k] = !cap;
+    if (!cap) ctx->btab_pending[k] = true;
     return MCG_OK;
 }
 
@@ -2789,16 +2848,10 @@ void launch_classify_multi(mcg_context *ctx, int nvol, long long nbricks, cudaSt
 
 template <int VT>
 cudaError_t launch_generate_multi(mcg_context *ctx, int nvol, long long nbricks, cudaStream_t s) {
-    if (!ensure(&ctx->batch_list, &ctx->batch_list_cap, (size_t)nbricks * sizeof(BatchBrick)))
-        return cudaErrorMemoryAllocation;
     const VolDesc *desc = reinterpret_cast<const VolDesc *>(ctx->d_btab);
-    BatchBrick *list = reinterpret_cast<BatchBrick *>(ctx->batch_list);
+    const BatchBrick *list = reinterpret_cast<const BatchBrick *>(ctx->batch_list);  // written by the batch's scan
     cudaError_t e = cudaMemsetAsync(&ctx->d_totals->gen_ticket, 0, sizeof(unsigned int), s);
     if (e != cudaSuccess) return e;
-    long long rgrid = (nbricks + 255) / 256;
-    if (rgrid > 4LL * ctx->num_sms) rgrid = 4LL * ctx->num_sms;
-    mc_resolve_multi_kernel<<<(unsigned int)rgrid, 256, 0, s>>>(desc, nvol, ctx->active, ctx->brick_vofs,
-                                                                 ctx->d_totals, list);
     const size_t smem = sizeof(GenSmemMulti<VT>);
     static int occ = 0;
     if (!occ) occ = occupancy(mc_generate_multi_kernel<VT>, THREADS, smem);
@@ -2821,7 +2874,16 @@ mcg_status mcg_mc_classify_batched(mcg_context *ctx, const mcg_volume *vols, int
     long long nbricks = 0;
     for (int v = 0; v < nvol; ++v) nbricks += geometry(vols[v].nx, vols[v].ny, vols[v].nz).nbricks;
     if (nbricks >= (1ll << 32)) return MCG_ERR_INVALID_ARG;
-    if (!ensure(&ctx->brick_tris, &ctx->brick_tris_cap, (size_t)nbricks) ||
+    // inside a stream capture nothing may be allocated: an earlier call of
+    // the same batch outside the capture has sized every buffer
+    if (mcg_capturing(s) &&
+        (ctx->brick_tris_cap < (size_t)nbricks || ctx->brick_occ_cap < (size_t)(CHUNK_FIELDS * num_chunks(nbricks)) ||
+         ctx->brick_vofs_cap < (size_t)nbricks || ctx->active_cap < (size_t)nbricks ||
+         ctx->d_vol_sums_cap < (size_t)(2 * nvol) || ctx->h_vol_sums_cap < (size_t)(2 * nvol) ||
+         ctx->batch_list_cap < (size_t)nbricks * sizeof(BatchBrick)))
+        return MCG_ERR_STATE;
+    if (!ensure(&ctx->batch_list, &ctx->batch_list_cap, (size_t)nbricks * sizeof(BatchBrick)) ||
+        !ensure(&ctx->brick_tris, &ctx->brick_tris_cap, (size_t)nbricks) ||
         !ensure(&ctx->brick_occ, &ctx->brick_occ_cap, (size_t)(CHUNK_FIELDS * num_chunks(nbricks))) ||
         !ensure(&ctx->brick_vofs, &ctx->brick_vofs_cap, (size_t)nbricks) ||
         !ensure(&ctx->active, &ctx->active_cap, (size_t)nbricks) ||
@@ -2846,9 +2908,12 @@ mcg_status mcg_mc_classify_batched(mcg_context *ctx, const mcg_volume *vols, int
     if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
     if (vols[0].voxel_type == MCG_VOXEL_SHORT2) launch_classify_multi<MCG_VOXEL_SHORT2>(ctx, nvol, nbricks, s);
     else launch_classify_multi<MCG_VOXEL_FLOAT2>(ctx, nvol, nbricks, s);
-    mc_scan_kernel<<<(unsigned int)num_chunks(nbricks), CHUNK, 0, s>>>(ctx->brick_tris, ctx->brick_occ, nbricks,
-                                                                      ctx->brick_vofs, ctx->active, nullptr,
-                                                                      ctx->d_totals, nullptr);
+    {
+        const ScanBatch bt{reinterpret_cast<const VolDesc *>(ctx->d_btab), nvol, ctx->d_vol_sums,
+                           reinterpret_cast<BatchBrick *>(ctx->batch_list)};
+        mc_scan_kernel<true><<<(unsigned int)num_chunks(nbricks), CHUNK, 0, s>>>(
+            ctx->brick_tris, ctx->brick_occ, nbricks, ctx->brick_vofs, ctx->active, nullptr, ctx->d_totals, nullptr, bt);
+    }
     e = cudaGetLastError();
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(ctx->h_totals, ctx->d_totals, sizeof(MeshTotals), cudaMemcpyDeviceToHost, s);

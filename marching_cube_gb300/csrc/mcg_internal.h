@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <vector>
+
 #include "mcg.h"
 
 namespace mcg {
@@ -113,6 +115,13 @@ struct mcg_context {
     cudaEvent_t btab_copied[2] = {nullptr, nullptr};
     bool btab_pending[2] = {false, false};
     int btab_slot = 0;
+    // pinned stagings for batched calls inside a stream capture (the graph's
+    // copy node reads its source at every replay): two spares made by the
+    // last call outside a capture, and those a graph took, kept until
+    // mcg_destroy
+    std::vector<unsigned char *> btab_spare;
+    size_t btab_spare_cap = 0;
+    std::vector<unsigned char *> btab_kept;
     unsigned char *batch_tma = nullptr;  // per volume of the classified batch: both boxes encodable
     size_t batch_tma_cap = 0;
     unsigned long long *d_vol_sums = nullptr;
@@ -179,13 +188,15 @@ struct mcg_context {
     unsigned int *integ_zmax = nullptr;  // the frame's largest ray-length depth (float bits)
     size_t integ_zmax_cap = 0;
     // x coordinates of the voxel centres as the reference accumulates them
-    // (p.x += grid_s per voxel); cached per (nx, grid_s)
-    float *ray_x = nullptr;
-    size_t ray_x_cap = 0;
-    float *h_ray_x = nullptr;  // pinned staging copy
-    size_t h_ray_x_cap = 0;
-    int ray_x_n = 0;
-    float ray_x_g = 0.0f;
+    // (p.x += grid_s per voxel), one device table per (nx, grid_s) seen on
+    // this context, built once and never rewritten, so the calls on several
+    // volumes of a frame (and a graph captured around them) share them
+    struct RayX {
+        int nx;
+        float g;
+        float *d;
+    };
+    std::vector<RayX> ray_x;
 
     // text-record loader: the text on the device, its fields, per-segment
     // and per-CTA counts, the result block and pinned staging
