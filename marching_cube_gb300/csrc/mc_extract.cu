@@ -353,7 +353,7 @@ __global__ void __launch_bounds__(NT)
     extern __shared__ __align__(128) unsigned char smem_raw[];
     ClsSmemG<VT, G, XH, CSTAGES, NT> &S = *reinterpret_cast<ClsSmemG<VT, G, XH, CSTAGES, NT> *>(smem_raw);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    for (int c = tid; c < 256; c += NT) S.ntri[c] = (c == 0 || c == 255) ? 0 : c_nverts[c] / 3;
+    for (int c = tid; c < 256; c += NT) S.ntri[c] = (c == 0 || c == 255) ? 0 : g_nverts[c] / 3;
     // everything above touches only shared and constant memory: the launch may
     // overlap the kernel before it, whose writes (the volume, the counters) are
     // waited for here
@@ -1112,8 +1112,8 @@ __global__ void __launch_bounds__(THREADS, GEN_MINB) mc_generate_kernel(const __
     const int nx = p.nx, ny = p.ny, nz = p.nz;
     const float cell = p.cell;
 
-    for (int i = tid; i < 256 * 16; i += THREADS) (&S.tri[0][0])[i] = (&c_tri[0][0])[i];
-    S.nv[tid] = (tid == 0 || tid == 255) ? 0 : c_nverts[tid];
+    load_tri_table(S.tri, tid, THREADS);
+    S.nv[tid] = (tid == 0 || tid == 255) ? 0 : g_nverts[tid];
     if (tid == 0) {
         S.abort = 0;
         if (TMA) {
@@ -1503,8 +1503,8 @@ __global__ void __launch_bounds__(FGeo<FG>::NT, MINB) mc_fused_kernel(const __gr
     const float cell = p.cell;
     const GenOut &o = p.out;
     const long long N = (long long)nx * ny * nz;
-    for (int i = tid; i < 256 * 16; i += THREADS) (&S.tri[0][0])[i] = (&c_tri[0][0])[i];
-    for (int c = tid; c < 256; c += THREADS) S.nv[c] = (c == 0 || c == 255) ? 0 : c_nverts[c];
+    load_tri_table(S.tri, tid, THREADS);
+    for (int c = tid; c < 256; c += THREADS) S.nv[c] = (c == 0 || c == 255) ? 0 : g_nverts[c];
     pdl_wait();  // the launch before (a writer of the volume or of the counters)
     unsigned int *ticket = &p.totals->cls_ticket;
     // thread 0: item -> origin and TMA load of its tile
@@ -1903,7 +1903,7 @@ __global__ void __launch_bounds__(CTHREADS)
     const long long stride = gridDim.x;
     uint32_t phase[2] = {0, 0};
     VolCache vc;
-    for (int c = tid; c < 256; c += CTHREADS) S.ntri[c] = (c == 0 || c == 255) ? 0 : c_nverts[c] / 3;
+    for (int c = tid; c < 256; c += CTHREADS) S.ntri[c] = (c == 0 || c == 255) ? 0 : g_nverts[c] / 3;
     if (tid == 0) {
         S.abort = 0;
         for (int s = 0; s < 2; ++s) mbar_init(&S.bars[s], 1);
@@ -2041,8 +2041,8 @@ __global__ void __launch_bounds__(THREADS, 4)
     GenSmemMulti<VT> &S = *reinterpret_cast<GenSmemMulti<VT> *>(smem_raw);
     const int tid = threadIdx.x;
     uint32_t phase[2] = {0, 0};
-    for (int i = tid; i < 256 * 16; i += THREADS) (&S.tri[0][0])[i] = (&c_tri[0][0])[i];
-    S.nv[tid] = (tid == 0 || tid == 255) ? 0 : c_nverts[tid];
+    load_tri_table(S.tri, tid, THREADS);
+    S.nv[tid] = (tid == 0 || tid == 255) ? 0 : g_nverts[tid];
     const unsigned int nactive = totals->active_bricks;
     unsigned int *ticket = &totals->gen_ticket;
     const unsigned int grid = gridDim.x, c = blockIdx.x;

@@ -103,7 +103,7 @@ struct IdxSmem {
     long long sbrick[ISTAGES];
     unsigned int scan[ITHREADS];
     unsigned int wsum[IWARPS][4];
-    signed char tri[256][16];
+    alignas(16) signed char tri[256][16];
     unsigned char ntri[256];
     int abort;
 };
@@ -362,8 +362,8 @@ struct IdxParams {
 
 template <int VT>
 __device__ __forceinline__ void load_tables(IdxSmem<VT> &S) {
-    for (int i = threadIdx.x; i < 256 * 16; i += ITHREADS) (&S.tri[0][0])[i] = (&c_tri[0][0])[i];
-    for (int c = threadIdx.x; c < 256; c += ITHREADS) S.ntri[c] = (c == 0 || c == 255) ? 0 : c_nverts[c] / 3;
+    load_tri_table(S.tri, threadIdx.x, ITHREADS);
+    for (int c = threadIdx.x; c < 256; c += ITHREADS) S.ntri[c] = (c == 0 || c == 255) ? 0 : g_nverts[c] / 3;
 }
 
 // ---- pass 1: counts --------------------------------------------------------------
