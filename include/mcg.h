@@ -60,7 +60,8 @@ typedef struct mcg_intrinsic { float fx, fy, cx, cy; float dc[5]; } mcg_intrinsi
 typedef struct mcg_extrinsic { float r[9]; float t[3]; } mcg_extrinsic;
 
 /* structure.h:20-27 cu_voxel, minus the truncation fields.  data is a dense
- * [z][y][x] device array (x fastest, no pitch). */
+ * [z][y][x] device array (x fastest, no pitch), aligned to the voxel size
+ * (4 bytes for short2, 8 for float2; MCG_ERR_INVALID_ARG otherwise). */
 typedef struct mcg_volume {
     const void *data;
     int32_t nx, ny, nz;

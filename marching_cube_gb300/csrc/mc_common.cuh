@@ -1,7 +1,7 @@
 // Device and host helpers shared by the marching-cubes translation units
 // (mc_extract.cu: soup extraction and its adjoint; mc_indexed.cu: indexed
 // extraction).  Everything is in an anonymous namespace, so each unit has its
-// own copy of the constant-memory tables and uploads them itself.
+// own copy of the device tables and uploads them itself.
 #pragma once
 
 #include <cuda.h>
@@ -120,48 +120,76 @@ __device__ __forceinline__ BrickPos slab_pos(long long b, int nbx, int nby, int 
 }
 
 // Fill of a (DX, DY, DZ) tile whose origin is (ox, oy, oz) for volumes TMA
-// cannot describe: one asynchronous copy per voxel (cp.async, so all of a
-// thread's loads are in flight at once), zero-filled outside the volume like
-// the TMA fill.  Thread t copies voxels t, t + blockDim.x, ... of the tile
-// in row-major order; its tile coordinates advance by the stride's fixed
-// decomposition with carries instead of a division per voxel.  Each thread
-// waits for its own copies (WAIT); the caller's barrier then publishes the
-// tile.
+// cannot describe (rows not a multiple of 16 bytes, or a misaligned base),
+// zero outside the volume like the TMA fill.  Each thread writes whole
+// 16-byte words of tile rows: the voxels of a tile word lie in at most two
+// aligned 16-byte words of the volume, which are loaded whole and shifted
+// into place; the volume's first and last words, partly outside its
+// allocation, are read voxel by voxel.  Rows outside the volume and voxels
+// with x outside [0, nx) are zero.  The stores are plain shared-memory
+// stores (WAIT is kept for the callers' cp.async bookkeeping); the caller's
+// barrier publishes the tile.
+template <int VT>
+__device__ __forceinline__ uint4 vol_word(const uint4 *__restrict__ gbase, const typename Vox<VT>::T *__restrict__ vol,
+                                          long long k, long long klo, long long khi, int b0, long long N) {
+    constexpr int B = Vox<VT>::bytes, VPW = 16 / B;
+    if (k >= klo && k <= khi) return __ldg(gbase + k);
+    // partly (or wholly) outside the volume: voxel by voxel
+    unsigned int u[4] = {0u, 0u, 0u, 0u};
+#pragma unroll
+    for (int j = 0; j < VPW; ++j) {
+        const long long L = k * VPW + j - b0;
+        if (L >= 0 && L < N) {
+            const unsigned int *src = reinterpret_cast<const unsigned int *>(vol + L);
+#pragma unroll
+            for (int q = 0; q < B / 4; ++q) u[j * (B / 4) + q] = src[q];
+        }
+    }
+    return make_uint4(u[0], u[1], u[2], u[3]);
+}
+
 template <int VT, int DX, int DY, int DZ, bool WAIT = true>
 __device__ __forceinline__ void fill_tile(typename Vox<VT>::T *tile, const typename Vox<VT>::T *__restrict__ vol,
                                           int nx, int ny, int nz, int ox, int oy, int oz) {
-    constexpr int B = Vox<VT>::bytes;
-    constexpr int N = DX * DY * DZ;
-    const int S = blockDim.x;
-    // the stride in tile coordinates (S < DX * DY for every tile here)
-    const int sx = S % DX, sr = S / DX, sy = sr % DY, sz = sr / DY;
-    int i = threadIdx.x;
-    int lx = i % DX, t = i / DX, ly = t % DY, lz = t / DY;
-    for (; i < N; i += S) {
-        const int gx = ox + lx, gy = oy + ly, gz = oz + lz;
-        const bool in = gx >= 0 && gy >= 0 && gz >= 0 && gx < nx && gy < ny && gz < nz;
-        // outside: no byte is read (source size 0) and the voxel is zero
-        const typename Vox<VT>::T *src = in ? vol + ((long long)gz * ny + gy) * nx + gx : vol;
-        const unsigned int n = in ? B : 0;
-        if (B == 4)
-            asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(smem_u32(tile + i)), "l"(src), "r"(n)
-                         : "memory");
-        else
-            asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(smem_u32(tile + i)), "l"(src), "r"(n)
-                         : "memory");
-        lx += sx;
-        ly += sy;
-        lz += sz;
-        if (lx >= DX) {
-            lx -= DX;
-            ++ly;
+    constexpr int B = Vox<VT>::bytes, VPW = 16 / B, WPR = DX / VPW, NWORDS = WPR * DY * DZ, UPV = B / 4;
+    static_assert(DX % VPW == 0, "tile rows hold whole 16-byte words");
+    const long long N = (long long)nx * ny * nz;
+    // voxel offsets below are counted from the 16-byte boundary at or below vol
+    const int b0 = (int)((reinterpret_cast<uintptr_t>(vol) & 15u) / B);
+    const uint4 *gbase = reinterpret_cast<const uint4 *>(reinterpret_cast<uintptr_t>(vol) & ~(uintptr_t)15);
+    const long long klo = b0 > 0 ? 1 : 0, khi = (b0 + N) / VPW - 1;  // words wholly inside the volume
+    uint4 *dst = reinterpret_cast<uint4 *>(tile);
+    for (int i = threadIdx.x; i < NWORDS; i += blockDim.x) {
+        const int w = i % WPR, r = i / WPR, ly = r % DY, lz = r / DY;
+        const int gy = oy + ly, gz = oz + lz, gx0 = ox + w * VPW;
+        uint4 out = make_uint4(0u, 0u, 0u, 0u);
+        if (gy >= 0 && gy < ny && gz >= 0 && gz < nz && gx0 + VPW > 0 && gx0 < nx) {
+            const long long A = ((long long)gz * ny + gy) * nx + gx0 + b0;
+            const long long k0 = A >> (VPW == 4 ? 2 : 1);  // floor, also below the base
+            const int m = (int)(A & (VPW - 1));
+            const uint4 a = vol_word<VT>(gbase, vol, k0, klo, khi, b0, N);
+            const uint4 c = m ? vol_word<VT>(gbase, vol, k0 + 1, klo, khi, b0, N) : make_uint4(0u, 0u, 0u, 0u);
+            // the 4 words starting at word m * UPV of the window (a, c)
+            switch (m * UPV) {
+                case 0: out = a; break;
+                case 1: out = make_uint4(a.y, a.z, a.w, c.x); break;
+                case 2: out = make_uint4(a.z, a.w, c.x, c.y); break;
+                default: out = make_uint4(a.w, c.x, c.y, c.z); break;
+            }
+            if (gx0 < 0 || gx0 + VPW > nx) {
+                unsigned int u[4] = {out.x, out.y, out.z, out.w};
+#pragma unroll
+                for (int j = 0; j < VPW; ++j)
+                    if (gx0 + j < 0 || gx0 + j >= nx) {
+#pragma unroll
+                        for (int q = 0; q < UPV; ++q) u[j * UPV + q] = 0u;
+                    }
+                out = make_uint4(u[0], u[1], u[2], u[3]);
+            }
         }
-        if (ly >= DY) {
-            ly -= DY;
-            ++lz;
-        }
+        dst[i] = out;
     }
-    if (WAIT) cp_async_wait_all();
+    (void)WAIT;
 }
 
 // ---- normals (cu_kinect_fusion_v1.cu:3146-3225) -----------------------------------
@@ -289,6 +317,8 @@ bool vol_ok(const mcg_volume *v) {
     if (v->nx < 2 || v->ny < 2 || v->nz < 2) return false;
     if (v->voxel_type != MCG_VOXEL_SHORT2 && v->voxel_type != MCG_VOXEL_FLOAT2) return false;
     if (!(v->cell > 0.0f)) return false;
+    // voxels are read whole: the data is aligned to the voxel size
+    if (reinterpret_cast<uintptr_t>(v->data) % (v->voxel_type == MCG_VOXEL_SHORT2 ? 4u : 8u)) return false;
     // brick ids are 32-bit in the active list
     if (geometry(v->nx, v->ny, v->nz).nbricks >= (1ll << 32)) return false;
     return true;

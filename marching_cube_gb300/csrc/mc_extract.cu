@@ -718,6 +718,7 @@ __global__ void __launch_bounds__(CHUNK)
         for (long long i = tid; i < nchunks * CHUNK_FIELDS; i += CHUNK) chunk[i] = 0;
         if (tid == 0) {
             totals->scan_done = 0;
+            if (BATCH) totals->gen_ticket = 0;  // the batch's generate launch draws from it
             if (host) {  // the flags live on in the host copy
                 totals->flags = 0;
                 totals->cls_ticket = 0;
@@ -2000,6 +2001,7 @@ __global__ void __launch_bounds__(CTHREADS)
         }
     }
     cp_async_wait_all();
+    pdl_trigger();  // the scan may be scheduled (it waits for this grid's completion)
     if (S.abort && tid == 0) {
         atomicOr(flags, 1u);
         for (int s = 0; s < 2; ++s) mbar_wait(&S.bars[s], phase[s], 100000000ull);
@@ -2043,6 +2045,7 @@ __global__ void __launch_bounds__(THREADS, 4)
     uint32_t phase[2] = {0, 0};
     load_tri_table(S.tri, tid, THREADS);
     S.nv[tid] = (tid == 0 || tid == 255) ? 0 : g_nverts[tid];
+    pdl_wait();  // the batch's scan: active list, totals, cleared counter
     const unsigned int nactive = totals->active_bricks;
     unsigned int *ticket = &totals->gen_ticket;
     const unsigned int grid = gridDim.x, c = blockIdx.x;
@@ -2694,6 +2697,19 @@ mcg_status mcg_mc_backward(mcg_context *ctx, const mcg_volume *vol, const float 
     return e == cudaSuccess ? MCG_OK : mcg_cuda_fail(ctx, e);
 }
 
+// Zeroes what a batch's count launch accumulates into: the flags, the
+// generate counter, the per-volume sums and the chunk sums.
+__global__ void mc_batch_reset_kernel(MeshTotals *totals, unsigned long long *__restrict__ vol_sums, int nvol,
+                                      uint32_t *__restrict__ chunk, long long nchunk_words) {
+    const long long i0 = (long long)blockIdx.x * blockDim.x + threadIdx.x, st = (long long)gridDim.x * blockDim.x;
+    if (i0 == 0) {
+        totals->flags = 0;
+        totals->gen_ticket = 0;
+    }
+    for (long long i = i0; i < 2LL * nvol; i += st) vol_sums[i] = 0;
+    for (long long i = i0; i < nchunk_words; i += st) chunk[i] = 0;
+}
+
 // ---- batched extraction host side -------------------------------------------------
 namespace mcg {
 namespace {
@@ -2846,36 +2862,33 @@ void launch_classify_multi(mcg_context *ctx, int nvol, long long nbricks, cudaSt
                                                                     &ctx->d_totals->flags);
 }
 
+// generate launch of a batch, chained to the batch's scan (programmatic
+// dependent launch: its prologue overlaps the scan's tail)
 template <int VT>
 cudaError_t launch_generate_multi(mcg_context *ctx, int nvol, long long nbricks, cudaStream_t s) {
     const VolDesc *desc = reinterpret_cast<const VolDesc *>(ctx->d_btab);
     const BatchBrick *list = reinterpret_cast<const BatchBrick *>(ctx->batch_list);  // written by the batch's scan
-    cudaError_t e = cudaMemsetAsync(&ctx->d_totals->gen_ticket, 0, sizeof(unsigned int), s);
-    if (e != cudaSuccess) return e;
     const size_t smem = sizeof(GenSmemMulti<VT>);
     static int occ = 0;
     if (!occ) occ = occupancy(mc_generate_multi_kernel<VT>, THREADS, smem);
     long long grid = (long long)ctx->num_sms * occ;
     if (grid > nbricks) grid = nbricks;
     const CUtensorMap *gmaps = reinterpret_cast<const CUtensorMap *>(ctx->d_btab + btab_desc_bytes(nvol)) + nvol;
-    mc_generate_multi_kernel<VT><<<(int)grid, THREADS, smem, s>>>(desc, gmaps, nvol, list, ctx->d_totals);
-    return cudaGetLastError();
+    return launch_pdl(mc_generate_multi_kernel<VT>, (unsigned int)grid, THREADS, smem, s, desc, gmaps, nvol, list,
+                      ctx->d_totals);
 }
 
-}  // namespace
-}  // namespace mcg
-
-mcg_status mcg_mc_classify_batched(mcg_context *ctx, const mcg_volume *vols, int32_t nvol, mcg_stream_t stream) {
-    if (!ctx || !batch_ok(vols, nvol)) return MCG_ERR_INVALID_ARG;
-    cudaStream_t s = (cudaStream_t)stream;
-    cudaError_t e = cudaSetDevice(ctx->device);
-    if (e == cudaSuccess) e = upload_tables(ctx->device);
-    if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
+// Bricks of a batch, or -1 when a volume or the sum is out of range.
+long long batch_bricks(const mcg_volume *vols, int32_t nvol) {
     long long nbricks = 0;
     for (int v = 0; v < nvol; ++v) nbricks += geometry(vols[v].nx, vols[v].ny, vols[v].nz).nbricks;
-    if (nbricks >= (1ll << 32)) return MCG_ERR_INVALID_ARG;
-    // inside a stream capture nothing may be allocated: an earlier call of
-    // the same batch outside the capture has sized every buffer
+    return nbricks >= (1ll << 32) ? -1 : nbricks;
+}
+
+// Sizes the context's scratch for a batch.  Inside a stream capture nothing
+// may be allocated: an earlier call of the same batch outside the capture
+// has sized every buffer (MCG_ERR_STATE otherwise).
+mcg_status batch_scratch(mcg_context *ctx, int32_t nvol, long long nbricks, cudaStream_t s) {
     if (mcg_capturing(s) &&
         (ctx->brick_tris_cap < (size_t)nbricks || ctx->brick_occ_cap < (size_t)(CHUNK_FIELDS * num_chunks(nbricks)) ||
          ctx->brick_vofs_cap < (size_t)nbricks || ctx->active_cap < (size_t)nbricks ||
@@ -2898,32 +2911,43 @@ mcg_status mcg_mc_classify_batched(mcg_context *ctx, const mcg_volume *vols, int
             return mcg_cuda_fail(ctx, cudaErrorMemoryAllocation);
         ctx->h_vol_sums_cap = 2 * nvol;
     }
-    long long total = 0;
-    mcg_status st = upload_btab(ctx, vols, nullptr, nvol, true, s, &total);
-    if (st != MCG_OK) return st;
-    ctx->counters_clean = false;  // the batched launches leave the counters in use
-    e = cudaMemsetAsync(&ctx->d_totals->flags, 0, sizeof(unsigned int), s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(ctx->brick_occ, 0, sizeof(uint32_t) * CHUNK_FIELDS * num_chunks(nbricks), s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(ctx->d_vol_sums, 0, sizeof(unsigned long long) * 2 * nvol, s);
-    if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
-    if (vols[0].voxel_type == MCG_VOXEL_SHORT2) launch_classify_multi<MCG_VOXEL_SHORT2>(ctx, nvol, nbricks, s);
+    return MCG_OK;
+}
+
+// The count launches of a batch whose table is on the device: one reset
+// launch for the counters, the count pass, the scan (which also resolves
+// the active list for the generate launch).
+cudaError_t launch_batch_count(mcg_context *ctx, int32_t vtype, int32_t nvol, long long nbricks, cudaStream_t s) {
+    const long long cw = (long long)CHUNK_FIELDS * num_chunks(nbricks);
+    long long rg = (cw + 255) / 256;
+    if (rg < 1) rg = 1;
+    if (rg > 4LL * ctx->num_sms) rg = 4LL * ctx->num_sms;
+    mc_batch_reset_kernel<<<(unsigned int)rg, 256, 0, s>>>(ctx->d_totals, ctx->d_vol_sums, nvol, ctx->brick_occ, cw);
+    if (vtype == MCG_VOXEL_SHORT2) launch_classify_multi<MCG_VOXEL_SHORT2>(ctx, nvol, nbricks, s);
     else launch_classify_multi<MCG_VOXEL_FLOAT2>(ctx, nvol, nbricks, s);
-    {
-        const ScanBatch bt{reinterpret_cast<const VolDesc *>(ctx->d_btab), nvol, ctx->d_vol_sums,
-                           reinterpret_cast<BatchBrick *>(ctx->batch_list)};
-        mc_scan_kernel<true><<<(unsigned int)num_chunks(nbricks), CHUNK, 0, s>>>(
-            ctx->brick_tris, ctx->brick_occ, nbricks, ctx->brick_vofs, ctx->active, nullptr, ctx->d_totals, nullptr, bt);
-    }
-    e = cudaGetLastError();
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(ctx->h_totals, ctx->d_totals, sizeof(MeshTotals), cudaMemcpyDeviceToHost, s);
+    const ScanBatch bt{reinterpret_cast<const VolDesc *>(ctx->d_btab), nvol, ctx->d_vol_sums,
+                       reinterpret_cast<BatchBrick *>(ctx->batch_list)};
+    launch_pdl(mc_scan_kernel<true>, (unsigned int)num_chunks(nbricks), CHUNK, 0, s, (const uint32_t *)ctx->brick_tris,
+               ctx->brick_occ, nbricks, ctx->brick_vofs, ctx->active, (unsigned long long *)nullptr, ctx->d_totals,
+               (MeshTotals *)nullptr, bt);
+    return cudaGetLastError();
+}
+
+// the totals and per-volume sums to the host copies, marked pending
+cudaError_t batch_counts_out(mcg_context *ctx, int32_t nvol, cudaStream_t s) {
+    cudaError_t e = cudaMemcpyAsync(ctx->h_totals, ctx->d_totals, sizeof(MeshTotals), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(ctx->h_vol_sums, ctx->d_vol_sums, sizeof(unsigned long long) * 2 * nvol,
                             cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = mcg_counts_event(ctx, s);
-    if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
+    return e;
+}
+
+// host state after a batch's count launches
+void batch_state(mcg_context *ctx, const mcg_volume *vols, int32_t nvol, long long nbricks) {
+    ctx->counters_clean = false;  // the batched launches leave the counters in use
     ctx->batch_classified = true;
-    ctx->cls_fused = false;  // the batch's scan wrote the totals
+    ctx->cls_fused = false;       // the batch's scan wrote the totals
     ctx->batch_nvol = nvol;
     ctx->batch_nbricks = nbricks;
     ctx->batch_vtype = vols[0].voxel_type;
@@ -2935,6 +2959,28 @@ mcg_status mcg_mc_classify_batched(mcg_context *ctx, const mcg_volume *vols, int
     }
     for (int v = 0; v < nvol; ++v) ctx->batch_caps[v] = -1;
     ctx->classified = false;  // the single-volume state no longer matches the scratch
+}
+
+}  // namespace
+}  // namespace mcg
+
+mcg_status mcg_mc_classify_batched(mcg_context *ctx, const mcg_volume *vols, int32_t nvol, mcg_stream_t stream) {
+    if (!ctx || !batch_ok(vols, nvol)) return MCG_ERR_INVALID_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e == cudaSuccess) e = upload_tables(ctx->device);
+    if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
+    const long long nbricks = batch_bricks(vols, nvol);
+    if (nbricks < 0) return MCG_ERR_INVALID_ARG;
+    mcg_status st = batch_scratch(ctx, nvol, nbricks, s);
+    if (st != MCG_OK) return st;
+    long long total = 0;
+    st = upload_btab(ctx, vols, nullptr, nvol, true, s, &total);
+    if (st != MCG_OK) return st;
+    e = launch_batch_count(ctx, vols[0].voxel_type, nvol, nbricks, s);
+    if (e == cudaSuccess) e = batch_counts_out(ctx, nvol, s);
+    if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
+    batch_state(ctx, vols, nvol, nbricks);
     return MCG_OK;
 }
 
@@ -2983,6 +3029,9 @@ mcg_status mcg_mc_generate_batched(mcg_context *ctx, const mcg_volume *vols, con
     mcg_status st = upload_btab(ctx, vols, outs, nvol, false, s, &total);
     if (st != MCG_OK) return st;
     if (total != ctx->batch_nbricks) return MCG_ERR_STATE;
+    // the scan cleared the counter; calls on the context since may have used it
+    e = cudaMemsetAsync(&ctx->d_totals->gen_ticket, 0, sizeof(unsigned int), s);
+    if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
     if (vols[0].voxel_type == MCG_VOXEL_SHORT2) e = launch_generate_multi<MCG_VOXEL_SHORT2>(ctx, nvol, total, s);
     else e = launch_generate_multi<MCG_VOXEL_FLOAT2>(ctx, nvol, total, s);
     if (e == cudaSuccess)
@@ -2995,9 +3044,38 @@ mcg_status mcg_mc_generate_batched(mcg_context *ctx, const mcg_volume *vols, con
 
 mcg_status mcg_mc_extract_batched(mcg_context *ctx, const mcg_volume *vols, const mcg_mesh_out *outs, int32_t nvol,
                                   mcg_stream_t stream) {
-    mcg_status st = mcg_mc_classify_batched(ctx, vols, nvol, stream);
+    // count and generate without a host round trip in between: one table
+    // upload (volumes, tensor maps and outputs), the reset, count, scan and
+    // generate launches chained on the device, one copy of the counts at the end
+    if (!ctx || !batch_ok(vols, nvol) || !outs) return MCG_ERR_INVALID_ARG;
+    for (int v = 0; v < nvol; ++v)
+        if (outs[v].capacity_vertices < 0) return MCG_ERR_INVALID_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e == cudaSuccess) e = upload_tables(ctx->device);
+    if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
+    const long long nbricks = batch_bricks(vols, nvol);
+    if (nbricks < 0) return MCG_ERR_INVALID_ARG;
+    mcg_status st = batch_scratch(ctx, nvol, nbricks, s);
     if (st != MCG_OK) return st;
-    return mcg_mc_generate_batched(ctx, vols, outs, nvol, stream);
+    for (int v = 0; v < nvol; ++v)
+        if (outs[v].ver_voxel) {
+            e = cudaMemsetAsync(outs[v].ver_voxel, 0, sizeof(int16_t) * (size_t)vols[v].nx * vols[v].ny * vols[v].nz, s);
+            if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
+        }
+    long long total = 0;
+    st = upload_btab(ctx, vols, outs, nvol, true, s, &total);
+    if (st != MCG_OK) return st;
+    e = launch_batch_count(ctx, vols[0].voxel_type, nvol, nbricks, s);
+    if (e == cudaSuccess) {
+        if (vols[0].voxel_type == MCG_VOXEL_SHORT2) e = launch_generate_multi<MCG_VOXEL_SHORT2>(ctx, nvol, nbricks, s);
+        else e = launch_generate_multi<MCG_VOXEL_FLOAT2>(ctx, nvol, nbricks, s);
+    }
+    if (e == cudaSuccess) e = batch_counts_out(ctx, nvol, s);
+    if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
+    batch_state(ctx, vols, nvol, nbricks);
+    for (int v = 0; v < nvol; ++v) ctx->batch_caps[v] = outs[v].capacity_vertices;
+    return MCG_OK;
 }
 
 // ---- extraction without any allocation ------------------------------------------
