@@ -102,6 +102,14 @@ struct IdxSmem {
     uint64_t bars[ISTAGES];
     long long sbrick[ISTAGES];
     unsigned int scan[ITHREADS];
+    unsigned long long vmask[ITHREADS];  // vertex pass: owned crossed edges of each (row, axis) slot
+    // triangle pass: per cube row (64, (z, y) order) the occupied cubes (bit
+    // x), their triangle counts (4 bits per cube) and the row's first
+    // triangle in the brick; the cube index of every cube of the brick
+    unsigned int rowocc[BY * BZ];
+    unsigned int rownib[BY * BZ][4];
+    unsigned int rowoff[BY * BZ];
+    unsigned char cci[BRICK_CUBES];
     unsigned int wsum[IWARPS][4];
     alignas(16) signed char tri[256][16];
     unsigned char ntri[256];
@@ -550,12 +558,31 @@ __global__ void __launch_bounds__(ITHREADS) mc_idx_vertex_kernel(const __grid_co
             }
             unsigned int total;
             const unsigned int off = block_scan(S, (unsigned int)__popcll(m), &total);
-            unsigned long long vid = p.brick_uofs[b] + off;
-            const int ty = oy + 1, tz = oz + 1;
-            const int dy = axis == 1, dz = axis == 2, dx = axis == 0;
-            while (m) {
-                const int i = __ffsll((long long)m) - 1;
-                m &= m - 1;
+            // the brick's vertices spread evenly over the threads: vertex v
+            // belongs to the last (row, axis) slot whose offset is <= v (slots
+            // without vertices share their offset with the next slot)
+            S.vmask[tid] = m;
+            S.scan[tid] = off;
+            __syncthreads();
+            const unsigned long long vbase = p.brick_uofs[b];
+            for (unsigned int v = tid; v < total; v += ITHREADS) {
+                int k = 0;
+                {
+                    int hi = 3 * IOWN_ROWS - 1;
+                    while (k < hi) {
+                        const int mid = (k + hi + 1) >> 1;
+                        if (S.scan[mid] <= v) k = mid; else hi = mid - 1;
+                    }
+                }
+                const unsigned long long mk = S.vmask[k];
+                const unsigned int j = v - S.scan[k];  // the j-th owned edge of the slot
+                const unsigned int mlo = (unsigned int)mk, mhi = (unsigned int)(mk >> 32);
+                const unsigned int plo = (unsigned int)__popc(mlo);
+                const int i = j < plo ? (int)__fns(mlo, 0, (int)j + 1) : 32 + (int)__fns(mhi, 0, (int)(j - plo) + 1);
+                const int axis = k % 3, oy = (k / 3) % 9, oz = (k / 3) / 9;
+                const int ty = oy + 1, tz = oz + 1;
+                const int dy = axis == 1, dz = axis == 2, dx = axis == 0;
+                const unsigned long long vid = vbase + v;
                 const int x = bp.x0 - 4 + i, y = bp.y0 + oy, z = bp.z0 + oz;
                 const T lo = tile[(tz * IY + ty) * IX + i];
                 const T hi = tile[((tz + dz) * IY + ty + dy) * IX + i + dx];
@@ -592,7 +619,6 @@ __global__ void __launch_bounds__(ITHREADS) mc_idx_vertex_kernel(const __grid_co
                     }
                     if (p.out.vertex_edge) p.out.vertex_edge[vid] = key;
                 }
-                ++vid;
             }
         });
     if (!ok && tid == 0) atomicOr(&p.totals->flags, 1u);
@@ -621,52 +647,64 @@ __global__ void __launch_bounds__(ITHREADS)
         p.active, &p.totals->idx_ticket, [&](const T *tile, long long b, BrickPos bp) {
             if (p.brick_tris[b] == 0) return;  // uniform across the CTA
             idx_prepare<VT>(S, tile, bp, p.nx, p.ny, p.nz);
-            // four adjacent threads per cube row (64 rows = 256 threads); thread q of a row
-            // emits the row's cubes x with x % 4 == q, all four walk the row for offsets
-            const int row = tid >> 2, q = tid & 3;
-            const CubeRow r = idx_cube_row<VT>(S, row % BY, row / BY);
-            unsigned int cnt = 0;
-            {
-                unsigned int m = r.occ & (0x11111111u << q);
-                while (m) {
-                    const int x = __ffs(m) - 1;
-                    m &= m - 1;
-                    cnt += S.ntri[idx_cube_index(r, x)];
-                }
-            }
-            unsigned int rt = cnt;  // row total
-            rt += __shfl_xor_sync(0xffffffffu, rt, 1);
-            rt += __shfl_xor_sync(0xffffffffu, rt, 2);
-            unsigned int total;
-            const unsigned int rbase = block_scan(S, q == 0 ? rt : 0u, &total);
-            const unsigned int base = __shfl_sync(0xffffffffu, rbase, (tid & 31) & ~3);
-            if (r.occ) {
-                const int cy = row % BY, cz = row / BY;
-                const int gy = bp.y0 + cy, gz = bp.z0 + cz;
-                unsigned long long tid_out = p.brick_tofs[b] + base;
+            // one thread per cube row: occupancy, triangles per cube, row total
+            unsigned int rt = 0;
+            if (tid < BY * BZ) {
+                const int row = tid;
+                const CubeRow r = idx_cube_row<VT>(S, row % BY, row / BY);
+                unsigned int nib[4] = {0u, 0u, 0u, 0u};
                 unsigned int m = r.occ;
                 while (m) {
                     const int x = __ffs(m) - 1;
                     m &= m - 1;
                     const unsigned int ci = idx_cube_index(r, x);
-                    const int nt = S.ntri[ci];
-                    if ((x & 3) == q) {
-                        const int gx = bp.x0 + x;
-                        for (int j = 0; j < nt; ++j) {
-                            const unsigned long long tt = tid_out + j;
-                            if ((long long)tt >= capt) break;
-                            // the soup's slot k holds edge tri[3j + 2 - k] (:322-333)
-                            if (p.out.triangles) {
-                                const int e2 = S.tri[ci][3 * j + 2], e1 = S.tri[ci][3 * j + 1], e0 = S.tri[ci][3 * j];
-                                p.out.triangles[3 * tt] = p.edge_map[edge_key(p.nx, p.ny, gx, gy, gz, e2)];
-                                p.out.triangles[3 * tt + 1] = p.edge_map[edge_key(p.nx, p.ny, gx, gy, gz, e1)];
-                                p.out.triangles[3 * tt + 2] = p.edge_map[edge_key(p.nx, p.ny, gx, gy, gz, e0)];
-                            }
-                            if (p.out.tri_cube) p.out.tri_cube[tt] = lin3(p.nx, p.ny, gx, gy, gz);
-                        }
-                    }
-                    tid_out += nt;
+                    const unsigned int nt = S.ntri[ci];
+                    S.cci[row * BX + x] = (unsigned char)ci;
+                    nib[x >> 3] |= nt << ((x & 7) * 4);
+                    rt += nt;
                 }
+                S.rowocc[row] = r.occ;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) S.rownib[row][k] = nib[k];
+            }
+            unsigned int total;
+            const unsigned int rbase = block_scan(S, rt, &total);
+            if (tid < BY * BZ) S.rowoff[tid] = rbase;
+            __syncthreads();
+            // the brick's triangles spread evenly over the threads, in the
+            // soup's order: rows in (z, y) order, cubes in x order, table order
+            const unsigned long long tbase = p.brick_tofs[b];
+            for (unsigned int t = tid; t < total; t += ITHREADS) {
+                int row = 0;
+                {
+                    int hi = BY * BZ - 1;
+                    while (row < hi) {
+                        const int mid = (row + hi + 1) >> 1;
+                        if (S.rowoff[mid] <= t) row = mid; else hi = mid - 1;
+                    }
+                }
+                unsigned int j = t - S.rowoff[row];
+                unsigned int m = S.rowocc[row];
+                int x = 0;
+                for (;;) {
+                    x = __ffs(m) - 1;
+                    const unsigned int n = (S.rownib[row][x >> 3] >> ((x & 7) * 4)) & 15u;
+                    if (j < n) break;
+                    j -= n;
+                    m &= m - 1;
+                }
+                const unsigned long long tt = tbase + t;
+                if ((long long)tt >= capt) continue;
+                const unsigned int ci = S.cci[row * BX + x];
+                const int gx = bp.x0 + x, gy = bp.y0 + row % BY, gz = bp.z0 + row / BY;
+                // the soup's slot k holds edge tri[3j + 2 - k] (:322-333)
+                if (p.out.triangles) {
+                    const int e2 = S.tri[ci][3 * j + 2], e1 = S.tri[ci][3 * j + 1], e0 = S.tri[ci][3 * j];
+                    p.out.triangles[3 * tt] = p.edge_map[edge_key(p.nx, p.ny, gx, gy, gz, e2)];
+                    p.out.triangles[3 * tt + 1] = p.edge_map[edge_key(p.nx, p.ny, gx, gy, gz, e1)];
+                    p.out.triangles[3 * tt + 2] = p.edge_map[edge_key(p.nx, p.ny, gx, gy, gz, e0)];
+                }
+                if (p.out.tri_cube) p.out.tri_cube[tt] = lin3(p.nx, p.ny, gx, gy, gz);
             }
         });
     if (!ok && tid == 0) atomicOr(&p.totals->flags, 1u);
