@@ -347,6 +347,97 @@ def bench_graph(mcg, synthetic, torch, n=256, frames=20):
     return {"volume": [n, n, n], "frames": frames, "eager_ms_per_frame": eager_ms, "graph_ms_per_frame": graph_ms}
 
 
+def bench_batch_graph(mcg, synthetic, torch, nvol=64, frames=10, seed=11):
+    """A multi-volume fusion frame: depth maps of one 640x480 frame, its
+    integration into nvol volumes of uneven sizes (each axis log-uniform in
+    32..256 voxels, each volume spanning the scene's 3 m cube), and one
+    batched extraction of all of them into preallocated buffers; eager calls
+    against one captured CUDA graph replayed per frame (the reference runs
+    mc.run volume by volume, cu_kinect_fusion_v1.cu:3511-3737)."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    dims = [tuple(int(d) for d in np.round(np.exp(rng.uniform(np.log(32), np.log(256), size=3))))
+            for _ in range(nvol)]
+    scene = synthetic.FusionScene(seed=2, extent=EXTENT)
+    k = mcg.intrinsic(FX, FY, CX, CY)
+    depths, poses = [], []
+    for i in range(frames):
+        R, t = scene.pose(i, frames)
+        depths.append(synthetic.mm_to_u16_bits(scene.depth_frame(R, t, w=W, h=H, fx=FX, fy=FY, cx=CX, cy=CY,
+                                                                  seed=100 + i, device="cuda")))
+        poses.append(mcg.extrinsic_tensor(R, t))
+    ctx = mcg.Context()
+    vols = []
+    for (nx, ny, nz) in dims:
+        g = EXTENT / max(nx, ny, nz)
+        vols.append(mcg.voxel_new((nx, ny, nz), 4 * g, 4 * g, g, ctx=ctx))
+    cells = [v.grid_s for v in vols]
+    saved = [v.data.clone() for v in vols]
+    d_in = torch.empty_like(depths[0])
+    meter = torch.empty((H, W), dtype=torch.float32, device="cuda")
+    pose_dev = torch.empty(12, dtype=torch.float32, device="cuda")
+    st = torch.cuda.Stream()
+    # capacities: 1.5x the counts after integrating every frame once
+    with torch.cuda.stream(st):
+        mcg.depth_to_maps(depths[0], k, vertex=False, normal=False, ctx=ctx, stream=st, out_meter=meter)
+        for i in range(frames):
+            d_in.copy_(depths[i])
+            pose_dev.copy_(poses[i])
+            mcg.depth_to_maps(d_in, k, vertex=False, normal=False, ctx=ctx, stream=st, out_meter=meter)
+            for v in vols:
+                mcg.volumetric_integration_device_pose(v, k, pose_dev, meter, ctx=ctx, stream=st)
+        meshes = mcg.extract_batched([v.data for v in vols], cells, ctx=ctx, stream=st)
+    torch.cuda.synchronize()
+    caps = [int(m.counts["vertices"] * 1.5) + 3000 for m in meshes]
+    del meshes
+    outs = [{"soup": torch.empty((c, 28), dtype=torch.uint8, device="cuda"),
+             "normals": torch.empty((c, 3), dtype=torch.float32, device="cuda")} for c in caps]
+
+    def frame():
+        mcg.depth_to_maps(d_in, k, vertex=False, normal=False, ctx=ctx, stream=st, out_meter=meter)
+        for v in vols:
+            mcg.volumetric_integration_device_pose(v, k, pose_dev, meter, ctx=ctx, stream=st)
+        mcg.extract_batched_into([v.data for v in vols], cells, outs, caps, ctx=ctx, stream=st)
+
+    def restore():
+        for v, s0 in zip(vols, saved):
+            v.data.copy_(s0)
+
+    def timed(step):
+        restore()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(st):
+            e0.record(st)
+            for i in range(frames):
+                d_in.copy_(depths[i])
+                pose_dev.copy_(poses[i])
+                step()
+            e1.record(st)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / frames
+
+    with torch.cuda.stream(st):
+        frame()  # warm-up outside the capture: every buffer and spare sized
+    torch.cuda.synchronize()
+    eager_ms = timed(frame)
+    counts_eager = [c["vertices"] for c in mcg.counts_batched(ctx, nvol)]
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=st):
+        frame()
+    torch.cuda.synchronize()
+    graph_ms = timed(g.replay)
+    cnt = mcg.counts_batched(ctx, nvol)
+    assert [c["vertices"] for c in cnt] == counts_eager
+    assert all(c["status"] == 0 for c in cnt)
+    voxels = sum(nx * ny * nz for (nx, ny, nz) in dims)
+    return {"volumes": nvol, "voxels": voxels, "frame": [W, H], "frames": frames,
+            "triangles_last_frame": int(sum(counts_eager) // 3),
+            "launches_per_frame": 1 + 3 * nvol + 6,
+            "eager_ms_per_frame": eager_ms, "graph_ms_per_frame": graph_ms,
+            "speedup": eager_ms / graph_ms}
+
+
 
 def bench_raycast(mcg, synthetic, torch, v, reps=20):
     """Ray casting the headline volume into 640x480 depth + normal maps from
@@ -790,6 +881,8 @@ def summarize(line):
         "full_outputs_ms": get("full_outputs", "ms_per_step"),
         "batched_speedup": get("batched", "speedup"), "batched_ms": get("batched", "batched_ms"),
         "loop_ms": get("batched", "loop_ms"),
+        "batch_frame_graph_ms": get("graph", "batch", "graph_ms_per_frame"),
+        "batch_frame_eager_ms": get("graph", "batch", "eager_ms_per_frame"),
         "adjoint_over_forward": get("adjoint", "path_adjoint_over_forward"),
         "integrate_ms_per_frame": get("integrate", "integrate_ms_per_frame"),
         "indexed_ms": get("indexed", "ms"), "stress_gvoxels_per_s": get("stress", "extract_gvoxels_per_s"),
@@ -1063,6 +1156,10 @@ def main():
             graph = bench_graph(mcg, synthetic, torch)
         except Exception as ex:  # pragma: no cover
             graph = {"error": str(ex)}
+        try:
+            graph["batch"] = bench_batch_graph(mcg, synthetic, torch)
+        except Exception as ex:  # pragma: no cover
+            graph["batch"] = {"error": str(ex)}
 
     raycast = None
     if not args.no_raycast:
