@@ -20,9 +20,11 @@
 #include <stdint.h>
 #include <string.h>
 
+#include <type_traits>
 #include <vector>
 
 #include "mcg_internal.h"
+#include "tma.cuh"
 
 namespace mcg {
 namespace {
@@ -45,6 +47,7 @@ __device__ __forceinline__ unsigned record_kind(uint32_t v, bool lossless) {
     return 3u;
 }
 
+// write pass: the chunk's record starts
 struct RleSmem {
     uint32_t pos[RCHUNK];   // record starts of the chunk (slice index)
     uint32_t vox[RCHUNK];   // their first voxels
@@ -53,8 +56,20 @@ struct RleSmem {
     int wr[RT / 32];
 };
 
+// count pass: two chunk buffers, the next chunk's asynchronous copies in
+// flight while the current one is scanned
+struct RleCountSmem {
+    alignas(16) uint32_t stage[2][RCHUNK];
+    uint32_t wn[RT / 32], wb[RT / 32];
+    int wr[RT / 32];
+};
+
+template <bool WRITE>
+using RleS = typename std::conditional<WRITE, RleSmem, RleCountSmem>::type;
+
 // block-wide exclusive sums of two values; totals returned through refs
-__device__ __forceinline__ void scan2(RleSmem &S, uint32_t a, uint32_t b, uint32_t &ea, uint32_t &eb, uint32_t &ta,
+template <class SM>
+__device__ __forceinline__ void scan2(SM &S, uint32_t a, uint32_t b, uint32_t &ea, uint32_t &eb, uint32_t &ta,
                                       uint32_t &tb) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint32_t x = a, y = b;
@@ -89,7 +104,8 @@ __device__ __forceinline__ void scan2(RleSmem &S, uint32_t a, uint32_t b, uint32
 }
 
 // block-wide inclusive max-scan of a signed value (run starts, -1 = none)
-__device__ __forceinline__ int scan_max(RleSmem &S, int v, int carry) {
+template <class SM>
+__device__ __forceinline__ int scan_max(SM &S, int v, int carry) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     int x = v;
 #pragma unroll
@@ -122,15 +138,38 @@ __device__ __forceinline__ void emit(uint8_t *img, unsigned long long off, uint3
     }
 }
 
+// count pass: chunk starting at c0 into buffer buf by asynchronous copies
+// (16 bytes at a time when vec: the slice is 16-byte aligned), zero past
+// the slice; one commit group per call
+__device__ __forceinline__ void rle_issue_chunk(RleCountSmem &S, const uint32_t *__restrict__ sl, int xy, int c0,
+                                                int buf, bool vec) {
+    const int i0 = c0 + threadIdx.x * RV;
+    uint32_t *dst = S.stage[buf] + threadIdx.x * RV;
+    if (vec && i0 + RV <= xy) {
+#pragma unroll
+        for (int q = 0; q < RV / 4; ++q) cp_async_16(dst + 4 * q, sl + i0 + 4 * q);
+    } else {
+#pragma unroll
+        for (int j = 0; j < RV; ++j) {
+            const bool in = i0 + j < xy;
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(smem_u32(dst + j)),
+                         "l"(in ? sl + i0 + j : sl), "r"(in ? 4u : 0u)
+                         : "memory");
+        }
+    }
+    cp_async_commit();
+}
+
 // WRITE = false: slice_bytes[z] = record bytes of slice z.  WRITE = true:
 // slice z goes to img + slice_off[z]: its byte count (uint32) then records.
+// vec: the slices are 16-byte aligned (count pass only).
 template <bool WRITE>
 __global__ void __launch_bounds__(RT) rle_encode_kernel(const uint32_t *__restrict__ vol, int xy, int lossless_i,
                                                         unsigned long long *__restrict__ slice_bytes,
                                                         const unsigned long long *__restrict__ slice_off,
-                                                        uint8_t *__restrict__ img) {
+                                                        uint8_t *__restrict__ img, int vec) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    RleSmem &S = *reinterpret_cast<RleSmem *>(smem_raw);
+    RleS<WRITE> &S = *reinterpret_cast<RleS<WRITE> *>(smem_raw);
     const bool lossless = lossless_i != 0;
     const int z = blockIdx.x;
     const uint32_t *sl = vol + (long long)z * xy;
@@ -144,16 +183,38 @@ __global__ void __launch_bounds__(RT) rle_encode_kernel(const uint32_t *__restri
     unsigned long long pend_off = 0;
     // slice indices fit 32 bits: the host rejects slices whose image could
     // pass the format's 32-bit byte count
-    for (int c0 = 0; c0 < xy; c0 += RCHUNK) {
+    if constexpr (!WRITE) rle_issue_chunk(S, sl, xy, 0, 0, vec != 0);
+    int buf = 0;
+    for (int c0 = 0; c0 < xy; c0 += RCHUNK, buf ^= 1) {
         const int i0 = c0 + tid * RV;
         uint32_t v[RV];
+        uint32_t left;
+        if constexpr (WRITE) {
 #pragma unroll
-        for (int j = 0; j < RV; ++j) v[j] = i0 + j < xy ? __ldg(sl + i0 + j) : 0u;
-        // previous voxel of each thread's first voxel
-        uint32_t left = __shfl_up_sync(0xffffffffu, v[RV - 1], 1);
-        if ((tid & 31) == 0) {
-            if (tid == 0) left = prev;
-            else left = i0 - 1 < xy ? __ldg(sl + i0 - 1) : 0u;
+            for (int j = 0; j < RV; ++j) v[j] = i0 + j < xy ? __ldg(sl + i0 + j) : 0u;
+            // previous voxel of each thread's first voxel
+            left = __shfl_up_sync(0xffffffffu, v[RV - 1], 1);
+            if ((tid & 31) == 0) {
+                if (tid == 0) left = prev;
+                else left = i0 - 1 < xy ? __ldg(sl + i0 - 1) : 0u;
+            }
+        } else {
+            // the next chunk's copies go out first (its buffer was last read
+            // before the barriers of the previous chunk), then this chunk's land
+            if (c0 + RCHUNK < xy) rle_issue_chunk(S, sl, xy, c0 + RCHUNK, buf ^ 1, vec != 0);
+            else cp_async_commit();
+            cp_async_wait_group<1>();
+            __syncthreads();
+            const uint4 *src = reinterpret_cast<const uint4 *>(S.stage[buf] + tid * RV);
+#pragma unroll
+            for (int q = 0; q < RV / 4; ++q) {
+                const uint4 w = src[q];
+                v[4 * q] = w.x;
+                v[4 * q + 1] = w.y;
+                v[4 * q + 2] = w.z;
+                v[4 * q + 3] = w.w;
+            }
+            left = tid == 0 ? prev : S.stage[buf][tid * RV - 1];
         }
         // run starts (local inclusive max), then the block max-scan
         int rs_loc = -1;
@@ -194,7 +255,7 @@ __global__ void __launch_bounds__(RT) rle_encode_kernel(const uint32_t *__restri
         }
         uint32_t er, eb, tr, tb;
         scan2(S, nrec, nb, er, eb, tr, tb);
-        if (WRITE) {
+        if constexpr (WRITE) {
             uint32_t k = er, b = eb;
 #pragma unroll
             for (int j = 0; j < RV; ++j) {
@@ -216,6 +277,7 @@ __global__ void __launch_bounds__(RT) rle_encode_kernel(const uint32_t *__restri
             }
             __syncthreads();  // pos / vox / boff are rewritten by the next chunk
         }
+        (void)buf;
         bytes += tb;
         // carries: the run start in force and the voxel at the chunk's end
         if (tid == RT - 1) {
@@ -264,11 +326,12 @@ extern "C" mcg_status mcg_rle_encode(mcg_context *ctx, const void *vol, int32_t 
     if (!ensure(&ctx->rle_slices, &ctx->rle_slices_cap, (size_t)2 * nz))
         return mcg_cuda_fail(ctx, cudaErrorMemoryAllocation);
     unsigned long long *d_bytes = ctx->rle_slices, *d_off = ctx->rle_slices + nz;
-    const size_t smem = sizeof(RleSmem);
-    cudaFuncSetAttribute(rle_encode_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const size_t smem = sizeof(RleSmem), csmem = sizeof(RleCountSmem);
+    cudaFuncSetAttribute(rle_encode_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csmem);
     cudaFuncSetAttribute(rle_encode_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    rle_encode_kernel<false><<<nz, RT, smem, s>>>(static_cast<const uint32_t *>(vol), (int)xy, lossless ? 1 : 0, d_bytes,
-                                                  nullptr, nullptr);
+    const int vec = ((reinterpret_cast<uintptr_t>(vol) & 15u) == 0 && xy % 4 == 0) ? 1 : 0;
+    rle_encode_kernel<false><<<nz, RT, csmem, s>>>(static_cast<const uint32_t *>(vol), (int)xy, lossless ? 1 : 0,
+                                                   d_bytes, nullptr, nullptr, vec);
     e = cudaGetLastError();
     if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
     std::vector<unsigned long long> bytes(nz), off(nz);
@@ -288,7 +351,7 @@ extern "C" mcg_status mcg_rle_encode(mcg_context *ctx, const void *vol, int32_t 
     e = cudaMemcpyAsync(d_off, off.data(), sizeof(unsigned long long) * nz, cudaMemcpyHostToDevice, s);
     if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
     rle_encode_kernel<true><<<nz, RT, smem, s>>>(static_cast<const uint32_t *>(vol), (int)xy, lossless ? 1 : 0, nullptr,
-                                                 d_off, ctx->rle_image);
+                                                 d_off, ctx->rle_image, 0);
     e = cudaGetLastError();
     if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
     // header (:1303-1310), then the slices
