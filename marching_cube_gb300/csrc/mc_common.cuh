@@ -10,6 +10,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#define MCG_TABLES_DEVICE  // the tables also as device data initialised with the module
 #include "mc_tables.h"
 #include "mcg_internal.h"
 #include "tma.cuh"
@@ -49,13 +50,15 @@ __device__ __forceinline__ int c_cz(int c) { return c >> 2; }
 // (vertex_interp argument order, :304-315)
 __device__ __forceinline__ int c_ea(int e) { return e < 8 ? e : e - 8; }
 __device__ __forceinline__ int c_eb(int e) { return e < 8 ? (e & 4) | ((e + 1) & 3) : e - 4; }
-// The triangle table and the vertex count of each cube case, in global
-// memory.  Kernels copy them into shared memory at start: the triangle table
-// with one 16-byte load per thread (from constant memory the lanes of a load
-// that read different words are served one after another, which made that
-// copy take most of a short kernel's time).
-__device__ __align__(16) signed char g_tri[256][16];
-__device__ unsigned char g_nverts[256];
+// The triangle table and the vertex count of each cube case are global
+// memory initialised with the module (mcg_tri_table_dev, mcg_num_verts_dev
+// in mc_tables.h), so nothing is uploaded and a device reset reloads them.
+// Kernels copy them into shared memory at start: the triangle table with one
+// 16-byte load per thread (from constant memory the lanes of a load that
+// read different words are served one after another, which made that copy
+// take most of a short kernel's time).
+#define g_tri mcg_tri_table_dev
+#define g_nverts mcg_num_verts_dev
 
 // dst[256][16] (16-byte aligned shared memory) <- g_tri, by threads tid of nt
 __device__ __forceinline__ void load_tri_table(signed char (*dst)[16], int tid, int nt) {
@@ -272,16 +275,6 @@ struct CubeRow {
 };
 
 // ---- host helpers -------------------------------------------------------------
-bool g_tables_ready[64] = {false};
-
-cudaError_t upload_tables(int device) {
-    if (device >= 0 && device < 64 && g_tables_ready[device]) return cudaSuccess;
-    cudaError_t e = cudaMemcpyToSymbol(g_tri, mcg_tri_table, sizeof(mcg_tri_table));
-    if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_nverts, mcg_num_verts, sizeof(mcg_num_verts));
-    if (e == cudaSuccess && device >= 0 && device < 64) g_tables_ready[device] = true;
-    return e;
-}
-
 struct Geometry {
     int nbx, nby, nbz;
     long long nbricks;

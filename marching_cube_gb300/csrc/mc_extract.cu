@@ -2442,7 +2442,6 @@ static mcg_status classify_impl(mcg_context *ctx, const mcg_volume *vol, int32_t
                                 mcg_stream_t stream) {
     cudaStream_t s = (cudaStream_t)stream;
     cudaError_t e = cudaSetDevice(ctx->device);
-    if (e == cudaSuccess) e = upload_tables(ctx->device);
     if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
     const Geometry g = geometry_slab(vol->nx, vol->ny, z0, z1);
     if (!ensure(&ctx->brick_tris, &ctx->brick_tris_cap, (size_t)g.nbricks) ||
@@ -2572,8 +2571,7 @@ mcg_status mcg_mc_extract(mcg_context *ctx, const mcg_volume *vol, const mcg_mes
     if ((fused == 1 && fused_applies<4>(vol, &map)) || (fused == 2 && fused_applies<2>(vol, &map))) {
         cudaStream_t s = (cudaStream_t)stream;
         cudaError_t e = cudaSetDevice(ctx->device);
-        if (e == cudaSuccess) e = upload_tables(ctx->device);
-        if (e == cudaSuccess && ctx->time_kernels && !ctx->tk0) {
+            if (e == cudaSuccess && ctx->time_kernels && !ctx->tk0) {
             e = cudaEventCreate(&ctx->tk0);
             if (e == cudaSuccess) e = cudaEventCreate(&ctx->tk1);
         }
@@ -2968,7 +2966,6 @@ mcg_status mcg_mc_classify_batched(mcg_context *ctx, const mcg_volume *vols, int
     if (!ctx || !batch_ok(vols, nvol)) return MCG_ERR_INVALID_ARG;
     cudaStream_t s = (cudaStream_t)stream;
     cudaError_t e = cudaSetDevice(ctx->device);
-    if (e == cudaSuccess) e = upload_tables(ctx->device);
     if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
     const long long nbricks = batch_bricks(vols, nvol);
     if (nbricks < 0) return MCG_ERR_INVALID_ARG;
@@ -3052,7 +3049,6 @@ mcg_status mcg_mc_extract_batched(mcg_context *ctx, const mcg_volume *vols, cons
         if (outs[v].capacity_vertices < 0) return MCG_ERR_INVALID_ARG;
     cudaStream_t s = (cudaStream_t)stream;
     cudaError_t e = cudaSetDevice(ctx->device);
-    if (e == cudaSuccess) e = upload_tables(ctx->device);
     if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
     const long long nbricks = batch_bricks(vols, nvol);
     if (nbricks < 0) return MCG_ERR_INVALID_ARG;
@@ -3124,8 +3120,6 @@ extern "C" mcg_status mcg_mc_extract_noalloc(const mcg_volume *vol, const mcg_me
     void *addr = nullptr;
     e = cudaGetSymbolAddress(&addr, g_noalloc_scratch);
     if (e != cudaSuccess || !addr) { cudaGetLastError(); return MCG_ERR_CUDA; }
-    e = upload_tables(dev);
-    if (e != cudaSuccess) { cudaGetLastError(); return MCG_ERR_CUDA; }
     unsigned char *base = static_cast<unsigned char *>(addr);
     Scratch sc;
     sc.tris = reinterpret_cast<uint32_t *>(base + kNoAllocTrisOff);

@@ -781,7 +781,6 @@ mcg_status mcg_mc_classify_indexed(mcg_context *ctx, const mcg_volume *vol, mcg_
     if (!ctx || !vol_ok(vol)) return MCG_ERR_INVALID_ARG;
     cudaStream_t s = (cudaStream_t)stream;
     cudaError_t e = cudaSetDevice(ctx->device);
-    if (e == cudaSuccess) e = upload_tables(ctx->device);
     if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
     const Geometry g = geometry(vol->nx, vol->ny, vol->nz);
     const long long nch = idx_chunks(g.nbricks);

@@ -127,6 +127,19 @@ def render(edge, tri, nv, prefix):
     for i in range(0, 256, 16):
         out.append("  " + ",".join("%d" % v for v in nv[i:i + 16]) + ",")
     out.append("};")
+    if prefix == "mcg_":
+        # the same lists as device data initialised with the module image (no
+        # upload, nothing to redo after a device reset)
+        out.append("#if defined(__CUDACC__) && defined(MCG_TABLES_DEVICE)")
+        out.append("static __device__ __align__(16) signed char %stri_table_dev[256][16] = {" % prefix)
+        for row in tri:
+            out.append("  {" + ",".join("%d" % v for v in row) + "},")
+        out.append("};")
+        out.append("static __device__ unsigned char %snum_verts_dev[256] = {" % prefix)
+        for i in range(0, 256, 16):
+            out.append("  " + ",".join("%d" % v for v in nv[i:i + 16]) + ",")
+        out.append("};")
+        out.append("#endif")
     out.append("#endif")
     return "\n".join(out) + "\n"
 
