@@ -205,7 +205,14 @@ mcg_status mcg_mc_extract_slab(mcg_context *ctx, const mcg_volume *vol, int32_t 
 /* Batched extraction: nvol volumes of any sizes (same voxel type) in one
  * launch per pass (replaces a loop of MarchingCubes::run calls).  Outputs
  * of volume v go to outs[v], in the same order and bit-identical to a
- * single-volume extraction of that volume.  counts: nvol entries. */
+ * single-volume extraction of that volume.  counts: nvol entries.
+ * mcg_mc_extract_batched chains the count, scan and generate launches on
+ * the device (preallocated outputs, no host round trip); classify, counts,
+ * generate size the outputs from the counts first.  Inside a stream capture
+ * the calls allocate and wait for nothing: make the same call once outside
+ * the capture first (MCG_ERR_STATE otherwise); the graph keeps its own copy
+ * of the volume table, so later calls on the context may use other
+ * batches no larger than the captured one. */
 mcg_status mcg_mc_classify_batched(mcg_context *ctx, const mcg_volume *vols, int32_t nvol, mcg_stream_t stream);
 mcg_status mcg_mc_counts_batched(mcg_context *ctx, mcg_mesh_counts *counts, int32_t nvol);
 mcg_status mcg_mc_generate_batched(mcg_context *ctx, const mcg_volume *vols, const mcg_mesh_out *outs,
