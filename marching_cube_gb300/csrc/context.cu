@@ -82,6 +82,7 @@ mcg_status mcg_destroy(mcg_context *ctx) {
     cudaFree(ctx->brick_uofs);
     cudaFree(ctx->edge_map);
     cudaFree(ctx->fx_item);
+    cudaFree(ctx->idx_cand);
     cudaFree(ctx->fx_group);
     cudaFree(ctx->d_totals);
     if (ctx->h_totals) cudaFreeHost(ctx->h_totals);

@@ -2485,6 +2485,27 @@ static mcg_status classify_impl(mcg_context *ctx, const mcg_volume *vol, int32_t
     return MCG_OK;
 }
 
+namespace mcg {
+cudaError_t soup_count_phase(mcg_context *ctx, const mcg_volume *vol, cudaStream_t s) {
+    const Geometry g = geometry(vol->nx, vol->ny, vol->nz);
+    if (!ensure(&ctx->brick_tris, &ctx->brick_tris_cap, (size_t)g.nbricks) ||
+        !ensure(&ctx->brick_occ, &ctx->brick_occ_cap, (size_t)(CHUNK_FIELDS * num_chunks(g.nbricks))) ||
+        !ensure(&ctx->brick_vofs, &ctx->brick_vofs_cap, (size_t)g.nbricks) ||
+        !ensure(&ctx->active, &ctx->active_cap, (size_t)g.nbricks) ||
+        !ensure(&ctx->list_vofs, &ctx->list_vofs_cap, (size_t)g.nbricks))
+        return cudaErrorMemoryAllocation;
+    if (ctx->chunk_clean_cap != ctx->brick_occ_cap) {
+        const cudaError_t e = cudaMemsetAsync(ctx->brick_occ, 0, sizeof(uint32_t) * ctx->brick_occ_cap, s);
+        if (e != cudaSuccess) return e;
+        ctx->chunk_clean_cap = ctx->brick_occ_cap;
+    }
+    Scratch sc = ctx_scratch(ctx);
+    sc.host = nullptr;  // the scan then leaves the flags and counters in d_totals
+    ctx->counters_clean = false;
+    return launch_count_phase(vol, g, sc, ctx->num_sms, s, ctx->mc_cfg, true);
+}
+}  // namespace mcg
+
 mcg_status mcg_set_kernel_timing(mcg_context *ctx, int32_t enable) {
     if (!ctx) return MCG_ERR_INVALID_ARG;
     ctx->time_kernels = enable != 0;

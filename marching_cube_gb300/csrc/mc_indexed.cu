@@ -365,6 +365,7 @@ struct IdxParams {
     const unsigned long long *brick_uofs;  // vertex offsets
     MeshTotals *totals;
     uint32_t *edge_map;
+    uint32_t *cand;  // count pass: the bricks whose owned edges are counted (totals->idx_cand of them)
     mcg_indexed_out out;
 };
 
@@ -375,25 +376,60 @@ __device__ __forceinline__ void load_tables(IdxSmem<VT> &S) {
 }
 
 // ---- pass 1: counts --------------------------------------------------------------
-template <int VT, bool TMA>
+// The bricks whose owned edges can be vertices: a vertex needs a valid
+// occupied cube around its edge, and the cubes around the edges a brick owns
+// lie in the brick or in its neighbours at -x, -y, -z, -x-y, -x-z, -y-z; an
+// occupied valid cube emits triangles, so a brick is listed when one of
+// those seven bricks has triangles (counts of the soup's count pass).  The
+// others own no vertex.  One thread per brick, one atomic per warp.
+__global__ void __launch_bounds__(256) mc_idx_cand_kernel(IdxParams p) {
+    const long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    bool cand = false;
+    if (b < p.nbricks) {
+        const long long r = b / p.nbx;
+        const int bx = (int)(b - r * p.nbx), by = (int)(r % p.nby), bz = (int)(r / p.nby);
+        const long long sy = p.nbx, sz = (long long)p.nbx * p.nby;
+#pragma unroll
+        for (int k = 0; k < 7; ++k) {  // (dx, dy, dz) in {0,1}^3 but (1,1,1)
+            const int dx = k & 1, dy = (k >> 1) & 1, dz = k >> 2;
+            if (bx >= dx && by >= dy && bz >= dz && p.brick_tris[b - dx - dy * sy - dz * sz] != 0u) cand = true;
+        }
+        if (!cand) p.brick_uniq[b] = 0u;
+    }
+    const unsigned int m = __ballot_sync(0xffffffffu, cand);
+    if (m) {
+        const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+        unsigned int base = 0;
+        if (lane == leader) base = atomicAdd(&p.totals->idx_cand, (unsigned int)__popc(m));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (cand) p.cand[base + __popc(m & ((1u << lane) - 1u))] = (uint32_t)b;
+    }
+}
+
+// Per brick: triangles, active flag, occupied cubes, owned vertices, into the
+// brick arrays and the chunk sums.  OWNED: the listed bricks only, owned
+// vertices only -- the triangles come from the soup's count pass (occupied
+// cubes then come from its totals).
+template <int VT, bool TMA, bool OWNED>
 __global__ void __launch_bounds__(ITHREADS) mc_idx_count_kernel(const __grid_constant__ CUtensorMap map, IdxParams p) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     IdxSmem<VT> &S = *reinterpret_cast<IdxSmem<VT> *>(smem_raw);
     load_tables(S);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const long long nitems = OWNED ? (long long)p.totals->idx_cand : p.nbricks;
     const bool ok = for_each_brick<VT, TMA>(
-        S, &map, static_cast<const typename Vox<VT>::T *>(p.vol), p.nx, p.ny, p.nz, p.nbx, p.nby, p.nbricks, nullptr,
-        &p.totals->cls_ticket, [&](const typename Vox<VT>::T *tile, long long b, BrickPos bp) {
+        S, &map, static_cast<const typename Vox<VT>::T *>(p.vol), p.nx, p.ny, p.nz, p.nbx, p.nby, nitems,
+        OWNED ? p.cand : nullptr, &p.totals->cls_ticket, [&](const typename Vox<VT>::T *tile, long long b, BrickPos bp) {
             if (!idx_tile_mixed<VT>(S, tile)) {
                 if (tid == 0) {
-                    p.brick_tris[b] = 0;
+                    if (!OWNED) p.brick_tris[b] = 0;
                     p.brick_uniq[b] = 0;
                 }
                 return;  // uniform across the CTA
             }
             idx_prepare<VT>(S, tile, bp, p.nx, p.ny, p.nz);
             unsigned int t = 0, o = 0, u = 0;
-            if (tid < BY * BZ) {
+            if (!OWNED && tid < BY * BZ) {
                 const CubeRow r = idx_cube_row<VT>(S, tid % BY, tid / BY);
                 o = __popc(r.occ);
                 unsigned int m = r.occ;
@@ -427,7 +463,8 @@ __global__ void __launch_bounds__(ITHREADS) mc_idx_count_kernel(const __grid_con
                     O += S.wsum[w][1];
                     U += S.wsum[w][2];
                 }
-                p.brick_tris[b] = T;
+                if (OWNED) T = p.brick_tris[b];
+                else p.brick_tris[b] = T;
                 p.brick_uniq[b] = U;
                 if (T || U) {
                     uint32_t *c = p.chunk + (b / CHUNK) * 4;
@@ -448,7 +485,7 @@ __global__ void __launch_bounds__(CHUNK)
     mc_idx_scan_kernel(const uint32_t *__restrict__ brick_tris, const uint32_t *__restrict__ brick_uniq,
                        const uint32_t *__restrict__ chunk, long long nb, unsigned long long *__restrict__ brick_tofs,
                        unsigned long long *__restrict__ brick_uofs, uint32_t *__restrict__ active,
-                       MeshTotals *__restrict__ totals) {
+                       MeshTotals *__restrict__ totals, int keep_occupied) {
     __shared__ unsigned long long s_part[7][CHUNK / 32];
     __shared__ unsigned long long s_base[3];
     __shared__ unsigned int s_w[3][CHUNK / 32];
@@ -488,7 +525,7 @@ __global__ void __launch_bounds__(CHUNK)
         if (j == 0) {
             totals->triangles = r[3];
             totals->active_bricks = (unsigned int)r[4];
-            totals->occupied = r[5];
+            if (!keep_occupied) totals->occupied = r[5];
             totals->vertices = r[6];
         }
     }
@@ -717,7 +754,7 @@ void launch_idx(int pass, const CUtensorMap &map, const IdxParams &p, int sms, l
     static int occ[3] = {0, 0, 0};
     long long grid;
     if (pass == 0) {
-        if (!occ[0]) occ[0] = occupancy(mc_idx_count_kernel<VT, TMA>, ITHREADS, smem);
+        if (!occ[0]) occ[0] = occupancy(mc_idx_count_kernel<VT, TMA, true>, ITHREADS, smem);
         grid = (long long)sms * occ[0];
     } else if (pass == 1) {
         if (!occ[1]) occ[1] = occupancy(mc_idx_vertex_kernel<VT, TMA>, ITHREADS, smem);
@@ -728,7 +765,7 @@ void launch_idx(int pass, const CUtensorMap &map, const IdxParams &p, int sms, l
     }
     if (grid > items) grid = items;
     if (grid < 1) grid = 1;
-    if (pass == 0) mc_idx_count_kernel<VT, TMA><<<(int)grid, ITHREADS, smem, s>>>(map, p);
+    if (pass == 0) mc_idx_count_kernel<VT, TMA, true><<<(int)grid, ITHREADS, smem, s>>>(map, p);
     else if (pass == 1) mc_idx_vertex_kernel<VT, TMA><<<(int)grid, ITHREADS, smem, s>>>(map, p);
     else mc_idx_triangle_kernel<VT, TMA><<<(int)grid, ITHREADS, smem, s>>>(map, p);
 }
@@ -784,24 +821,27 @@ mcg_status mcg_mc_classify_indexed(mcg_context *ctx, const mcg_volume *vol, mcg_
     if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
     const Geometry g = geometry(vol->nx, vol->ny, vol->nz);
     const long long nch = idx_chunks(g.nbricks);
-    if (!ensure(&ctx->brick_tris, &ctx->brick_tris_cap, (size_t)g.nbricks) ||
-        !ensure(&ctx->brick_uniq, &ctx->brick_uniq_cap, (size_t)g.nbricks) ||
-        !ensure(&ctx->brick_occ, &ctx->brick_occ_cap, (size_t)(4 * nch)) ||
-        !ensure(&ctx->brick_vofs, &ctx->brick_vofs_cap, (size_t)g.nbricks) ||
+    if (!ensure(&ctx->brick_uniq, &ctx->brick_uniq_cap, (size_t)g.nbricks) ||
         !ensure(&ctx->brick_uofs, &ctx->brick_uofs_cap, (size_t)g.nbricks) ||
-        !ensure(&ctx->active, &ctx->active_cap, (size_t)g.nbricks))
+        !ensure(&ctx->idx_cand, &ctx->idx_cand_cap, (size_t)g.nbricks))
         return mcg_cuda_fail(ctx, cudaErrorMemoryAllocation);
-    // flags and the three work counters
-    e = cudaMemsetAsync(&ctx->d_totals->flags, 0, 4 * sizeof(unsigned int), s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(ctx->brick_occ, 0, sizeof(uint32_t) * 4 * nch, s);
+    // the soup's count phase: brick triangle counts, occupied cubes; its scan
+    // leaves the chunk sums zero for the sums below
+    e = soup_count_phase(ctx, vol, s);
+    if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
+    // the counters the count phase used, and the candidate count
+    e = cudaMemsetAsync(&ctx->d_totals->cls_ticket, 0, 3 * sizeof(unsigned int), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(&ctx->d_totals->idx_cand, 0, sizeof(unsigned int), s);
     ctx->chunk_clean_cap = 0;  // these sums stay behind: the next count phase clears the array first
     ctx->counters_clean = false;
     if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
-    const IdxParams p = idx_params(ctx, vol, g);
+    IdxParams p = idx_params(ctx, vol, g);
+    p.cand = ctx->idx_cand;
+    mc_idx_cand_kernel<<<(unsigned int)((g.nbricks + 255) / 256), 256, 0, s>>>(p);
     launch_idx_pass(0, vol, p, ctx->num_sms, g.nbricks, s);
     mc_idx_scan_kernel<<<(unsigned int)nch, CHUNK, 0, s>>>(ctx->brick_tris, ctx->brick_uniq, ctx->brick_occ,
                                                           g.nbricks, ctx->brick_vofs, ctx->brick_uofs, ctx->active,
-                                                          ctx->d_totals);
+                                                          ctx->d_totals, 1);
     e = cudaGetLastError();
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(ctx->h_totals, ctx->d_totals, sizeof(MeshTotals), cudaMemcpyDeviceToHost, s);

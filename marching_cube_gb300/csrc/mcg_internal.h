@@ -26,6 +26,7 @@ struct MeshTotals {
     unsigned int idx_ticket;
     unsigned int scan_done;   // finished CTAs of the scan / generate launch (the last one resets it)
     unsigned int gen_exit;
+    unsigned int idx_cand;    // indexed count phase: bricks listed for the owned-edge count
 };
 static_assert(sizeof(MeshTotals) <= 256, "MeshTotals fits the totals region of the fixed scratch");
 
@@ -103,6 +104,8 @@ struct mcg_context {
     bool cls_fused = false;          // the last count phase was a fused extraction (counts only, no brick list)
     mcg_mc_config mc_cfg = {0, 4, 3, 0};  // launch configuration (mcg_mc_set_config)
     int64_t last_capacity_tris = -1;  // indexed: triangle capacity of the last generate
+    uint32_t *idx_cand = nullptr;     // indexed: bricks whose owned edges are counted
+    size_t idx_cand_cap = 0;
 
     // batched extraction: device tables (volume descriptors, classify and
     // generate tensor maps), pinned staging for them, per-volume sums
@@ -218,6 +221,13 @@ struct mcg_context {
 
 // records a CUDA failure on ctx and returns the matching status
 mcg_status mcg_cuda_fail(mcg_context *ctx, cudaError_t e);
+
+namespace mcg {
+// The soup extraction's count phase (count launch + scan) over the whole
+// volume, its totals left in ctx->d_totals (no mapped host copy), for the
+// indexed extraction, which takes the brick triangle counts from it.
+cudaError_t soup_count_phase(mcg_context *ctx, const mcg_volume *vol, cudaStream_t s);
+}  // namespace mcg
 
 // true while `s` is being captured into a CUDA graph
 inline bool mcg_capturing(cudaStream_t s) {
