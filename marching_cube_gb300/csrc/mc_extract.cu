@@ -33,8 +33,8 @@
 // lines.  The three launches chain with programmatic dependent launch.
 //
 // When TMA cannot describe the volume (x row not a multiple of 16 bytes or an
-// unaligned base) the same kernels fill the tiles with per-voxel cp.async
-// copies.
+// unaligned base) the same kernels fill the tiles by 16-byte words of the
+// volume shifted into place (fill_tile).
 //
 // Output order is deterministic: bricks in (bz, by, bx) order, cubes in
 // (z, y, x) order inside a brick, then the table slot -- the reference's
@@ -498,8 +498,8 @@ __global__ void __launch_bounds__(NT)
 // Bricks of all volumes of a batch form one index space: volume v owns bricks
 // [brick_base, brick_base + nbricks).  A brick's volume is found by binary
 // search over the descriptor table; tiles come by TMA through the volume's
-// own tensor map (global memory) when TMA can describe it, by asynchronous
-// per-voxel copies otherwise.  Soup offsets come from one scan over all
+// own tensor map (global memory) when TMA can describe it, by 16-byte words
+// shifted into place otherwise (fill_tile).  Soup offsets come from one scan over all
 // bricks; a volume's soup starts at the offset of its first brick, i.e. 3x
 // the triangles of the volumes before it.
 struct VolDesc {
@@ -1888,9 +1888,9 @@ __device__ __forceinline__ void issue_cls_tile(ClsSmemMulti<VT> &S, int s, const
 }
 
 // Count pass over all volumes of a batch, one brick per work item, bricks a
-// fixed stride apart per CTA, 2 tile stages: TMA volumes load by TMA, the
-// others by asynchronous per-voxel copies (one copy group per iteration), so
-// in both cases the next tile loads while the current one is classified.
+// fixed stride apart per CTA, 2 tile stages: TMA volumes load by TMA, so the
+// next tile loads while the current one is classified; the others are
+// filled by 16-byte words (fill_tile) when their stage is refilled.
 template <int VT>
 __global__ void __launch_bounds__(CTHREADS)
     mc_classify_multi_kernel(const VolDesc *__restrict__ vols, const CUtensorMap *maps, int nvol, long long nbricks,
