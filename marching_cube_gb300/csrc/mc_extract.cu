@@ -1851,8 +1851,10 @@ struct ClsSmemMulti {
     int svol[2];
     int stma[2];
     int4 spos[2];  // origin of each stage's brick
+    long long sb[2];  // brick of each stage, -1: none
     int4 nxt;      // the brick refilled at the end of this iteration: {volume, TMA, origin x, y}
     int nxt_z;
+    long long nxt_b;  // its brick id, or -1
     int abort;
 };
 
@@ -1887,37 +1889,43 @@ __device__ __forceinline__ void issue_cls_tile(ClsSmemMulti<VT> &S, int s, const
     }
 }
 
-// Count pass over all volumes of a batch, one brick per work item, bricks a
-// fixed stride apart per CTA, 2 tile stages: TMA volumes load by TMA, so the
-// next tile loads while the current one is classified; the others are
-// filled by 16-byte words (fill_tile) when their stage is refilled.
+// Count pass over all volumes of a batch, one brick per work item, bricks
+// drawn from a counter (`ticket`, zero at launch) so that CTAs whose bricks
+// were cheap take more, 2 tile stages: TMA volumes load by TMA, so the next
+// tile loads while the current one is classified; the others are filled by
+// 16-byte words (fill_tile) when their stage is refilled.  Thread 0 draws
+// each refill's ticket one brick before it is used, so no CTA waits on the
+// counter.
 template <int VT>
 __global__ void __launch_bounds__(CTHREADS)
     mc_classify_multi_kernel(const VolDesc *__restrict__ vols, const CUtensorMap *maps, int nvol, long long nbricks,
                              uint32_t *__restrict__ brick_tris, uint32_t *__restrict__ chunk,
-                             unsigned long long *__restrict__ vol_sums, unsigned int *__restrict__ flags) {
+                             unsigned long long *__restrict__ vol_sums, unsigned int *__restrict__ flags,
+                             unsigned int *__restrict__ ticket) {
     using V = Vox<VT>;
     using T = typename V::T;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     ClsSmemMulti<VT> &S = *reinterpret_cast<ClsSmemMulti<VT> *>(smem_raw);
     const int tid = threadIdx.x;
-    const long long stride = gridDim.x;
     uint32_t phase[2] = {0, 0};
     VolCache vc;
+    long long pend = -1;  // thread 0: the brick of the next refill
     for (int c = tid; c < 256; c += CTHREADS) S.ntri[c] = (c == 0 || c == 255) ? 0 : g_nverts[c] / 3;
     if (tid == 0) {
         S.abort = 0;
         for (int s = 0; s < 2; ++s) mbar_init(&S.bars[s], 1);
         fence_barrier_init();
         for (int s = 0; s < 2; ++s) {
-            const long long b = blockIdx.x + s * stride;
+            const long long b = (long long)atomicAdd(ticket, 1u);
+            S.sb[s] = b < nbricks ? b : -1ll;
             if (b < nbricks) issue_cls_tile<VT>(S, s, vols, nvol, maps, b, vc);
         }
+        pend = (long long)atomicAdd(ticket, 1u);
     }
     __syncthreads();
     // the plain-copy fills of the first two stages, one copy group each
     for (int s = 0; s < 2; ++s) {
-        if (blockIdx.x + s * stride < nbricks && !S.stma[s]) {
+        if (S.sb[s] >= 0 && !S.stma[s]) {
             const VolDesc &d = vols[S.svol[s]];
             fill_tile<VT, CTX, CTY, CTZ, false>(reinterpret_cast<T *>(S.tiles[s]), static_cast<const T *>(d.data),
                                                 d.nx, d.ny, d.nz, S.spos[s].x, S.spos[s].y, S.spos[s].z);
@@ -1925,9 +1933,10 @@ __global__ void __launch_bounds__(CTHREADS)
         cp_async_commit();
     }
     for (int i = 0;; ++i) {
-        const long long b = blockIdx.x + (long long)i * stride;
-        if (b >= nbricks) break;
         const int s = i & 1;
+        // written by thread 0 two iterations back, barriers in between
+        const long long b = S.sb[s];
+        if (b < 0) break;  // uniform; tickets go to the stages in processing order
         T *tile = reinterpret_cast<T *>(S.tiles[s]);
         const int v = S.svol[s];
         const VolDesc &d = vols[v];
@@ -1947,21 +1956,27 @@ __global__ void __launch_bounds__(CTHREADS)
         __syncthreads();
         if (S.abort) break;
         // the brick that refills this stage: resolved by thread 0 now, read by
-        // all after the barrier in tile_mixed
-        const long long nb = b + 2 * stride;
-        if (tid == 0 && nb < nbricks) {
-            const int nv = cached_volume(vc, vols, nvol, nb);
-            const BrickPos np = brick_pos(nb - vc.base, vols[nv].nbx, vols[nv].nby);
-            S.nxt = make_int4(nv, vols[nv].tma, np.x0, np.y0);
-            S.nxt_z = np.z0;
+        // all after the barrier in tile_mixed; the ticket after it is drawn now
+        // and used at the next refill
+        if (tid == 0) {
+            const long long nbt = pend < nbricks ? pend : -1ll;
+            S.nxt_b = nbt;
+            if (nbt >= 0) {
+                const int nv = cached_volume(vc, vols, nvol, nbt);
+                const BrickPos np = brick_pos(nbt - vc.base, vols[nv].nbx, vols[nv].nby);
+                S.nxt = make_int4(nv, vols[nv].tma, np.x0, np.y0);
+                S.nxt_z = np.z0;
+                pend = (long long)atomicAdd(ticket, 1u);
+            }
         }
         const bool mixed = tile_mixed<VT>(S, tile);
+        const long long nb = S.nxt_b;
         if (mixed) {
             classify_brick<VT>(S, tile, d.nx, d.ny, d.nz, bp);
             __syncthreads();  // tile s consumed, red[] complete
         }
         // tile s is free: refill it
-        if (nb < nbricks) {
+        if (nb >= 0) {
             const int4 nx4 = S.nxt;
             const int nz0 = S.nxt_z;
             if (nx4.y) {
@@ -1993,7 +2008,8 @@ __global__ void __launch_bounds__(CTHREADS)
                 atomicAdd(&vol_sums[2 * v + 0], (unsigned long long)t);
                 atomicAdd(&vol_sums[2 * v + 1], (unsigned long long)o);
             }
-            if (nb < nbricks) {
+            S.sb[s] = nb;
+            if (nb >= 0) {
                 S.svol[s] = S.nxt.x;
                 S.stma[s] = S.nxt.y;
                 S.spos[s] = make_int4(S.nxt.z, S.nxt.w, S.nxt_z, 0);
@@ -2716,13 +2732,14 @@ mcg_status mcg_mc_backward(mcg_context *ctx, const mcg_volume *vol, const float 
     return e == cudaSuccess ? MCG_OK : mcg_cuda_fail(ctx, e);
 }
 
-// Zeroes what a batch's count launch accumulates into: the flags, the
-// generate counter, the per-volume sums and the chunk sums.
+// Zeroes what a batch's count launch accumulates into: the flags, the count
+// and generate counters, the per-volume sums and the chunk sums.
 __global__ void mc_batch_reset_kernel(MeshTotals *totals, unsigned long long *__restrict__ vol_sums, int nvol,
                                       uint32_t *__restrict__ chunk, long long nchunk_words) {
     const long long i0 = (long long)blockIdx.x * blockDim.x + threadIdx.x, st = (long long)gridDim.x * blockDim.x;
     if (i0 == 0) {
         totals->flags = 0;
+        totals->cls_ticket = 0;
         totals->gen_ticket = 0;
     }
     for (long long i = i0; i < 2LL * nvol; i += st) vol_sums[i] = 0;
@@ -2878,7 +2895,7 @@ void launch_classify_multi(mcg_context *ctx, int nvol, long long nbricks, cudaSt
     const CUtensorMap *cmaps = reinterpret_cast<const CUtensorMap *>(ctx->d_btab + btab_desc_bytes(nvol));
     mc_classify_multi_kernel<VT><<<(int)grid, CTHREADS, smem, s>>>(desc, cmaps, nvol, nbricks, ctx->brick_tris,
                                                                     ctx->brick_occ, ctx->d_vol_sums,
-                                                                    &ctx->d_totals->flags);
+                                                                    &ctx->d_totals->flags, &ctx->d_totals->cls_ticket);
 }
 
 // generate launch of a batch, chained to the batch's scan (programmatic
