@@ -246,7 +246,7 @@ def bench_full_outputs(mcg, torch, lib, ctx, vol, cell, nvert, stream, steps=50)
             "bytes_out_per_step": nvert * (28 + 12 + 12) + 2 * vox * 2}
 
 
-def bench_batched(mcg, synthetic, torch, ctx, n=64, reps=10):
+def bench_batched(mcg, synthetic, torch, ctx, n=64, reps=30):
     """64 volumes, each axis log-uniform in [32, 256], 1-8 spheres/boxes:
     one batched extraction vs a loop of single-volume extractions (both
     asynchronous, into preallocated soup + normal buffers)."""
@@ -269,7 +269,7 @@ def bench_batched(mcg, synthetic, torch, ctx, n=64, reps=10):
 
     res = {}
     for name, fn in (("loop", loop), ("batched", batch)):
-        for _ in range(3):
+        for _ in range(5):
             fn()
         torch.cuda.synchronize()
         e0.record()

@@ -555,6 +555,7 @@ struct ScanBatch {
     int nvol;
     const unsigned long long *vol_sums;  // {triangles, occupied cubes} per volume
     BatchBrick *list;                    // one entry per active-list entry
+    unsigned long long *host_vol_sums;   // mapped host copy of vol_sums (written by CTA 0), or null
 };
 
 template <bool BATCH>
@@ -635,6 +636,10 @@ __global__ void __launch_bounds__(CHUNK)
         }
     }
     __syncthreads();
+    if (BATCH && j == 0 && bt.host_vol_sums) {
+        for (int i = tid; i < 2 * bt.nvol; i += CHUNK) bt.host_vol_sums[i] = bt.vol_sums[i];
+        __threadfence_system();
+    }
     // BATCH: the soup start of each volume this chunk's bricks lie in (at
     // most CHUNK volumes, each owning at least one brick): 3x the triangles
     // of the volumes before it
@@ -2052,7 +2057,7 @@ __device__ __forceinline__ void issue_gen_tile(GenSmemMulti<VT> &S, int s, const
 template <int VT>
 __global__ void __launch_bounds__(THREADS, 4)
     mc_generate_multi_kernel(const VolDesc *__restrict__ vols, const CUtensorMap *maps, int nvol,
-                             const BatchBrick *__restrict__ list, MeshTotals *totals) {
+                             const BatchBrick *__restrict__ list, MeshTotals *totals, MeshTotals *host) {
     using V = Vox<VT>;
     using T = typename V::T;
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -2137,6 +2142,19 @@ __global__ void __launch_bounds__(THREADS, 4)
     if (S.abort && tid == 0) {
         atomicOr(&totals->flags, 1u);
         for (int s = 0; s < 2; ++s) mbar_wait(&S.bars[s], phase[s], 100000000ull);
+    }
+    // the last CTA out folds the flags into the mapped host copy, where the
+    // batch's scan put the count launch's
+    if (tid == 0) {
+        __threadfence();
+        if (atomicAdd(&totals->gen_exit, 1u) == gridDim.x - 1) {
+            totals->gen_exit = 0;
+            if (host) {
+                host->flags |= *(volatile unsigned int *)&totals->flags;
+                totals->flags = 0;
+                __threadfence_system();
+            }
+        }
     }
 }
 
@@ -2884,6 +2902,12 @@ mcg_status upload_btab(mcg_context *ctx, const mcg_volume *vols, const mcg_mesh_
     return MCG_OK;
 }
 
+// The mapped host copy of the totals when the batch's counts can reach the
+// host without copies (the per-volume sums mapped too), else null.
+MeshTotals *batch_host(mcg_context *ctx) {
+    return ctx->h_totals_dev && ctx->h_vol_sums_dev ? ctx->h_totals_dev : nullptr;
+}
+
 template <int VT>
 void launch_classify_multi(mcg_context *ctx, int nvol, long long nbricks, cudaStream_t s) {
     const size_t smem = sizeof(ClsSmemMulti<VT>);
@@ -2911,7 +2935,7 @@ cudaError_t launch_generate_multi(mcg_context *ctx, int nvol, long long nbricks,
     if (grid > nbricks) grid = nbricks;
     const CUtensorMap *gmaps = reinterpret_cast<const CUtensorMap *>(ctx->d_btab + btab_desc_bytes(nvol)) + nvol;
     return launch_pdl(mc_generate_multi_kernel<VT>, (unsigned int)grid, THREADS, smem, s, desc, gmaps, nvol, list,
-                      ctx->d_totals);
+                      ctx->d_totals, batch_host(ctx));
 }
 
 // Bricks of a batch, or -1 when a volume or the sum is out of range.
@@ -2943,9 +2967,17 @@ mcg_status batch_scratch(mcg_context *ctx, int32_t nvol, long long nbricks, cuda
         if (ctx->h_vol_sums) cudaFreeHost(ctx->h_vol_sums);
         ctx->h_vol_sums = nullptr;
         ctx->h_vol_sums_cap = 0;
-        if (cudaMallocHost((void **)&ctx->h_vol_sums, sizeof(unsigned long long) * 2 * nvol) != cudaSuccess)
+        ctx->h_vol_sums_dev = nullptr;
+        if (cudaHostAlloc((void **)&ctx->h_vol_sums, sizeof(unsigned long long) * 2 * nvol,
+                          cudaHostAllocMapped | cudaHostAllocPortable) != cudaSuccess)
             return mcg_cuda_fail(ctx, cudaErrorMemoryAllocation);
         ctx->h_vol_sums_cap = 2 * nvol;
+        // the batch's scan writes the sums straight into host memory through
+        // this address; without one the host copies them
+        if (cudaHostGetDevicePointer((void **)&ctx->h_vol_sums_dev, ctx->h_vol_sums, 0) != cudaSuccess) {
+            cudaGetLastError();
+            ctx->h_vol_sums_dev = nullptr;
+        }
     }
     return MCG_OK;
 }
@@ -2961,20 +2993,25 @@ cudaError_t launch_batch_count(mcg_context *ctx, int32_t vtype, int32_t nvol, lo
     mc_batch_reset_kernel<<<(unsigned int)rg, 256, 0, s>>>(ctx->d_totals, ctx->d_vol_sums, nvol, ctx->brick_occ, cw);
     if (vtype == MCG_VOXEL_SHORT2) launch_classify_multi<MCG_VOXEL_SHORT2>(ctx, nvol, nbricks, s);
     else launch_classify_multi<MCG_VOXEL_FLOAT2>(ctx, nvol, nbricks, s);
+    MeshTotals *host = batch_host(ctx);
     const ScanBatch bt{reinterpret_cast<const VolDesc *>(ctx->d_btab), nvol, ctx->d_vol_sums,
-                       reinterpret_cast<BatchBrick *>(ctx->batch_list)};
+                       reinterpret_cast<BatchBrick *>(ctx->batch_list), host ? ctx->h_vol_sums_dev : nullptr};
     launch_pdl(mc_scan_kernel<true>, (unsigned int)num_chunks(nbricks), CHUNK, 0, s, (const uint32_t *)ctx->brick_tris,
                ctx->brick_occ, nbricks, ctx->brick_vofs, ctx->active, (unsigned long long *)nullptr, ctx->d_totals,
-               (MeshTotals *)nullptr, bt);
+               host, bt);
     return cudaGetLastError();
 }
 
-// the totals and per-volume sums to the host copies, marked pending
+// the totals and per-volume sums in the host copies, marked pending: written
+// there by the kernels when mapped, copied otherwise
 cudaError_t batch_counts_out(mcg_context *ctx, int32_t nvol, cudaStream_t s) {
-    cudaError_t e = cudaMemcpyAsync(ctx->h_totals, ctx->d_totals, sizeof(MeshTotals), cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(ctx->h_vol_sums, ctx->d_vol_sums, sizeof(unsigned long long) * 2 * nvol,
-                            cudaMemcpyDeviceToHost, s);
+    cudaError_t e = cudaSuccess;
+    if (!batch_host(ctx)) {
+        e = cudaMemcpyAsync(ctx->h_totals, ctx->d_totals, sizeof(MeshTotals), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(ctx->h_vol_sums, ctx->d_vol_sums, sizeof(unsigned long long) * 2 * nvol,
+                                cudaMemcpyDeviceToHost, s);
+    }
     if (e == cudaSuccess) e = mcg_counts_event(ctx, s);
     return e;
 }
@@ -3069,7 +3106,7 @@ mcg_status mcg_mc_generate_batched(mcg_context *ctx, const mcg_volume *vols, con
     if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);
     if (vols[0].voxel_type == MCG_VOXEL_SHORT2) e = launch_generate_multi<MCG_VOXEL_SHORT2>(ctx, nvol, total, s);
     else e = launch_generate_multi<MCG_VOXEL_FLOAT2>(ctx, nvol, total, s);
-    if (e == cudaSuccess)
+    if (e == cudaSuccess && !batch_host(ctx))
         e = cudaMemcpyAsync(ctx->h_totals, ctx->d_totals, sizeof(MeshTotals), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = mcg_counts_event(ctx, s);
     if (e != cudaSuccess) return mcg_cuda_fail(ctx, e);

@@ -129,7 +129,8 @@ struct mcg_context {
     size_t batch_tma_cap = 0;
     unsigned long long *d_vol_sums = nullptr;
     size_t d_vol_sums_cap = 0;
-    unsigned long long *h_vol_sums = nullptr;  // pinned
+    unsigned long long *h_vol_sums = nullptr;  // pinned, mapped
+    unsigned long long *h_vol_sums_dev = nullptr;  // its device address; null if it has none
     size_t h_vol_sums_cap = 0;
     int batch_nvol = 0;
     long long batch_nbricks = 0;
