@@ -82,6 +82,19 @@ def test_max_tsdf_quirk_and_border_reads(orc):
     _same_extract(orc.mc_extract(vol, 0.3), ref.mc_extract(vol, 0.3))
 
 
+def test_batch_volumes_match_reference(orc):
+    # every eighth volume of the 64-volume batch set (each axis log-uniform
+    # in 32..256, spheres and boxes), every output
+    vols = synthetic.batch_volumes(64, seed=7, lo=32, hi=256, device="cpu")
+    total = 0
+    for i in range(0, 64, 8):
+        v = vols[i].numpy()
+        r = ref.mc_extract(v, 0.01)
+        total += len(r["soup"])
+        _same_extract(orc.mc_extract(v, 0.01), r)
+    assert total > 100000
+
+
 def test_fused_volume_extraction_matches_reference(orc):
     vol, cell = _fused(orc, 96, 4, seed=5)
     r = ref.mc_extract(vol, cell)
